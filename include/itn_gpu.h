@@ -1,0 +1,154 @@
+/*
+ * itn_gpu.h -- C ABI of libitn_gpu.so, the GB300 (sm_103a) belief-propagation and
+ * network-contraction engine behind ITensorNetworksNext.jl's hot path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int32 status
+ * (ITN_OK = 0) and never aborts; on failure itn_last_error(ctx) holds a message.
+ * A context owns one CUDA stream and all device buffers it allocates; calls are
+ * synchronous at return.  A context is not thread-safe; separate contexts may be
+ * used from separate threads.
+ *
+ * Data model (shared by every call).  A network of nv vertices is a CSR adjacency:
+ *   vertex u owns leg slots csr_off[u] .. csr_off[u+1]-1; slot s is the directed edge
+ *   u -> csr_nbr[s] with bond dimension bond[s]; rev[s] is the slot of the opposite
+ *   direction.  All link indices shared by one pair of vertices form one leg (their
+ *   dimensions multiply), exactly as linknames() intersects dim names in the reference
+ *   (src/abstracttensornetwork.jl:52-73).
+ *   Site tensor of u: row-major [phys][leg_0]...[leg_{z-1}] ("canonical" layout), the
+ *   tensors of all vertices packed back to back in vertex order.
+ *   Message on slot s: layers == 2 (norm network <psi|psi>): D x D row-major
+ *   m[bra][ket] (message_environment, src/beliefpropagation/messagecache.jl:205-229);
+ *   layers == 1 (plain network): a length-D vector.  Packed in slot order.
+ *
+ * Paths below are relative to the ITensorNetworksNext.jl source tree.
+ */
+#ifndef ITN_GPU_H
+#define ITN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ITN_ABI_VERSION 1
+
+enum {
+  ITN_OK = 0,
+  ITN_ERR_ARG = 1,         /* bad argument: maps to ArgumentError in the Julia shim */
+  ITN_ERR_CUDA = 2,        /* CUDA runtime failure */
+  ITN_ERR_OOM = 3,         /* device allocation failed */
+  ITN_ERR_NAN = 4,         /* NaN/Inf met where a finite value is required */
+  ITN_ERR_TIMEOUT = 5,     /* iteration cap reached without meeting the tolerance */
+  ITN_ERR_UNSUPPORTED = 6, /* shape / dtype / precision combination not implemented */
+  ITN_ERR_STATE = 7        /* call order violated (e.g. run before upload) */
+};
+
+enum { ITN_F32 = 0, ITN_F64 = 1, ITN_C64 = 2, ITN_C128 = 3 };
+enum { ITN_SCHED_PARALLEL = 0, ITN_SCHED_SEQUENTIAL = 1 };
+/* ITN_PREC_NATIVE: arithmetic in the stored dtype on CUDA cores.
+ * ITN_PREC_BF16 / ITN_PREC_TF32: tensor-core (tcgen05) contractions with FP32
+ * accumulation for all but the last split_sweeps sweeps, which run in split
+ * (hi/lo) precision; requires ITN_F32 storage. */
+enum { ITN_PREC_NATIVE = 0, ITN_PREC_BF16 = 1, ITN_PREC_TF32 = 2 };
+enum { ITN_MSG_IDENTITY_NORMALIZED = 0, ITN_MSG_IDENTITY = 1, ITN_MSG_ONES = 2 };
+
+typedef struct itn_ctx itn_ctx;
+
+typedef struct {
+  int32_t schedule;      /* ITN_SCHED_* */
+  int32_t maxiter;       /* StopAfterIteration(maxiter); < 0 = not given */
+  double tol;            /* StopWhenConverged(tol); < 0 = not given */
+  int32_t normalize;     /* SimpleMessageUpdate(normalize) */
+  int32_t precision;     /* ITN_PREC_* */
+  int32_t split_sweeps;  /* final sweeps in split precision (tensor-core modes) */
+  int32_t reserved0;
+  const int64_t *edges;  /* sequential schedule: directed slots, in sweep order */
+  int64_t n_edges;
+} itn_bp_opts;
+
+typedef struct {
+  int32_t iterations;    /* outer iterations (sweeps) performed */
+  int32_t at_iteration;  /* StopWhenConvergedState.at_iteration (-1 if not converged) */
+  double delta;          /* last iterate_diff value (Inf if never computed) */
+  double device_ms;      /* device time of the sweeps (CUDA events on the ctx stream) */
+  int32_t kernel_launches; /* kernels launched by this call */
+  int32_t reserved0;
+} itn_bp_result;
+
+/* Library/ABI identification. */
+int32_t itn_abi_version(void);
+const char *itn_status_string(int32_t status);
+
+/* Context life cycle.  Replaces nothing in the reference (it has no device state);
+ * the Julia shim creates one per GPU strategy object. */
+int32_t itn_create(itn_ctx **out, int32_t device, int32_t flags);
+int32_t itn_destroy(itn_ctx *ctx);
+const char *itn_last_error(const itn_ctx *ctx);
+int32_t itn_synchronize(itn_ctx *ctx);
+
+/* Network structure.  Replaces the graph bookkeeping the reference derives from
+ * shared dim names: ITensorNetwork / set!_tensornetwork (src/tensornetwork.jl:21-48,
+ * 138-173), linkinds/siteinds (src/abstracttensornetwork.jl:52-95) and the directed
+ * edge set of MessageCache (src/beliefpropagation/messagecache.jl:15-49).
+ * rev may be NULL (computed by pairing the k-th u->w slot with the k-th w->u slot);
+ * phys may be NULL (all 1); net_id (network of each vertex, for batches of
+ * independent networks) may be NULL (one network).  layers: 1 = plain network
+ * (factors are the tensors), 2 = norm network (factor = A * conj(A) with the site
+ * index shared, src/normnetwork.jl:49-54). */
+int32_t itn_graph_upload(itn_ctx *ctx, int64_t nv, const int64_t *csr_off,
+                         const int64_t *csr_nbr, const int32_t *bond, const int64_t *rev,
+                         const int32_t *phys, int32_t layers, const int32_t *net_id);
+/* Sizes of the uploaded network. */
+int32_t itn_graph_info(const itn_ctx *ctx, int64_t *nv, int64_t *nslots, int64_t *tensor_elems,
+                       int64_t *message_elems, int32_t *n_nets, int64_t *n_undirected);
+
+/* Site tensors, canonical packed layout.  Replaces the per-vertex ket tensors of
+ * NormNetwork.ket / ITensorNetwork.tensors (src/normnetwork.jl:13-25). */
+int32_t itn_tensors_upload(itn_ctx *ctx, int32_t dtype, const void *packed);
+/* Site tensors in any strided layout (e.g. Julia column-major arrays with the
+ * ITensor's own index order): site_ptrs[u] points at vertex u's array and
+ * strides[(off)] lists, for vertex u, 1 + degree(u) element strides in canonical axis
+ * order (phys, leg_0, ...); a vertex without a site index uses stride 0 with phys 1.
+ * Strides of vertex u start at csr_off[u] + u.  Permuted on the device. */
+int32_t itn_tensors_upload_strided(itn_ctx *ctx, int32_t dtype, const void *const *site_ptrs,
+                                   const int64_t *strides);
+/* Site tensors back in canonical packed layout. */
+int32_t itn_tensors_download(itn_ctx *ctx, int32_t dtype, void *packed);
+
+/* Messages (MessageCache contents, src/beliefpropagation/messagecache.jl:15-49). */
+int32_t itn_messages_upload(itn_ctx *ctx, int32_t dtype, const void *packed);
+int32_t itn_messages_download(itn_ctx *ctx, int32_t dtype, void *packed);
+/* message_environment(f, nn) for f = one / ones, device side
+ * (src/beliefpropagation/messagecache.jl:205-229); kind = ITN_MSG_*. */
+int32_t itn_messages_init(itn_ctx *ctx, int32_t kind);
+
+/* beliefpropagation(factors, messages; edges, stopping_criterion,
+ * message_update_algorithm) (src/beliefpropagation/beliefpropagation.jl:69-92):
+ * runs the whole solve on the device on the uploaded messages, in place. */
+int32_t itn_bp_run(itn_ctx *ctx, const itn_bp_opts *opts, itn_bp_result *result);
+
+/* message_update!(SimpleMessageUpdate(normalize), cache, factors, edge)
+ * (src/beliefpropagation/beliefpropagation.jl:242-257) for the directed slot. */
+int32_t itn_message_update(itn_ctx *ctx, int64_t slot, int32_t normalize);
+
+/* AIE.iterate_diff(cache1, cache2) (src/beliefpropagation/beliefpropagation.jl:261-267)
+ * of two packed message sets with this context's layout, FP64 on the device. */
+int32_t itn_iterate_diff(itn_ctx *ctx, int32_t dtype, const void *m1, const void *m2,
+                         double *out);
+
+/* vertex_scalars / edge_scalars / bethe_free_energy
+ * (src/beliefpropagation/messagecache.jl:139-201) on the current messages.
+ * zv: nv raw scalars, ze: one per undirected edge (slot < rev[slot], slot order), both
+ * in the context dtype (may be NULL).  logzv / logze: (re, im) pairs in FP64 (may be
+ * NULL).  totals: (re, im) of sum log Zv - sum log Ze per network.  flags per network:
+ * bit0 any Re Zv < 0, bit1 any Re Ze < 0, bit2 any Ze == 0 (bethe_free_energy returns
+ * -Inf then). */
+int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *logze,
+                       double *totals, int32_t *flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ITN_GPU_H */

@@ -1,0 +1,753 @@
+// bp_generic.cu -- CUDA-core belief-propagation kernels for any graph, bond dimensions
+// and element type (float, double, complex64, complex128).
+//
+// Two-layer (norm network) message update, reference semantics
+// (src/beliefpropagation/beliefpropagation.jl:242-257 with the factor of
+// src/normnetwork.jl:49-54):
+//   m_{u->v}[b, k] = sum A_u[s, k_1..k_z] conj(A_u[s, b_1..b_z]) prod_{w != v} m_{w->u}[b_w, k_w]
+// with (b_v, k_v) = (b, k) left open, then m /= sum(m) unless the sum is zero.
+//
+// One CTA owns one vertex at a time (persistent loop over work items).  The vertex's
+// site tensor and its incoming messages are staged in shared memory and an op-program
+// built on the host is interpreted:
+//   ABSORB(src, dst, w): dst[o][b][i] = sum_k src[o][k][i] * m_w[b][k]   (ket leg w -> bra)
+//   FINAL(src, v)      : out[b][k] = sum_{o,i} src[o][k][i] * conj(A[o][b][i]), normalise, store
+//   FULL(src)          : Z_u = sum_j src[j] * conj(A[j])  (vertex_scalar, messagecache.jl:139-143)
+// The host program absorbs legs in a leave-one-out binary split, so the z outgoing
+// messages of a vertex share partial products (8 absorptions instead of 12 at z = 4).
+//
+// One-layer networks (plain ITensorNetwork factors, vector messages) use a direct
+// per-entry kernel; they are small known-answer cases (spin ice, Ising, trees).
+#include <math.h>
+#include <string.h>
+
+#include "itn_common.cuh"
+#include "itn_internal.h"
+
+namespace itn {
+
+namespace {
+
+constexpr int kRedWidth = 64;  // per-warp partial-sum slots for D*D <= 64
+
+struct LegMeta {
+  int z, d, n;          // legs, physical dim, tensor elements
+  int dims[kMaxLegs];
+  int inner[kMaxLegs];  // prod of dims after the leg
+  int outer[kMaxLegs];  // d * prod of dims before the leg
+  int moffs[kMaxLegs];  // offset of the leg's incoming message in shared staging
+};
+
+// ---- warp reduce-scatter of NV (power of two) values -------------------------------
+// After the call, lane holds in v[j] (j < max(NV/32, 1)) the warp sum of index base+j.
+template <typename T, int NV, int STEP>
+__device__ __forceinline__ void rs_step(T (&v)[NV], int lane, int& base) {
+  if constexpr (STEP < 5) {
+    constexpr int off = 16 >> STEP;
+    constexpr int cnt = NV >> (STEP + 1);
+    if constexpr (cnt >= 1) {
+      const bool up = (lane & off) != 0;
+#pragma unroll
+      for (int j = 0; j < cnt; ++j) {
+        T send = up ? v[j] : v[j + cnt];
+        T keep = up ? v[j + cnt] : v[j];
+        v[j] = add(keep, shfl_xor(send, off));
+      }
+      if (up) base += cnt;
+    } else {
+      v[0] = add(v[0], shfl_xor(v[0], off));
+    }
+    rs_step<T, NV, STEP + 1>(v, lane, base);
+  }
+}
+
+template <int D> struct Pow2Of { static constexpr int v = (D * D <= 1) ? 1 : (D * D <= 2) ? 2 : (D * D <= 4) ? 4 : (D * D <= 8) ? 8 : (D * D <= 16) ? 16 : (D * D <= 32) ? 32 : 64; };
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v = add(v, shfl_xor(v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one value; result valid in every thread.  red needs nwarps slots.
+template <typename T>
+__device__ T block_sum(T v, T* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T r = tzero<T>();
+  for (int w = 0; w < nw; ++w) r = add(r, red[w]);
+  __syncthreads();
+  return r;
+}
+
+// ---- ABSORB with compile-time bond dimension ---------------------------------------
+template <typename T, int D>
+__device__ __forceinline__ void absorb_fixed(const T* __restrict__ src, T* __restrict__ dst,
+                                             int outer, int inner, const T* __restrict__ m) {
+  T mr[D * D];
+#pragma unroll
+  for (int j = 0; j < D * D; ++j) mr[j] = m[j];
+  const int n = outer * inner;
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    const int o = p / inner, i = p - o * inner;
+    const T* s = src + o * D * inner + i;
+    T t[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) t[k] = s[k * inner];
+    T* dd = dst + o * D * inner + i;
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      T acc = mul(t[0], mr[b * D]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) acc = fmac(t[k], mr[b * D + k], acc);
+      dd[b * inner] = acc;
+    }
+  }
+}
+
+template <typename T>
+__device__ void absorb_rt(const T* __restrict__ src, T* __restrict__ dst, int outer, int D,
+                          int inner, const T* __restrict__ m) {
+  const int n = outer * inner;
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    const int o = p / inner, i = p - o * inner;
+    const T* s = src + o * D * inner + i;
+    T* dd = dst + o * D * inner + i;
+    for (int b = 0; b < D; ++b) {
+      T acc = tzero<T>();
+      for (int k = 0; k < D; ++k) acc = fmac(s[k * inner], m[b * D + k], acc);
+      dd[b * inner] = acc;
+    }
+  }
+}
+
+// ---- FINAL with compile-time bond dimension: out[b][k] -------------------------------
+template <typename T, int D>
+__device__ __forceinline__ void final_fixed(const T* __restrict__ src, const T* __restrict__ A,
+                                            int outer, int inner, T* __restrict__ out,
+                                            T* __restrict__ red) {
+  constexpr int NV = Pow2Of<D>::v;
+  T acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) acc[j] = tzero<T>();
+  const int n = outer * inner;
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    const int o = p / inner, i = p - o * inner;
+    const T* s = src + o * D * inner + i;
+    const T* a = A + o * D * inner + i;
+    T t[D], c[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) t[k] = s[k * inner];
+#pragma unroll
+    for (int b = 0; b < D; ++b) c[b] = conjx(a[b * inner]);
+#pragma unroll
+    for (int b = 0; b < D; ++b)
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc[b * D + k] = fmac(t[k], c[b], acc[b * D + k]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int base = 0;
+  rs_step<T, NV, 0>(acc, lane, base);
+  constexpr int keep = NV >= 32 ? NV / 32 : 1;
+#pragma unroll
+  for (int j = 0; j < keep; ++j) red[warp * kRedWidth + base + j] = acc[j];
+  __syncthreads();
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    T r = tzero<T>();
+    for (int w = 0; w < nw; ++w) r = add(r, red[w * kRedWidth + e]);
+    out[e] = r;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void final_rt(const T* __restrict__ src, const T* __restrict__ A, int outer, int D,
+                         int inner, T* __restrict__ out, T* __restrict__ red) {
+  const int n = outer * inner;
+  for (int e = 0; e < D * D; ++e) {
+    const int b = e / D, k = e - b * D;
+    T acc = tzero<T>();
+    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+      const int o = p / inner, i = p - o * inner;
+      acc = fmac(src[(o * D + k) * inner + i], conjx(A[(o * D + b) * inner + i]), acc);
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) out[e] = acc;
+  }
+  __syncthreads();
+}
+
+// Normalise out (D*D entries in shared memory) by its sum, store it to global memory
+// and, when requested, record the convergence value against the previous message.
+// Executed by warp 0.
+template <typename T>
+__device__ void store_message(const GenericArgs& a, const T* out, int n, int slot) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
+  T s = tzero<T>();
+  for (int j = lane; j < n; j += 32) s = add(s, out[j]);
+  s = warp_sum(s);
+  const bool scale = a.normalize && !is_zero(s);
+  T* dst = reinterpret_cast<T*>(a.msg_out) + a.moff[slot];
+  const T* old = reinterpret_cast<const T*>(a.msg_in) + a.moff[slot];
+  double n1 = 0, n2 = 0, dre = 0, dim = 0;
+  for (int j = lane; j < n; j += 32) {
+    T v = scale ? divx(out[j], s) : out[j];
+    if (a.slot_diff) {
+      T ov = old[j];
+      const double vr = re_d(v), vi = im_d(v), orr = re_d(ov), oi = im_d(ov);
+      n1 += vr * vr + vi * vi;
+      n2 += orr * orr + oi * oi;
+      dre += vr * orr + vi * oi;   // conj(v) * ov
+      dim += vr * oi - vi * orr;
+    }
+    dst[j] = v;
+  }
+  if (a.slot_diff) {
+    n1 = warp_sum_d(n1);
+    n2 = warp_sum_d(n2);
+    dre = warp_sum_d(dre);
+    dim = warp_sum_d(dim);
+    if (lane == 0) {
+      const double val = 1.0 - (dre * dre + dim * dim) / (n1 * n2);
+      a.slot_diff[slot] = val;
+      if (val != val) {
+        if (a.nan_flag) atomicExch(a.nan_flag, 1);
+      } else if (a.diff_max) {
+        atomicMax(a.diff_max, enc_double(val));
+      }
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dispatch_absorb(const T* src, T* dst, int outer, int D, int inner,
+                                                const T* m) {
+  switch (D) {
+    case 1: absorb_fixed<T, 1>(src, dst, outer, inner, m); break;
+    case 2: absorb_fixed<T, 2>(src, dst, outer, inner, m); break;
+    case 3: absorb_fixed<T, 3>(src, dst, outer, inner, m); break;
+    case 4: absorb_fixed<T, 4>(src, dst, outer, inner, m); break;
+    case 5: absorb_fixed<T, 5>(src, dst, outer, inner, m); break;
+    case 6: absorb_fixed<T, 6>(src, dst, outer, inner, m); break;
+    case 7: absorb_fixed<T, 7>(src, dst, outer, inner, m); break;
+    case 8: absorb_fixed<T, 8>(src, dst, outer, inner, m); break;
+    default: absorb_rt<T>(src, dst, outer, D, inner, m); break;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dispatch_final(const T* src, const T* A, int outer, int D,
+                                               int inner, T* out, T* red) {
+  switch (D) {
+    case 1: final_fixed<T, 1>(src, A, outer, inner, out, red); break;
+    case 2: final_fixed<T, 2>(src, A, outer, inner, out, red); break;
+    case 3: final_fixed<T, 3>(src, A, outer, inner, out, red); break;
+    case 4: final_fixed<T, 4>(src, A, outer, inner, out, red); break;
+    case 5: final_fixed<T, 5>(src, A, outer, inner, out, red); break;
+    case 6: final_fixed<T, 6>(src, A, outer, inner, out, red); break;
+    case 7: final_fixed<T, 7>(src, A, outer, inner, out, red); break;
+    case 8: final_fixed<T, 8>(src, A, outer, inner, out, red); break;
+    default: final_rt<T>(src, A, outer, D, inner, out, red); break;
+  }
+}
+
+// Shared-memory carve-up (all regions 16-byte aligned).
+struct SmemLayout {
+  size_t bufs, msgs, out, red, meta, total;
+};
+template <typename T>
+__host__ __device__ inline SmemLayout smem_layout(const GenericArgs& a, int block, bool in_smem) {
+  auto up = [](size_t x) { return (x + 15) & ~size_t(15); };
+  SmemLayout L;
+  size_t o = 0;
+  L.bufs = o;
+  if (in_smem) o += up((size_t)a.nbuf * a.buf_elems * sizeof(T));
+  L.msgs = o;
+  o += up((size_t)a.msg_cap * sizeof(T));
+  L.out = o;
+  o += up((size_t)(a.max_d2 > 0 ? a.max_d2 : 1) * sizeof(T));
+  L.red = o;
+  o += up((size_t)(block / 32) * kRedWidth * sizeof(T));
+  L.meta = o;
+  o += up(sizeof(LegMeta));
+  L.total = o;
+  return L;
+}
+
+// ---- the two-layer interpreter ---------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SmemLayout L = smem_layout<T>(a, blockDim.x, a.gscratch == nullptr);
+  T* bufs = a.gscratch ? reinterpret_cast<T*>(a.gscratch) + (size_t)blockIdx.x * a.nbuf * a.buf_elems
+                       : reinterpret_cast<T*>(smem + L.bufs);
+  T* msgs = reinterpret_cast<T*>(smem + L.msgs);
+  T* out = reinterpret_cast<T*>(smem + L.out);
+  T* red = reinterpret_cast<T*>(smem + L.red);
+  LegMeta* meta = reinterpret_cast<LegMeta*>(smem + L.meta);
+  const T* tens = reinterpret_cast<const T*>(a.tens);
+  const T* min_ = reinterpret_cast<const T*>(a.msg_in);
+
+  if (a.done && *reinterpret_cast<const volatile int*>(a.done)) return;
+
+  for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
+    const int u = a.items[2 * it];
+    const unsigned* prog = a.prog + a.items[2 * it + 1];
+    if (threadIdx.x == 0) {
+      const int s0 = a.off[u];
+      const int z = a.off[u + 1] - s0;
+      meta->z = z;
+      meta->d = a.phys[u];
+      int n = meta->d, mo = 0;
+      for (int l = 0; l < z; ++l) {
+        meta->dims[l] = a.bond[s0 + l];
+        n *= meta->dims[l];
+        meta->moffs[l] = mo;
+        mo += meta->dims[l] * meta->dims[l];
+      }
+      meta->n = n;
+      int inner = 1;
+      for (int l = z - 1; l >= 0; --l) {
+        meta->inner[l] = inner;
+        inner *= meta->dims[l];
+      }
+      for (int l = 0; l < z; ++l) meta->outer[l] = n / (meta->inner[l] * meta->dims[l]);
+    }
+    __syncthreads();
+    const int z = meta->z, n = meta->n;
+    // stage the site tensor (buffer 0) and the incoming messages m_{w->u}
+    const T* A_g = tens + a.toff[u];
+    T* A = bufs;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+    const int s0 = a.off[u];
+    for (int l = 0; l < z; ++l) {
+      const int D2 = meta->dims[l] * meta->dims[l];
+      const T* src = min_ + a.moff[a.rev[s0 + l]];
+      for (int j = threadIdx.x; j < D2; j += blockDim.x) msgs[meta->moffs[l] + j] = src[j];
+    }
+    __syncthreads();
+    const int nops = (int)prog[0];
+    for (int q = 1; q <= nops; ++q) {
+      const unsigned op = prog[q];
+      const int type = op >> 28, srcb = (op >> 20) & 0xff, dstb = (op >> 12) & 0xff,
+                leg = op & 0xfff;
+      const T* src = bufs + (size_t)srcb * a.buf_elems;
+      if (type == OP_ABSORB) {
+        T* dst = bufs + (size_t)dstb * a.buf_elems;
+        dispatch_absorb<T>(src, dst, meta->outer[leg], meta->dims[leg], meta->inner[leg],
+                           msgs + meta->moffs[leg]);
+        __syncthreads();
+      } else if (type == OP_FINAL) {
+        const int D = meta->dims[leg];
+        dispatch_final<T>(src, A, meta->outer[leg], D, meta->inner[leg], out, red);
+        store_message<T>(a, out, D * D, s0 + leg);
+        __syncthreads();
+      } else {  // OP_FULL
+        T acc = tzero<T>();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) acc = fmac(src[j], conjx(A[j]), acc);
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) reinterpret_cast<T*>(a.zv_out)[u] = acc;
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- the one-layer kernel ----------------------------------------------------------------
+// items: (vertex, leg mask); mask bit v set -> compute m_{u->v}; mask == 0 -> vertex scalar.
+template <typename T>
+__global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const SmemLayout L = smem_layout<T>(a, blockDim.x, false);
+  T* msgs = reinterpret_cast<T*>(smem + L.msgs);
+  T* out = reinterpret_cast<T*>(smem + L.out);
+  T* red = reinterpret_cast<T*>(smem + L.red);
+  LegMeta* meta = reinterpret_cast<LegMeta*>(smem + L.meta);
+  const T* tens = reinterpret_cast<const T*>(a.tens);
+  const T* min_ = reinterpret_cast<const T*>(a.msg_in);
+  if (a.done && *reinterpret_cast<const volatile int*>(a.done)) return;
+
+  for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
+    const int u = a.items[2 * it];
+    const unsigned mask = (unsigned)a.items[2 * it + 1];
+    if (threadIdx.x == 0) {
+      const int s0 = a.off[u];
+      const int z = a.off[u + 1] - s0;
+      meta->z = z;
+      meta->d = a.phys[u];
+      int n = meta->d, mo = 0;
+      for (int l = 0; l < z; ++l) {
+        meta->dims[l] = a.bond[s0 + l];
+        n *= meta->dims[l];
+        meta->moffs[l] = mo;
+        mo += meta->dims[l];
+      }
+      meta->n = n;
+      int inner = 1;
+      for (int l = z - 1; l >= 0; --l) {
+        meta->inner[l] = inner;
+        inner *= meta->dims[l];
+      }
+    }
+    __syncthreads();
+    const int z = meta->z, n = meta->n;
+    const int s0 = a.off[u];
+    for (int l = 0; l < z; ++l) {
+      const T* src = min_ + a.moff[a.rev[s0 + l]];
+      for (int j = threadIdx.x; j < meta->dims[l]; j += blockDim.x) msgs[meta->moffs[l] + j] = src[j];
+    }
+    __syncthreads();
+    const T* A = tens + a.toff[u];
+    if (mask == 0) {
+      T acc = tzero<T>();
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        T p = A[j];
+        for (int l = 0; l < z; ++l) {
+          const int kl = (j / meta->inner[l]) % meta->dims[l];
+          p = mul(p, msgs[meta->moffs[l] + kl]);
+        }
+        acc = add(acc, p);
+      }
+      acc = block_sum(acc, red);
+      if (threadIdx.x == 0) reinterpret_cast<T*>(a.zv_out)[u] = acc;
+      __syncthreads();
+      continue;
+    }
+    for (int v = 0; v < z; ++v) {
+      if (!((mask >> v) & 1u)) continue;
+      const int Dv = meta->dims[v];
+      const int innv = meta->inner[v];
+      const int nrest = n / Dv;
+      for (int k = 0; k < Dv; ++k) {
+        T acc = tzero<T>();
+        for (int r = threadIdx.x; r < nrest; r += blockDim.x) {
+          const int o = r / innv, i = r - o * innv;
+          const int j = (o * Dv + k) * innv + i;
+          T p = A[j];
+          for (int l = 0; l < z; ++l) {
+            if (l == v) continue;
+            const int kl = (j / meta->inner[l]) % meta->dims[l];
+            p = mul(p, msgs[meta->moffs[l] + kl]);
+          }
+          acc = add(acc, p);
+        }
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) out[k] = acc;
+      }
+      __syncthreads();
+      store_message<T>(a, out, Dv, s0 + v);
+      __syncthreads();
+    }
+  }
+}
+
+// ---- edge scalars: Z_e = sum_j m_{u->v}[j] * m_{v->u}[j]  (messagecache.jl:153-157) -----
+template <typename T>
+__global__ void edge_scalar_kernel(const long long* moff, const int* rev, const int* eslots,
+                                   int n_e, const T* msgs, T* ze) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n_e) return;
+  const int s = eslots[warp];
+  const T* x = msgs + moff[s];
+  const T* y = msgs + moff[rev[s]];
+  const int n = (int)(moff[s + 1] - moff[s]);
+  T acc = tzero<T>();
+  for (int j = lane; j < n; j += 32) acc = fmac(x[j], y[j], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) ze[warp] = acc;
+}
+
+// log of a scalar as (re, im) in double; real values promote like complex.(x) does in
+// bethe_free_energy (messagecache.jl:189-194).
+template <typename T>
+__device__ __forceinline__ void log2d(T z, double& re, double& im) {
+  const double a = re_d(z), b = im_d(z);
+  if constexpr (is_cplx<T>::value) {
+    re = 0.5 * log(a * a + b * b);
+    im = atan2(b, a);
+  } else {
+    if (a < 0) { re = log(-a); im = M_PI; }
+    else { re = log(a); im = 0.0; }
+  }
+}
+
+// One block per network: FP64 logs of vertex/edge scalars and the Bethe sum
+// log Z = sum_v log Z_v - sum_e log Z_e (messagecache.jl:185-201).
+// flags per net: bit0 any Re Z_v < 0, bit1 any Re Z_e < 0, bit2 any Z_e == 0.
+template <typename T>
+__global__ void logsum_kernel(const T* zv, const T* ze, const int* voff, const int* vlist,
+                              const int* eoff, const int* elist, double* logzv, double* logze,
+                              double* totals, int* flags) {
+  __shared__ double sre[32], sim[32];
+  __shared__ int sfl[32];
+  const int net = blockIdx.x;
+  double are = 0, aim = 0;
+  int fl = 0;
+  for (int j = voff[net] + threadIdx.x; j < voff[net + 1]; j += blockDim.x) {
+    const int v = vlist[j];
+    double re, im;
+    log2d(zv[v], re, im);
+    logzv[2 * v] = re;
+    logzv[2 * v + 1] = im;
+    if (re_d(zv[v]) < 0) fl |= 1;
+    are += re;
+    aim += im;
+  }
+  for (int j = eoff[net] + threadIdx.x; j < eoff[net + 1]; j += blockDim.x) {
+    const int e = elist[j];
+    double re, im;
+    log2d(ze[e], re, im);
+    logze[2 * e] = re;
+    logze[2 * e + 1] = im;
+    if (re_d(ze[e]) < 0) fl |= 2;
+    if (is_zero(ze[e])) fl |= 4;
+    are -= re;
+    aim -= im;
+  }
+  are = warp_sum_d(are);
+  aim = warp_sum_d(aim);
+  for (int o = 16; o >= 1; o >>= 1) fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sre[warp] = are; sim[warp] = aim; sfl[warp] = fl; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0, i = 0;
+    int f = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { r += sre[w]; i += sim[w]; f |= sfl[w]; }
+    totals[2 * net] = r;
+    totals[2 * net + 1] = i;
+    flags[net] = f;
+  }
+}
+
+// kind 0: identity / D (message_environment(one) then normalised), 1: identity,
+// 2: all ones.  One-layer messages: kind 0 -> ones / D, else ones.
+template <typename T>
+__global__ void init_messages_kernel(int layers, int kind, const long long* moff, const int* bond,
+                                     int nslots, T* msgs) {
+  const int s = blockIdx.x;
+  if (s >= nslots) return;
+  const int D = bond[s];
+  T* m = msgs + moff[s];
+  const int n = layers == 2 ? D * D : D;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double val;
+    if (layers == 2) {
+      const bool diag = (j / D) == (j % D);
+      val = kind == 2 ? 1.0 : (diag ? (kind == 0 ? 1.0 / D : 1.0) : 0.0);
+    } else {
+      val = kind == 0 ? 1.0 / D : 1.0;
+    }
+    T t = tzero<T>();
+    if constexpr (is_cplx<T>::value) t.x = (typename real_of<T>::type)val;
+    else t = (T)val;
+    m[j] = t;
+  }
+}
+
+template <typename T>
+__global__ void iterate_diff_kernel(const long long* moff, int nslots, const T* m1, const T* m2,
+                                    double* slot_diff, unsigned long long* dmax, int* nan_flag) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nslots) return;
+  double n1 = 0, n2 = 0, dre = 0, dim = 0;
+  for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) {
+    const double ar = re_d(m1[j]), ai = im_d(m1[j]), br = re_d(m2[j]), bi = im_d(m2[j]);
+    n1 += ar * ar + ai * ai;
+    n2 += br * br + bi * bi;
+    dre += ar * br + ai * bi;
+    dim += ar * bi - ai * br;
+  }
+  n1 = warp_sum_d(n1);
+  n2 = warp_sum_d(n2);
+  dre = warp_sum_d(dre);
+  dim = warp_sum_d(dim);
+  if (lane == 0) {
+    const double val = 1.0 - (dre * dre + dim * dim) / (n1 * n2);
+    if (slot_diff) slot_diff[warp] = val;
+    if (val != val) atomicExch(nan_flag, 1);
+    else atomicMax(dmax, enc_double(val));
+  }
+}
+
+// Site-tensor permutation into the canonical row-major [phys][legs...] layout.
+// For vertex u, canonical axis a has extent dims[rank_off[u]+a] and source stride
+// sstride[rank_off[u]+a] (elements); source tensor starts at soff[u].
+template <typename T>
+__global__ void permute_kernel(int nv, const long long* soff, const long long* toff,
+                               const int* rank_off, const int* dims, const long long* sstride,
+                               const T* src, T* dst) {
+  const int u = blockIdx.y;
+  if (u >= nv) return;
+  const long long n = toff[u + 1] - toff[u];
+  const int r0 = rank_off[u], r = rank_off[u + 1] - r0;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    long long rem = j, so = 0;
+    for (int ax = r - 1; ax >= 0; --ax) {
+      const int e = dims[r0 + ax];
+      const long long idx = rem % e;
+      rem /= e;
+      so += idx * sstride[r0 + ax];
+    }
+    dst[toff[u] + j] = src[soff[u] + so];
+  }
+}
+
+__global__ void convergence_check_kernel(unsigned long long* dmax, int* nan_flag, double tol,
+                                         int iter, int* done, int* at_iter, double* delta_out,
+                                         int* iters_out) {
+  if (*done) return;
+  double delta = dec_double(*dmax);
+  if (*nan_flag) delta = nan("");
+  *iters_out = iter;
+  if (delta_out) *delta_out = delta;
+  if (tol >= 0 && delta < tol) {
+    *done = 1;
+    *at_iter = iter;
+  }
+  *dmax = enc_double(-INFINITY);
+  *nan_flag = 0;
+}
+
+template <typename T>
+cudaError_t launch_generic_t(const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
+  if (cfg.grid <= 0 || a.n_items <= 0) return cudaSuccess;
+  if (a.layers == 2) {
+    auto k = bp2_kernel<T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    k<<<cfg.grid, cfg.block, cfg.smem, st>>>(a);
+  } else {
+    auto k = bp1_kernel<T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    k<<<cfg.grid, cfg.block, cfg.smem, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+int max_active_t(int layers, int block, size_t smem) {
+  int n = 0;
+  if (layers == 2) {
+    cudaFuncSetAttribute(bp2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_kernel<T>, block, smem);
+  } else {
+    cudaFuncSetAttribute(bp1_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp1_kernel<T>, block, smem);
+  }
+  return n;
+}
+
+}  // namespace
+
+#define ITN_DISPATCH(dtype, ...)                         \
+  switch (dtype) {                                       \
+    case DT_F32: { using T = float; __VA_ARGS__; }       \
+    case DT_F64: { using T = double; __VA_ARGS__; }      \
+    case DT_C64: { using T = c64; __VA_ARGS__; }         \
+    case DT_C128: { using T = c128; __VA_ARGS__; }       \
+    default: return cudaErrorInvalidValue;               \
+  }
+
+size_t generic_smem_bytes(int dtype, const GenericArgs& a, int block, bool in_smem) {
+  switch (dtype) {
+    case DT_F32: return smem_layout<float>(a, block, in_smem).total;
+    case DT_F64: return smem_layout<double>(a, block, in_smem).total;
+    case DT_C64: return smem_layout<c64>(a, block, in_smem).total;
+    case DT_C128: return smem_layout<c128>(a, block, in_smem).total;
+  }
+  return 0;
+}
+
+int generic_max_active(int dtype, int layers, int block, size_t smem) {
+  switch (dtype) {
+    case DT_F32: return max_active_t<float>(layers, block, smem);
+    case DT_F64: return max_active_t<double>(layers, block, smem);
+    case DT_C64: return max_active_t<c64>(layers, block, smem);
+    case DT_C128: return max_active_t<c128>(layers, block, smem);
+  }
+  return 0;
+}
+
+cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
+  ITN_DISPATCH(dtype, return launch_generic_t<T>(a, cfg, st));
+}
+
+cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,
+                                const int* eslots, int n_e, const void* msgs, void* ze_out,
+                                cudaStream_t st) {
+  (void)layers;
+  if (n_e <= 0) return cudaSuccess;
+  const int block = 256, grid = (n_e * 32 + block - 1) / block;
+  ITN_DISPATCH(dtype, edge_scalar_kernel<T><<<grid, block, 0, st>>>(
+                          moff, rev, eslots, n_e, reinterpret_cast<const T*>(msgs),
+                          reinterpret_cast<T*>(ze_out));
+               return cudaGetLastError());
+}
+
+cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
+                          const int* voff, const int* vlist, const int* eoff, const int* elist,
+                          int n_nets, double* logzv, double* logze, double* totals, int* flags,
+                          cudaStream_t st) {
+  (void)nv;
+  (void)ne;
+  if (n_nets <= 0) return cudaSuccess;
+  ITN_DISPATCH(dtype, logsum_kernel<T><<<n_nets, 256, 0, st>>>(
+                          reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), voff,
+                          vlist, eoff, elist, logzv, logze, totals, flags);
+               return cudaGetLastError());
+}
+
+cudaError_t launch_init_messages(int dtype, int layers, int kind, const long long* moff,
+                                 const int* bond, int nslots, void* msgs, cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  ITN_DISPATCH(dtype, init_messages_kernel<T><<<nslots, 64, 0, st>>>(
+                          layers, kind, moff, bond, nslots, reinterpret_cast<T*>(msgs));
+               return cudaGetLastError());
+}
+
+cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, const void* m1,
+                                const void* m2, double* slot_diff, unsigned long long* dmax,
+                                int* nan_flag, cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  const int block = 256, grid = (nslots * 32 + block - 1) / block;
+  ITN_DISPATCH(dtype, iterate_diff_kernel<T><<<grid, block, 0, st>>>(
+                          moff, nslots, reinterpret_cast<const T*>(m1),
+                          reinterpret_cast<const T*>(m2), slot_diff, dmax, nan_flag);
+               return cudaGetLastError());
+}
+
+cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long long* toff,
+                           const int* rank_off, const int* dims, const long long* sstride,
+                           const void* src, void* dst, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  dim3 grid(8, nv);
+  ITN_DISPATCH(dtype, permute_kernel<T><<<grid, 256, 0, st>>>(
+                          nv, soff, toff, rank_off, dims, sstride,
+                          reinterpret_cast<const T*>(src), reinterpret_cast<T*>(dst));
+               return cudaGetLastError());
+}
+
+cudaError_t launch_convergence_check(const unsigned long long* dmax, const int* nan_flag,
+                                     double tol, int iter, int* done, int* at_iter,
+                                     double* delta_out, int* iters_out, cudaStream_t st) {
+  convergence_check_kernel<<<1, 1, 0, st>>>(const_cast<unsigned long long*>(dmax),
+                                            const_cast<int*>(nan_flag), tol, iter, done, at_iter,
+                                            delta_out, iters_out);
+  return cudaGetLastError();
+}
+
+}  // namespace itn

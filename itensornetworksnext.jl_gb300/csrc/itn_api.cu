@@ -1,0 +1,1086 @@
+// itn_api.cu -- the C ABI of libitn_gpu.so (declared in include/itn_gpu.h).
+//
+// Host-side responsibilities: validate arguments, keep the network (CSR) and the
+// per-vertex op programs, own device buffers, and drive the solve loop.  The whole
+// beliefpropagation solve runs on the device: each outer iteration is one sweep
+// launch plus a one-thread convergence check that raises a device flag; later sweeps
+// see the flag and return at once, so a fixed launch sequence (captured once as a
+// CUDA graph) reproduces StopAfterIteration(maxiter) | StopWhenConverged(tol)
+// without a host round trip per iteration.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/itn_gpu.h"
+#include "itn_common.cuh"
+#include "itn_internal.h"
+#include "itn_tc.h"
+
+using namespace itn;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct Program {
+  std::vector<uint32_t> ops;
+  int nbuf = 1;
+};
+
+// Leave-one-out program generator (see bp_generic.cu): buffer 0 holds the site
+// tensor; absorb chains ping-pong between two scratch buffers.
+struct ProgGen {
+  std::vector<uint32_t> ops;
+  std::vector<int> free_list;
+  int next = 1;
+  int high = 1;
+  int alloc() {
+    int b;
+    if (!free_list.empty()) {
+      b = free_list.back();
+      free_list.pop_back();
+    } else {
+      b = next++;
+    }
+    high = std::max(high, b + 1);
+    return b;
+  }
+  void release(int b) {
+    if (b > 0) free_list.push_back(b);
+  }
+  int absorb_chain(int src, const std::vector<int>& legs) {
+    if (legs.empty()) return src;
+    const int n = (int)legs.size();
+    const int res = alloc();
+    const int tmp = n > 1 ? alloc() : -1;
+    int cur = src;
+    for (int j = 0; j < n; ++j) {
+      const int dst = ((n - 1 - j) % 2 == 0) ? res : tmp;
+      ops.push_back(make_op(OP_ABSORB, cur, dst, legs[j]));
+      cur = dst;
+    }
+    if (tmp >= 0) release(tmp);
+    return res;
+  }
+  void loo(int cur, const std::vector<int>& L) {
+    if (L.size() == 1) {
+      ops.push_back(make_op(OP_FINAL, cur, 0, L[0]));
+      return;
+    }
+    const size_t h = (L.size() + 1) / 2;
+    std::vector<int> L1(L.begin(), L.begin() + h), L2(L.begin() + h, L.end());
+    int b = absorb_chain(cur, L2);
+    loo(b, L1);
+    if (b != cur) release(b);
+    b = absorb_chain(cur, L1);
+    loo(b, L2);
+    if (b != cur) release(b);
+  }
+};
+
+Program make_program(int z, uint32_t mask, bool full) {
+  ProgGen g;
+  if (full) {
+    std::vector<int> all;
+    for (int l = 0; l < z; ++l) all.push_back(l);
+    int b = g.absorb_chain(0, all);
+    g.ops.push_back(make_op(OP_FULL, b, 0, 0));
+  } else {
+    std::vector<int> others, req;
+    for (int l = 0; l < z; ++l) ((mask >> l) & 1u ? req : others).push_back(l);
+    int b = g.absorb_chain(0, others);
+    if (!req.empty()) g.loo(b, req);
+  }
+  Program p;
+  p.ops = g.ops;
+  p.nbuf = g.high;
+  return p;
+}
+
+}  // namespace
+
+struct itn_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  int sm_count = 0;
+  int smem_optin = 0;
+
+  // network (host)
+  bool have_graph = false;
+  int64_t nv = 0, nslots = 0;
+  int layers = 2;
+  std::vector<int64_t> off, nbr, rev, toff, moff;
+  std::vector<int32_t> bond, phys, net;
+  int n_nets = 1;
+  int max_d2 = 1;
+  int64_t max_tensor = 1;
+  std::vector<int> eslots;  // undirected edges: slot < rev[slot]
+
+  // network (device)
+  DevBuf d_off, d_rev, d_bond, d_phys, d_toff, d_moff, d_eslots;
+  DevBuf d_net_voff, d_net_vlist, d_net_eoff, d_net_elist;
+
+  // programs and work lists
+  std::map<std::pair<int, uint32_t>, int> prog_index;  // (z, mask|full bit) -> offset
+  std::vector<uint32_t> prog_host;
+  DevBuf d_prog;
+  bool prog_dirty = true;
+  int nbuf = 1;
+  int msg_cap = 1;
+  std::vector<int> items_par, items_scal;
+  DevBuf d_items_par, d_items_scal;
+  std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
+
+  // data
+  int dtype = -1;
+  bool have_tensors = false, have_messages = false;
+  DevBuf d_tens;
+  DevBuf d_msg[2];
+  int cur = 0;
+  DevBuf d_zv, d_ze, d_logzv, d_logze, d_tot, d_flags;
+  DevBuf d_scratch;
+  DevBuf d_stage;  // upload staging
+
+  // convergence state (device): dmax, nan, done, at, iters, delta, counter
+  DevBuf d_slot_diff, d_state;
+
+  // cached solve graphs
+  std::map<std::string, cudaGraphExec_t> graphs;
+
+  // tensor-core engine (bp_tc.cu), created on first use
+  TcEngine* tc = nullptr;
+
+  ~itn_ctx() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (tc) tc_destroy(tc);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+struct ConvState {
+  unsigned long long dmax;
+  int nan_flag;
+  int done;
+  int at_iter;
+  int iters;
+  double delta;
+  int counter;
+  int pad;
+};
+
+int fail(itn_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(itn_ctx* c, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  const int code = (e == cudaErrorMemoryAllocation) ? ITN_ERR_OOM : ITN_ERR_CUDA;
+  return fail(c, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                          \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+  } while (0)
+
+int ensure_device(itn_ctx* c) {
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  return ITN_OK;
+}
+
+template <typename T>
+int upload_vec(itn_ctx* c, DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  CK(b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T)));
+  if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return ITN_OK;
+}
+
+int program_offset(itn_ctx* c, int z, uint32_t mask, bool full) {
+  const uint32_t key = full ? 0x80000000u : mask;
+  auto it = c->prog_index.find({z, key});
+  if (it != c->prog_index.end()) return it->second;
+  Program p = make_program(z, mask, full);
+  const int offv = (int)c->prog_host.size();
+  c->prog_host.push_back((uint32_t)p.ops.size());
+  c->prog_host.insert(c->prog_host.end(), p.ops.begin(), p.ops.end());
+  c->nbuf = std::max(c->nbuf, p.nbuf);
+  c->prog_index[{z, key}] = offv;
+  c->prog_dirty = true;
+  return offv;
+}
+
+int sync_programs(itn_ctx* c) {
+  if (!c->prog_dirty) return ITN_OK;
+  int r = upload_vec(c, c->d_prog, c->prog_host, c->stream);
+  if (r) return r;
+  c->prog_dirty = false;
+  return ITN_OK;
+}
+
+int block_for(itn_ctx* c) {
+  if (c->max_tensor <= 256) return 64;
+  if (c->max_tensor <= 2048) return 128;
+  return 256;
+}
+
+// Prepare GenericArgs and a launch configuration for a list of items.
+int plan_generic(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items, int n_items,
+                 const void* msg_in, void* msg_out) {
+  memset(&a, 0, sizeof(a));
+  a.layers = c->layers;
+  a.off = c->d_off.as<int>();
+  a.rev = c->d_rev.as<int>();
+  a.bond = c->d_bond.as<int>();
+  a.phys = c->d_phys.as<int>();
+  a.toff = c->d_toff.as<long long>();
+  a.moff = c->d_moff.as<long long>();
+  a.tens = c->d_tens.p;
+  a.msg_in = msg_in;
+  a.msg_out = msg_out;
+  a.items = d_items;
+  a.n_items = n_items;
+  a.prog = c->d_prog.as<unsigned>();
+  a.nbuf = c->layers == 2 ? c->nbuf : 0;
+  a.buf_elems = (c->max_tensor + 15) & ~15LL;
+  a.msg_cap = c->msg_cap;
+  a.max_d2 = c->max_d2;
+  a.normalize = 1;
+  cfg.block = block_for(c);
+  bool in_smem = true;
+  size_t smem = generic_smem_bytes(c->dtype, a, cfg.block, true);
+  if (c->layers == 2 && smem > (size_t)c->smem_optin) {
+    in_smem = false;
+    smem = generic_smem_bytes(c->dtype, a, cfg.block, false);
+    if (smem > (size_t)c->smem_optin)
+      return fail(c, ITN_ERR_UNSUPPORTED, "vertex needs %zu bytes of shared staging", smem);
+  }
+  int per_sm = generic_max_active(c->dtype, c->layers, cfg.block, smem);
+  if (per_sm <= 0) per_sm = 1;
+  cfg.grid = std::max(1, std::min(n_items, c->sm_count * per_sm));
+  cfg.smem = smem;
+  if (!in_smem) {
+    const size_t need = (size_t)cfg.grid * a.nbuf * a.buf_elems * dtype_size(c->dtype);
+    CK(c->d_scratch.ensure(need));
+    a.gscratch = c->d_scratch.p;
+  }
+  return ITN_OK;
+}
+
+ConvState* conv(itn_ctx* c) { return c->d_state.as<ConvState>(); }
+
+int check_ready(itn_ctx* c, bool need_msgs) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return fail(c, ITN_ERR_STATE, "no network uploaded");
+  if (!c->have_tensors) return fail(c, ITN_ERR_STATE, "no site tensors uploaded");
+  if (need_msgs && !c->have_messages) return fail(c, ITN_ERR_STATE, "no messages uploaded");
+  return ITN_OK;
+}
+
+// Kernel launches that reset the convergence state for a new solve.
+__global__ void reset_state_kernel(ConvState* s) {
+  s->dmax = enc_double(-INFINITY);
+  s->nan_flag = 0;
+  s->done = 0;
+  s->at_iter = -1;
+  s->iters = 0;
+  s->delta = INFINITY;
+  s->counter = 0;
+}
+
+// Convergence check with a device-side iteration counter (graph-position independent).
+__global__ void step_check_kernel(ConvState* s, double tol, int use_tol) {
+  if (s->done) return;
+  const int iter = ++s->counter;
+  s->iters = iter;
+  if (!use_tol) return;
+  double delta = dec_double(s->dmax);
+  if (s->nan_flag) delta = nan("");
+  s->delta = delta;
+  if (delta < tol) {
+    s->done = 1;
+    s->at_iter = iter;
+  }
+  s->dmax = enc_double(-INFINITY);
+  s->nan_flag = 0;
+}
+
+__global__ void copy_kernel(const int4* __restrict__ src, int4* __restrict__ dst, long long n16,
+                            const ConvState* s) {
+  if (s->done) return;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n16;
+       j += (long long)gridDim.x * blockDim.x)
+    dst[j] = src[j];
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+int32_t itn_abi_version(void) { return ITN_ABI_VERSION; }
+
+const char* itn_status_string(int32_t s) {
+  switch (s) {
+    case ITN_OK: return "ok";
+    case ITN_ERR_ARG: return "invalid argument";
+    case ITN_ERR_CUDA: return "CUDA error";
+    case ITN_ERR_OOM: return "out of device memory";
+    case ITN_ERR_NAN: return "non-finite value";
+    case ITN_ERR_TIMEOUT: return "iteration cap reached";
+    case ITN_ERR_UNSUPPORTED: return "unsupported";
+    case ITN_ERR_STATE: return "invalid call order";
+  }
+  return "unknown status";
+}
+
+int32_t itn_create(itn_ctx** out, int32_t device, int32_t flags) {
+  (void)flags;
+  if (!out) return ITN_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return ITN_ERR_CUDA;
+  }
+  if (device < 0 || device >= n) return ITN_ERR_ARG;
+  itn_ctx* c = new itn_ctx();
+  c->device = device;
+  if (int r = ensure_device(c)) {
+    delete c;
+    return r;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    delete c;
+    return ITN_ERR_CUDA;
+  }
+  c->sm_count = prop.multiProcessorCount;
+  c->smem_optin = (int)prop.sharedMemPerBlockOptin;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      c->d_state.ensure(sizeof(ConvState)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return ITN_ERR_CUDA;
+  }
+  *out = c;
+  return ITN_OK;
+}
+
+int32_t itn_destroy(itn_ctx* c) {
+  if (!c) return ITN_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  delete c;
+  return ITN_OK;
+}
+
+const char* itn_last_error(const itn_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int32_t itn_synchronize(itn_ctx* c) {
+  if (!c) return ITN_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const int64_t* csr_nbr,
+                         const int32_t* bond, const int64_t* rev, const int32_t* phys,
+                         int32_t layers, const int32_t* net_id) {
+  if (!c) return ITN_ERR_ARG;
+  if (int r = ensure_device(c)) return r;
+  if (nv < 0 || nv > (1LL << 30)) return fail(c, ITN_ERR_ARG, "nv out of range");
+  if (nv > 0 && (!csr_off || !csr_nbr || !bond)) return fail(c, ITN_ERR_ARG, "null CSR array");
+  if (layers != 1 && layers != 2) return fail(c, ITN_ERR_ARG, "layers must be 1 or 2");
+  if (nv > 0 && csr_off[0] != 0) return fail(c, ITN_ERR_ARG, "csr_off[0] must be 0");
+  const int64_t ns = nv > 0 ? csr_off[nv] : 0;
+  if (ns < 0 || ns > (1LL << 30)) return fail(c, ITN_ERR_ARG, "slot count out of range");
+  for (int64_t u = 0; u < nv; ++u) {
+    const int64_t z = csr_off[u + 1] - csr_off[u];
+    if (z < 0) return fail(c, ITN_ERR_ARG, "csr_off not monotone at vertex %lld", (long long)u);
+    if (z > kMaxLegs) return fail(c, ITN_ERR_UNSUPPORTED, "vertex %lld has %lld legs (max %d)",
+                                  (long long)u, (long long)z, kMaxLegs);
+  }
+  for (int64_t s = 0; s < ns; ++s) {
+    if (csr_nbr[s] < 0 || csr_nbr[s] >= nv) return fail(c, ITN_ERR_ARG, "neighbour out of range at slot %lld", (long long)s);
+    if (bond[s] < 1 || bond[s] > 4096) return fail(c, ITN_ERR_ARG, "bond dimension out of range at slot %lld", (long long)s);
+  }
+  c->have_graph = c->have_tensors = c->have_messages = false;
+  c->nv = nv;
+  c->nslots = ns;
+  c->layers = layers;
+  c->off.assign(csr_off, csr_off + nv + 1);
+  if (nv == 0) c->off.assign(1, 0);
+  c->nbr.assign(csr_nbr, csr_nbr + ns);
+  c->bond.assign(bond, bond + ns);
+  c->phys.assign(nv, 1);
+  if (phys) c->phys.assign(phys, phys + nv);
+  for (int64_t u = 0; u < nv; ++u)
+    if (c->phys[u] < 1) return fail(c, ITN_ERR_ARG, "physical dimension < 1 at vertex %lld", (long long)u);
+  if (layers == 1)
+    for (int64_t u = 0; u < nv; ++u)
+      if (c->phys[u] != 1) return fail(c, ITN_ERR_UNSUPPORTED, "plain (one-layer) networks need phys = 1 (open site index at vertex %lld)", (long long)u);
+  // reverse slots
+  c->rev.assign(ns, -1);
+  if (rev) {
+    for (int64_t s = 0; s < ns; ++s) c->rev[s] = rev[s];
+  } else {
+    std::map<std::pair<int64_t, int64_t>, std::vector<int64_t>> pend;
+    for (int64_t u = 0; u < nv; ++u)
+      for (int64_t s = c->off[u]; s < c->off[u + 1]; ++s) pend[{u, c->nbr[s]}].push_back(s);
+    for (auto& kv : pend) {
+      auto it = pend.find({kv.first.second, kv.first.first});
+      if (it == pend.end() || it->second.size() != kv.second.size())
+        return fail(c, ITN_ERR_ARG, "edge %lld->%lld has no matching reverse", (long long)kv.first.first, (long long)kv.first.second);
+      for (size_t k = 0; k < kv.second.size(); ++k) c->rev[kv.second[k]] = it->second[k];
+    }
+  }
+  for (int64_t u = 0; u < nv; ++u)
+    for (int64_t s = c->off[u]; s < c->off[u + 1]; ++s) {
+      const int64_t r = c->rev[s];
+      if (r < 0 || r >= ns || c->rev[r] != s || c->nbr[r] != u || c->bond[r] != c->bond[s] || c->nbr[s] == u)
+        return fail(c, ITN_ERR_ARG, "inconsistent reverse slot for slot %lld", (long long)s);
+    }
+  // offsets
+  c->toff.assign(nv + 1, 0);
+  c->max_tensor = 1;
+  c->msg_cap = 1;
+  for (int64_t u = 0; u < nv; ++u) {
+    int64_t n = c->phys[u];
+    int64_t mc = 0;
+    for (int64_t s = c->off[u]; s < c->off[u + 1]; ++s) {
+      n *= c->bond[s];
+      mc += (layers == 2) ? (int64_t)c->bond[s] * c->bond[s] : c->bond[s];
+      if (n > (1LL << 28)) return fail(c, ITN_ERR_UNSUPPORTED, "site tensor of vertex %lld too large", (long long)u);
+    }
+    c->toff[u + 1] = c->toff[u] + n;
+    c->max_tensor = std::max(c->max_tensor, n);
+    c->msg_cap = (int)std::max<int64_t>(c->msg_cap, mc);
+  }
+  c->moff.assign(ns + 1, 0);
+  c->max_d2 = 1;
+  for (int64_t s = 0; s < ns; ++s) {
+    const int64_t m = layers == 2 ? (int64_t)c->bond[s] * c->bond[s] : c->bond[s];
+    c->moff[s + 1] = c->moff[s] + m;
+    c->max_d2 = (int)std::max<int64_t>(c->max_d2, m);
+  }
+  // networks
+  c->net.assign(nv, 0);
+  if (net_id) c->net.assign(net_id, net_id + nv);
+  int nn = 0;
+  for (int64_t u = 0; u < nv; ++u) {
+    if (c->net[u] < 0) return fail(c, ITN_ERR_ARG, "negative network id");
+    nn = std::max(nn, c->net[u] + 1);
+  }
+  for (int64_t u = 0; u < nv; ++u)
+    for (int64_t s = c->off[u]; s < c->off[u + 1]; ++s)
+      if (c->net[c->nbr[s]] != c->net[u]) return fail(c, ITN_ERR_ARG, "edge joins two networks");
+  c->n_nets = std::max(nn, 1);
+  c->eslots.clear();
+  for (int64_t s = 0; s < ns; ++s)
+    if (s < c->rev[s]) c->eslots.push_back((int)s);
+  std::vector<int> voff(c->n_nets + 1, 0), eoff(c->n_nets + 1, 0), vlist(nv), elist(c->eslots.size());
+  for (int64_t u = 0; u < nv; ++u) voff[c->net[u] + 1]++;
+  std::vector<int> esrc(c->eslots.size());
+  for (size_t e = 0; e < c->eslots.size(); ++e) {
+    int64_t s = c->eslots[e];
+    int64_t u = std::upper_bound(c->off.begin(), c->off.end(), s) - c->off.begin() - 1;
+    esrc[e] = (int)u;
+    eoff[c->net[u] + 1]++;
+  }
+  for (int k = 0; k < c->n_nets; ++k) {
+    voff[k + 1] += voff[k];
+    eoff[k + 1] += eoff[k];
+  }
+  {
+    std::vector<int> vp(voff.begin(), voff.end() - 1), ep(eoff.begin(), eoff.end() - 1);
+    for (int64_t u = 0; u < nv; ++u) vlist[vp[c->net[u]]++] = (int)u;
+    for (size_t e = 0; e < c->eslots.size(); ++e) elist[ep[c->net[esrc[e]]]++] = (int)e;
+  }
+  // programs & work lists
+  c->prog_index.clear();
+  c->prog_host.clear();
+  c->nbuf = 1;
+  c->items_par.clear();
+  c->items_scal.clear();
+  c->seq_plans.clear();
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+  for (int64_t u = 0; u < nv; ++u) {
+    const int z = (int)(c->off[u + 1] - c->off[u]);
+    const uint32_t full = z >= 32 ? 0xffffffffu : ((1u << z) - 1u);
+    if (layers == 2) {
+      if (z > 0) {
+        c->items_par.push_back((int)u);
+        c->items_par.push_back(program_offset(c, z, full, false));
+      }
+      c->items_scal.push_back((int)u);
+      c->items_scal.push_back(program_offset(c, z, 0, true));
+    } else {
+      if (z > 0) {
+        c->items_par.push_back((int)u);
+        c->items_par.push_back((int)full);
+      }
+      c->items_scal.push_back((int)u);
+      c->items_scal.push_back(0);
+    }
+  }
+  if (c->prog_host.empty()) c->prog_host.push_back(0);
+  c->prog_dirty = true;
+  std::vector<int> off32(c->off.begin(), c->off.end()), rev32(c->rev.begin(), c->rev.end());
+  std::vector<long long> toffl(c->toff.begin(), c->toff.end()), moffl(c->moff.begin(), c->moff.end());
+  int r;
+  if ((r = upload_vec(c, c->d_off, off32, c->stream)) || (r = upload_vec(c, c->d_rev, rev32, c->stream)) ||
+      (r = upload_vec(c, c->d_bond, c->bond, c->stream)) || (r = upload_vec(c, c->d_phys, c->phys, c->stream)) ||
+      (r = upload_vec(c, c->d_toff, toffl, c->stream)) || (r = upload_vec(c, c->d_moff, moffl, c->stream)) ||
+      (r = upload_vec(c, c->d_eslots, c->eslots, c->stream)) ||
+      (r = upload_vec(c, c->d_net_voff, voff, c->stream)) || (r = upload_vec(c, c->d_net_vlist, vlist, c->stream)) ||
+      (r = upload_vec(c, c->d_net_eoff, eoff, c->stream)) || (r = upload_vec(c, c->d_net_elist, elist, c->stream)) ||
+      (r = upload_vec(c, c->d_items_par, c->items_par, c->stream)) ||
+      (r = upload_vec(c, c->d_items_scal, c->items_scal, c->stream)) || (r = sync_programs(c)))
+    return r;
+  CK(c->d_slot_diff.ensure(std::max<int64_t>(ns, 1) * sizeof(double)));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_graph = true;
+  c->dtype = -1;
+  if (c->tc) tc_invalidate(c->tc);
+  return ITN_OK;
+}
+
+int32_t itn_graph_info(const itn_ctx* c, int64_t* nv, int64_t* nslots, int64_t* tensor_elems,
+                       int64_t* message_elems, int32_t* n_nets, int64_t* n_undirected) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return ITN_ERR_STATE;
+  if (nv) *nv = c->nv;
+  if (nslots) *nslots = c->nslots;
+  if (tensor_elems) *tensor_elems = c->toff[c->nv];
+  if (message_elems) *message_elems = c->moff[c->nslots];
+  if (n_nets) *n_nets = c->n_nets;
+  if (n_undirected) *n_undirected = (int64_t)c->eslots.size();
+  return ITN_OK;
+}
+
+static int set_dtype(itn_ctx* c, int32_t dtype) {
+  if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
+  if (c->dtype != dtype) {
+    c->dtype = dtype;
+    c->have_messages = false;
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+  }
+  return ITN_OK;
+}
+
+int32_t itn_tensors_upload(itn_ctx* c, int32_t dtype, const void* packed) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
+  if (!packed && c->toff[c->nv] > 0) return fail(c, ITN_ERR_ARG, "null tensor pointer");
+  if (int r = ensure_device(c)) return r;
+  if (int r = set_dtype(c, dtype)) return r;
+  const size_t bytes = (size_t)c->toff[c->nv] * dtype_size(dtype);
+  CK(c->d_tens.ensure(bytes));
+  if (bytes) CK(cudaMemcpyAsync(c->d_tens.p, packed, bytes, cudaMemcpyHostToDevice, c->stream));
+  const size_t mb = (size_t)c->moff[c->nslots] * dtype_size(dtype);
+  CK(c->d_msg[0].ensure(mb));
+  CK(c->d_msg[1].ensure(mb));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_tensors = true;
+  if (c->tc) tc_invalidate(c->tc);
+  return ITN_OK;
+}
+
+int32_t itn_tensors_upload_strided(itn_ctx* c, int32_t dtype, const void* const* site_ptrs,
+                                   const int64_t* strides) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
+  if (!site_ptrs || !strides) return fail(c, ITN_ERR_ARG, "null pointer");
+  if (int r = ensure_device(c)) return r;
+  if (int r = set_dtype(c, dtype)) return r;
+  const size_t es = dtype_size(dtype);
+  // Gather each vertex's source extent (max offset + 1) into one staging buffer.
+  std::vector<long long> soff(c->nv + 1, 0), sstride;
+  std::vector<int> rank_off(c->nv + 1, 0), dims;
+  for (int64_t u = 0; u < c->nv; ++u) {
+    const int64_t z = c->off[u + 1] - c->off[u];
+    const int64_t base = c->off[u] + u;
+    long long ext = 1;
+    for (int64_t a = 0; a <= z; ++a) {
+      const int dim = a == 0 ? c->phys[u] : c->bond[c->off[u] + a - 1];
+      const long long st = strides[base + a];
+      if (st < 0) return fail(c, ITN_ERR_ARG, "negative stride at vertex %lld", (long long)u);
+      ext += (long long)(dim - 1) * st;
+      dims.push_back(dim);
+      sstride.push_back(st);
+    }
+    if (!site_ptrs[u]) return fail(c, ITN_ERR_ARG, "null tensor pointer at vertex %lld", (long long)u);
+    soff[u + 1] = soff[u] + ext;
+    rank_off[u + 1] = rank_off[u] + (int)(z + 1);
+  }
+  std::vector<unsigned char> host((size_t)soff[c->nv] * es);
+  for (int64_t u = 0; u < c->nv; ++u)
+    memcpy(host.data() + (size_t)soff[u] * es, site_ptrs[u], (size_t)(soff[u + 1] - soff[u]) * es);
+  DevBuf d_soff, d_toffl, d_rank, d_dims, d_str;
+  std::vector<long long> toffl(c->toff.begin(), c->toff.end());
+  int r;
+  if ((r = upload_vec(c, d_soff, soff, c->stream)) || (r = upload_vec(c, d_toffl, toffl, c->stream)) ||
+      (r = upload_vec(c, d_rank, rank_off, c->stream)) || (r = upload_vec(c, d_dims, dims, c->stream)) ||
+      (r = upload_vec(c, d_str, sstride, c->stream)))
+    return r;
+  CK(c->d_stage.ensure(host.size()));
+  if (!host.empty()) CK(cudaMemcpyAsync(c->d_stage.p, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(c->d_tens.ensure((size_t)c->toff[c->nv] * es));
+  CK(launch_permute(dtype, (int)c->nv, d_soff.as<long long>(), d_toffl.as<long long>(), d_rank.as<int>(),
+                    d_dims.as<int>(), d_str.as<long long>(), c->d_stage.p, c->d_tens.p, c->stream));
+  const size_t mb = (size_t)c->moff[c->nslots] * es;
+  CK(c->d_msg[0].ensure(mb));
+  CK(c->d_msg[1].ensure(mb));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_tensors = true;
+  if (c->tc) tc_invalidate(c->tc);
+  return ITN_OK;
+}
+
+int32_t itn_tensors_download(itn_ctx* c, int32_t dtype, void* packed) {
+  if (int r = check_ready(c, false)) return r;
+  if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "dtype differs from the uploaded tensors");
+  const size_t bytes = (size_t)c->toff[c->nv] * dtype_size(dtype);
+  if (bytes) CK(cudaMemcpyAsync(packed, c->d_tens.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+int32_t itn_messages_upload(itn_ctx* c, int32_t dtype, const void* packed) {
+  if (int r = check_ready(c, false)) return r;
+  if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "message dtype must equal the tensor dtype");
+  const size_t bytes = (size_t)c->moff[c->nslots] * dtype_size(dtype);
+  if (bytes && !packed) return fail(c, ITN_ERR_ARG, "null message pointer");
+  c->cur = 0;
+  if (bytes) CK(cudaMemcpyAsync(c->d_msg[0].p, packed, bytes, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_messages = true;
+  return ITN_OK;
+}
+
+int32_t itn_messages_download(itn_ctx* c, int32_t dtype, void* packed) {
+  if (int r = check_ready(c, true)) return r;
+  if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "dtype differs from the uploaded data");
+  const size_t bytes = (size_t)c->moff[c->nslots] * dtype_size(dtype);
+  if (bytes && !packed) return fail(c, ITN_ERR_ARG, "null message pointer");
+  if (bytes) CK(cudaMemcpyAsync(packed, c->d_msg[c->cur].p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+int32_t itn_messages_init(itn_ctx* c, int32_t kind) {
+  if (int r = check_ready(c, false)) return r;
+  if (kind < 0 || kind > 2) return fail(c, ITN_ERR_ARG, "unknown message init kind");
+  c->cur = 0;
+  CK(launch_init_messages(c->dtype, c->layers, kind, c->d_moff.as<long long>(), c->d_bond.as<int>(),
+                          (int)c->nslots, c->d_msg[0].p, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_messages = true;
+  return ITN_OK;
+}
+
+}  // extern "C"
+
+// ---- solve helpers ------------------------------------------------------------------------
+namespace {
+
+// Dependency levels that make a sequential (Gauss-Seidel) sweep over `edges` exact when
+// the updates of one level run concurrently: an update follows every earlier update it
+// reads from (RAW), every earlier reader of the slot it writes (WAR) and every earlier
+// writer of that slot (WAW).
+std::vector<std::vector<int>> sequential_levels(itn_ctx* c, const int64_t* edges, int64_t n) {
+  std::vector<int> last_w(c->nslots, 0), last_r(c->nslots, 0);
+  std::vector<std::vector<int>> levels;
+  for (int64_t e = 0; e < n; ++e) {
+    const int64_t s = edges[e];
+    const int64_t u = std::upper_bound(c->off.begin(), c->off.end(), s) - c->off.begin() - 1;
+    int lv = std::max(last_w[s], last_r[s]);
+    for (int64_t t = c->off[u]; t < c->off[u + 1]; ++t) {
+      if (t == s) continue;
+      lv = std::max(lv, last_w[c->rev[t]]);
+    }
+    lv += 1;
+    last_w[s] = lv;
+    for (int64_t t = c->off[u]; t < c->off[u + 1]; ++t)
+      if (t != s) last_r[c->rev[t]] = std::max(last_r[c->rev[t]], lv);
+    if ((int)levels.size() < lv) levels.resize(lv);
+    levels[lv - 1].push_back((int)e);
+  }
+  return levels;
+}
+
+struct SeqPlan {
+  std::vector<int> level_off;  // into items (pairs)
+  std::shared_ptr<DevBuf> items;
+};
+
+int get_seq_plan(itn_ctx* c, const int64_t* edges, int64_t n, SeqPlan& plan) {
+  std::vector<int64_t> key(edges, edges + n);
+  auto it = c->seq_plans.find(key);
+  if (it != c->seq_plans.end()) {
+    plan.level_off = it->second.first;
+    plan.items = it->second.second;
+    return ITN_OK;
+  }
+  for (int64_t e = 0; e < n; ++e)
+    if (edges[e] < 0 || edges[e] >= c->nslots) return fail(c, ITN_ERR_ARG, "edge slot %lld out of range", (long long)edges[e]);
+  auto levels = sequential_levels(c, edges, n);
+  std::vector<int> items, loff(1, 0);
+  for (auto& lv : levels) {
+    for (int e : lv) {
+      const int64_t s = edges[e];
+      const int64_t u = std::upper_bound(c->off.begin(), c->off.end(), s) - c->off.begin() - 1;
+      const int z = (int)(c->off[u + 1] - c->off[u]);
+      const int leg = (int)(s - c->off[u]);
+      items.push_back((int)u);
+      items.push_back(c->layers == 2 ? program_offset(c, z, 1u << leg, false) : (int)(1u << leg));
+    }
+    loff.push_back((int)items.size() / 2);
+  }
+  auto buf = std::make_shared<DevBuf>();
+  if (int r = upload_vec(c, *buf, items, c->stream)) return r;
+  if (int r = sync_programs(c)) return r;
+  c->seq_plans[key] = {loff, buf};
+  plan.level_off = loff;
+  plan.items = buf;
+  return ITN_OK;
+}
+
+// Launch plans are computed before stream capture (no allocation or occupancy query
+// happens while capturing).
+struct ParPlan {
+  GenericArgs a[2];  // a[i]: reads buffer i, writes buffer i ^ 1
+  LaunchCfg cfg[2];
+};
+
+int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
+  const bool use_tol = o->tol >= 0;
+  for (int in = 0; in < 2; ++in) {
+    if (int r = plan_generic(c, p.a[in], p.cfg[in], c->d_items_par.as<int>(), (int)c->items_par.size() / 2,
+                             c->d_msg[in].p, c->d_msg[in ^ 1].p))
+      return r;
+    p.a[in].normalize = o->normalize;
+    p.a[in].done = &conv(c)->done;
+    if (use_tol) {
+      p.a[in].slot_diff = c->d_slot_diff.as<double>();
+      p.a[in].diff_max = &conv(c)->dmax;
+      p.a[in].nan_flag = &conv(c)->nan_flag;
+    }
+  }
+  return ITN_OK;
+}
+
+// Record `nsweeps` outer iterations of the parallel schedule onto the stream, starting
+// from buffer `start`.
+int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const itn_bp_opts* o,
+                    int* launches) {
+  const bool use_tol = o->tol >= 0;
+  for (int t = 0; t < nsweeps; ++t) {
+    const int in = (start + t) & 1, out = in ^ 1;
+    const int prec = o->precision;
+    if (prec != ITN_PREC_NATIVE) {
+      TcRun tr;
+      tr.msg_in = c->d_msg[in].p;
+      tr.msg_out = c->d_msg[out].p;
+      tr.precision = prec;
+      tr.split = t >= nsweeps - o->split_sweeps;
+      tr.normalize = o->normalize;
+      tr.slot_diff = use_tol ? c->d_slot_diff.as<double>() : nullptr;
+      tr.diff_max = use_tol ? &conv(c)->dmax : nullptr;
+      tr.nan_flag = use_tol ? &conv(c)->nan_flag : nullptr;
+      tr.done = &conv(c)->done;
+      cudaError_t e = tc_sweep(c->tc, tr, c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
+    } else {
+      CK(launch_generic(c->dtype, p.a[in], p.cfg[in], c->stream));
+    }
+    step_check_kernel<<<1, 1, 0, c->stream>>>(conv(c), o->tol, use_tol ? 1 : 0);
+    CK(cudaGetLastError());
+    *launches += 2;
+  }
+  return ITN_OK;
+}
+
+struct SeqLaunch {
+  GenericArgs a;
+  LaunchCfg cfg;
+};
+
+int make_seq_launches(itn_ctx* c, const SeqPlan& plan, const itn_bp_opts* o, std::vector<SeqLaunch>& out) {
+  void* m = c->d_msg[0].p;
+  out.clear();
+  for (size_t lv = 0; lv + 1 < plan.level_off.size(); ++lv) {
+    const int b = plan.level_off[lv], e = plan.level_off[lv + 1];
+    SeqLaunch L;
+    if (int r = plan_generic(c, L.a, L.cfg, plan.items->as<int>() + 2 * b, e - b, m, m)) return r;
+    L.a.normalize = o->normalize;
+    L.a.done = &conv(c)->done;
+    out.push_back(L);
+  }
+  return ITN_OK;
+}
+
+int record_sequential(itn_ctx* c, const std::vector<SeqLaunch>& lv, int nsweeps, const itn_bp_opts* o,
+                      int* launches) {
+  const bool use_tol = o->tol >= 0;
+  const size_t mbytes = (size_t)c->moff[c->nslots] * dtype_size(c->dtype);
+  void* m = c->d_msg[0].p;
+  void* prev = c->d_msg[1].p;
+  for (int t = 0; t < nsweeps; ++t) {
+    if (use_tol) {
+      const long long n16 = (long long)(mbytes / 16);
+      if (n16 > 0) {
+        copy_kernel<<<(int)std::min<long long>((n16 + 255) / 256, 4096), 256, 0, c->stream>>>(
+            reinterpret_cast<const int4*>(m), reinterpret_cast<int4*>(prev), n16, conv(c));
+        *launches += 1;
+      }
+      const size_t tail = mbytes - (size_t)n16 * 16;
+      if (tail) CK(cudaMemcpyAsync((char*)prev + n16 * 16, (const char*)m + n16 * 16, tail,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    }
+    for (const SeqLaunch& L : lv) {
+      CK(launch_generic(c->dtype, L.a, L.cfg, c->stream));
+      *launches += 1;
+    }
+    if (use_tol) {
+      CK(launch_iterate_diff(c->dtype, c->d_moff.as<long long>(), (int)c->nslots, m, prev,
+                             c->d_slot_diff.as<double>(), &conv(c)->dmax, &conv(c)->nan_flag, c->stream));
+      *launches += 1;
+    }
+    step_check_kernel<<<1, 1, 0, c->stream>>>(conv(c), o->tol, use_tol ? 1 : 0);
+    CK(cudaGetLastError());
+    *launches += 1;
+  }
+  return ITN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
+  if (int r = check_ready(c, true)) return r;
+  if (!o) return fail(c, ITN_ERR_ARG, "null options");
+  if (int r = ensure_device(c)) return r;
+  if (o->maxiter < 0 && !(o->tol >= 0))
+    return fail(c, ITN_ERR_ARG, "At least one of `maxiter` or `tol` must be specified.");
+  if (o->schedule != ITN_SCHED_PARALLEL && o->schedule != ITN_SCHED_SEQUENTIAL)
+    return fail(c, ITN_ERR_ARG, "unknown schedule");
+  if (o->precision != ITN_PREC_NATIVE) {
+    if (o->schedule != ITN_SCHED_PARALLEL)
+      return fail(c, ITN_ERR_UNSUPPORTED, "tensor-core precision modes run the parallel schedule");
+    if (c->dtype != ITN_F32) return fail(c, ITN_ERR_UNSUPPORTED, "tensor-core precision modes need float32 storage");
+    if (!c->tc) c->tc = tc_create();
+    const char* why = nullptr;
+    cudaError_t e = tc_prepare(c->tc, c->layers, c->nv, c->off.data(), c->bond.data(), c->phys.data(),
+                               c->d_off.as<int>(), c->d_rev.as<int>(), c->d_moff.as<long long>(),
+                               c->d_tens.p, c->toff.data(), o->precision, c->stream, &why);
+    if (why) return fail(c, ITN_ERR_UNSUPPORTED, "%s", why);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core prepare");
+  }
+  if (o->split_sweeps < 0) return fail(c, ITN_ERR_ARG, "split_sweeps < 0");
+  SeqPlan plan;
+  if (o->schedule == ITN_SCHED_SEQUENTIAL) {
+    if (!o->edges && o->n_edges > 0) return fail(c, ITN_ERR_ARG, "null edge list");
+    if (int r = get_seq_plan(c, o->edges, o->n_edges, plan)) return r;
+    // the sequential schedule works in place on buffer 0
+    if (c->cur != 0) {
+      CK(cudaMemcpyAsync(c->d_msg[0].p, c->d_msg[1].p, (size_t)c->moff[c->nslots] * dtype_size(c->dtype),
+                         cudaMemcpyDeviceToDevice, c->stream));
+      c->cur = 0;
+    }
+  }
+  if (int r = sync_programs(c)) return r;
+  ParPlan pplan;
+  std::vector<SeqLaunch> slaunch;
+  if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE) {
+    if (int r = make_par_plan(c, o, pplan)) return r;
+  } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {
+    if (int r = make_seq_launches(c, plan, o, slaunch)) return r;
+  }
+  reset_state_kernel<<<1, 1, 0, c->stream>>>(conv(c));
+  CK(cudaGetLastError());
+  int launches = 1;
+  const bool use_tol = o->tol >= 0;
+  const int chunk = o->maxiter >= 0 ? o->maxiter : 64;
+  const int64_t cap = o->maxiter >= 0 ? o->maxiter : 1000000;
+  int64_t issued = 0;
+  float total_ms = 0.f;
+  ConvState hs;
+  memset(&hs, 0, sizeof(hs));
+  while (issued < cap) {
+    const int n = (int)std::min<int64_t>(chunk, cap - issued);
+    if (n <= 0) break;
+    // one cached graph per (schedule, start buffer, sweep count, options)
+    char keyb[256];
+    snprintf(keyb, sizeof(keyb), "s%d c%d n%d t%d p%d sp%d nz%d e%p:%lld", o->schedule, c->cur, n,
+             use_tol ? 1 : 0, o->precision, o->split_sweeps, o->normalize,
+             (const void*)plan.items.get(), (long long)o->n_edges);
+    std::string key(keyb);
+    if (o->precision != ITN_PREC_NATIVE && n != o->maxiter) key += " chunk";
+    cudaGraphExec_t exec = nullptr;
+    auto it = c->graphs.find(key);
+    int rec_launches = 0;
+    if (it != c->graphs.end()) {
+      exec = it->second;
+    } else {
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      itn_bp_opts oo = *o;
+      if (o->precision != ITN_PREC_NATIVE && o->maxiter < 0) oo.split_sweeps = 0;
+      int r = o->schedule == ITN_SCHED_PARALLEL ? record_parallel(c, pplan, c->cur, n, &oo, &rec_launches)
+                                                : record_sequential(c, slaunch, n, &oo, &rec_launches);
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+      if (r) return r;
+      if (ce != cudaSuccess) return cuda_fail(c, ce, "stream capture");
+      ce = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) return cuda_fail(c, ce, "graph instantiate");
+      c->graphs[key] = exec;
+    }
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(cudaGraphLaunch(exec, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaMemcpyAsync(&hs, conv(c), sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    total_ms += ms;
+    // every recorded sweep is 2 launches (parallel) -- count what the graph holds
+    launches += (o->schedule == ITN_SCHED_PARALLEL) ? 2 * n
+                : (int)(n * ((plan.level_off.size() - 1) + (use_tol ? 3 : 1)));
+    issued += n;
+    if (hs.done) break;
+  }
+  // messages now live in buffer (cur + executed sweeps) for the parallel schedule
+  if (o->schedule == ITN_SCHED_PARALLEL) c->cur = (c->cur + hs.iters) & 1;
+  if (res) {
+    res->iterations = hs.iters;
+    res->at_iteration = hs.at_iter;
+    res->delta = use_tol ? hs.delta : INFINITY;
+    res->device_ms = total_ms;
+    res->kernel_launches = launches;
+  }
+  if (o->maxiter < 0 && !hs.done) return fail(c, ITN_ERR_TIMEOUT, "no convergence within %lld iterations", (long long)cap);
+  return ITN_OK;
+}
+
+int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
+  if (int r = check_ready(c, true)) return r;
+  if (slot < 0 || slot >= c->nslots) return fail(c, ITN_ERR_ARG, "slot out of range");
+  if (int r = ensure_device(c)) return r;
+  SeqPlan plan;
+  const int64_t e = slot;
+  if (int r = get_seq_plan(c, &e, 1, plan)) return r;
+  void* m = c->d_msg[c->cur].p;
+  GenericArgs a;
+  LaunchCfg cfg;
+  if (int r = plan_generic(c, a, cfg, plan.items->as<int>(), 1, m, m)) return r;
+  a.normalize = normalize;
+  CK(launch_generic(c->dtype, a, cfg, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+int32_t itn_iterate_diff(itn_ctx* c, int32_t dtype, const void* m1, const void* m2, double* out) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return fail(c, ITN_ERR_STATE, "no network uploaded");
+  if (!m1 || !m2 || !out) return fail(c, ITN_ERR_ARG, "null pointer");
+  if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype");
+  if (int r = ensure_device(c)) return r;
+  const size_t bytes = (size_t)c->moff[c->nslots] * dtype_size(dtype);
+  DevBuf a, b;
+  CK(a.ensure(bytes));
+  CK(b.ensure(bytes));
+  if (bytes) {
+    CK(cudaMemcpyAsync(a.p, m1, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(b.p, m2, bytes, cudaMemcpyHostToDevice, c->stream));
+  }
+  reset_state_kernel<<<1, 1, 0, c->stream>>>(conv(c));
+  CK(launch_iterate_diff(dtype, c->d_moff.as<long long>(), (int)c->nslots, a.p, b.p,
+                         c->d_slot_diff.as<double>(), &conv(c)->dmax, &conv(c)->nan_flag, c->stream));
+  ConvState hs;
+  CK(cudaMemcpyAsync(&hs, conv(c), sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *out = hs.nan_flag ? nan("") : dec_double(hs.dmax);
+  return ITN_OK;
+}
+
+int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* logze,
+                       double* totals, int32_t* flags) {
+  if (int r = check_ready(c, true)) return r;
+  if (int r = ensure_device(c)) return r;
+  const size_t es = dtype_size(c->dtype);
+  const int ne = (int)c->eslots.size();
+  CK(c->d_zv.ensure(std::max<int64_t>(c->nv, 1) * es));
+  CK(c->d_ze.ensure(std::max(ne, 1) * es));
+  CK(c->d_logzv.ensure(std::max<int64_t>(c->nv, 1) * 2 * sizeof(double)));
+  CK(c->d_logze.ensure(std::max(ne, 1) * 2 * sizeof(double)));
+  CK(c->d_tot.ensure(c->n_nets * 2 * sizeof(double)));
+  CK(c->d_flags.ensure(c->n_nets * sizeof(int)));
+  void* m = c->d_msg[c->cur].p;
+  if (c->nv > 0) {
+    GenericArgs a;
+    LaunchCfg cfg;
+    if (int r = plan_generic(c, a, cfg, c->d_items_scal.as<int>(), (int)c->items_scal.size() / 2, m, m)) return r;
+    a.zv_out = c->d_zv.p;
+    CK(launch_generic(c->dtype, a, cfg, c->stream));
+  }
+  CK(launch_edge_scalars(c->dtype, c->layers, c->d_moff.as<long long>(), c->d_rev.as<int>(),
+                         c->d_eslots.as<int>(), ne, m, c->d_ze.p, c->stream));
+  CK(launch_logsum(c->dtype, c->d_zv.p, c->d_ze.p, (int)c->nv, ne, c->d_net_voff.as<int>(),
+                   c->d_net_vlist.as<int>(), c->d_net_eoff.as<int>(), c->d_net_elist.as<int>(), c->n_nets,
+                   c->d_logzv.as<double>(), c->d_logze.as<double>(), c->d_tot.as<double>(),
+                   c->d_flags.as<int>(), c->stream));
+  if (zv && c->nv) CK(cudaMemcpyAsync(zv, c->d_zv.p, c->nv * es, cudaMemcpyDeviceToHost, c->stream));
+  if (ze && ne) CK(cudaMemcpyAsync(ze, c->d_ze.p, ne * es, cudaMemcpyDeviceToHost, c->stream));
+  if (logzv && c->nv) CK(cudaMemcpyAsync(logzv, c->d_logzv.p, c->nv * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (logze && ne) CK(cudaMemcpyAsync(logze, c->d_logze.p, ne * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (totals) CK(cudaMemcpyAsync(totals, c->d_tot.p, c->n_nets * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (flags) CK(cudaMemcpyAsync(flags, c->d_flags.p, c->n_nets * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+}  // extern "C"

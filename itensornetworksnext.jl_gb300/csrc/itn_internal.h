@@ -1,0 +1,88 @@
+// itn_internal.h -- declarations shared between the C-ABI layer (itn_api.cu) and the
+// kernel translation units.  Not part of the public interface (that is include/itn_gpu.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace itn {
+
+enum Dtype { DT_F32 = 0, DT_F64 = 1, DT_C64 = 2, DT_C128 = 3 };
+inline size_t dtype_size(int dt) {
+  switch (dt) {
+    case DT_F32: return 4;
+    case DT_F64: return 8;
+    case DT_C64: return 8;
+    case DT_C128: return 16;
+  }
+  return 0;
+}
+
+// Op-program opcodes for the two-layer vertex interpreter (bp_generic.cu).
+enum OpCode { OP_ABSORB = 0, OP_FINAL = 1, OP_FULL = 2 };
+inline uint32_t make_op(int type, int src, int dst, int leg) {
+  return ((uint32_t)type << 28) | ((uint32_t)src << 20) | ((uint32_t)dst << 12) | (uint32_t)leg;
+}
+constexpr int kMaxLegs = 16;
+constexpr int kMaxBufs = 8;
+
+// Arguments of one generic launch (one dtype, one list of work items).
+struct GenericArgs {
+  int layers;
+  const int* off;          // nv + 1
+  const int* rev;          // nslots
+  const int* bond;         // nslots
+  const int* phys;         // nv
+  const long long* toff;   // nv + 1
+  const long long* moff;   // nslots + 1
+  const void* tens;
+  const void* msg_in;
+  void* msg_out;
+  const int* items;        // n_items x (vertex, program offset or leg mask)
+  int n_items;
+  const unsigned* prog;    // programs: [n_ops, op...]
+  int nbuf;                // buffers per CTA including the copy of the site tensor
+  long long buf_elems;     // elements per buffer
+  void* gscratch;          // non-null: buffers live in global memory (gridDim.x slots)
+  int msg_cap;             // elements of incoming-message staging in shared memory
+  int max_d2;              // max D*D (two-layer) or D (one-layer) over slots
+  int normalize;
+  void* zv_out;            // OP_FULL writes one scalar per vertex here
+  double* slot_diff;       // per-slot 1 - |<m_new, m_old>|^2 (nullable)
+  unsigned long long* diff_max;  // order-encoded max of slot_diff (nullable)
+  int* nan_flag;           // set to 1 when a diff is NaN (nullable)
+  const int* done;         // when non-null and *done != 0 the launch does no work
+};
+
+struct LaunchCfg {
+  int grid;
+  int block;
+  size_t smem;
+};
+
+// bp_generic.cu
+size_t generic_smem_bytes(int dtype, const GenericArgs& a, int block, bool buffers_in_smem);
+cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st);
+int generic_max_active(int dtype, int layers, int block, size_t smem);
+
+cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,
+                                const int* eslots, int n_e, const void* msgs, void* ze_out,
+                                cudaStream_t st);
+cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
+                          const int* net_voff, const int* net_vlist, const int* net_eoff,
+                          const int* net_elist, int n_nets, double* logzv, double* logze,
+                          double* totals, int* flags, cudaStream_t st);
+cudaError_t launch_init_messages(int dtype, int layers, int kind, const long long* moff,
+                                 const int* bond, int nslots, void* msgs, cudaStream_t st);
+cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, const void* m1,
+                                const void* m2, double* slot_diff, unsigned long long* dmax,
+                                int* nan_flag, cudaStream_t st);
+cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long long* toff,
+                           const int* rank_off, const int* dims, const long long* sstride,
+                           const void* src, void* dst, cudaStream_t st);
+cudaError_t launch_convergence_check(const unsigned long long* dmax, const int* nan_flag,
+                                     double tol, int iter, int* done, int* at_iter,
+                                     double* delta_out, int* iters_out, cudaStream_t st);
+
+}  // namespace itn

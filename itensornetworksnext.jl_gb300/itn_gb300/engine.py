@@ -1,0 +1,170 @@
+"""Array-level engine over the C ABI: one device context per network.
+
+``BPEngine`` holds a network (``graphs.Graph``), its site tensors and its messages on
+the GPU and exposes the hot-path operations with the reference's semantics:
+``run`` = beliefpropagation (beliefpropagation.jl:69-92), ``message_update`` =
+message_update! (:242-257), ``logscalars`` / ``bethe_free_energy`` =
+messagecache.jl:139-201, ``iterate_diff`` = beliefpropagation.jl:261-267.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .graphs import Graph
+
+_PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16, "tf32": L.PREC_TF32}
+
+
+@dataclass
+class RunResult:
+    iterations: int
+    at_iteration: int
+    delta: float
+    device_ms: float
+    kernel_launches: int
+
+
+class BPEngine:
+    def __init__(self, graph: Graph, device: int = 0):
+        self.lib = L.load()
+        self.graph = graph
+        self._ctx = ctypes.c_void_p()
+        st = self.lib.itn_create(ctypes.byref(self._ctx), int(device), 0)
+        if st != L.ITN_OK:
+            raise L.ItnError(st, f"itn_create failed: {self.lib.itn_status_string(st).decode()}")
+        self._keep = []
+        self.dtype = None
+        g = graph
+        self._off = np.ascontiguousarray(g.off, dtype=np.int64)
+        self._nbr = np.ascontiguousarray(g.nbr, dtype=np.int64)
+        self._bond = np.ascontiguousarray(g.bond, dtype=np.int32)
+        self._rev = np.ascontiguousarray(g.rev, dtype=np.int64)
+        self._phys = np.ascontiguousarray(g.phys, dtype=np.int32)
+        self._net = np.ascontiguousarray(g.net, dtype=np.int32)
+        self._check(self.lib.itn_graph_upload(
+            self._ctx, g.nv, L.ptr(self._off), L.ptr(self._nbr), L.ptr(self._bond),
+            L.ptr(self._rev), L.ptr(self._phys), int(g.layers), L.ptr(self._net)))
+        self.n_undirected = int(np.sum(np.arange(g.nslots) < g.rev))
+
+    # -- life cycle ---------------------------------------------------------------------
+    def close(self):
+        if self._ctx:
+            self.lib.itn_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        L.check(self._ctx, st)
+
+    # -- data ---------------------------------------------------------------------------
+    def set_tensors(self, packed: np.ndarray):
+        a = np.ascontiguousarray(packed)
+        if a.size != int(self.graph.toff[-1]):
+            raise ValueError("packed tensor size does not match the network")
+        code = L.DTYPE_CODE[a.dtype]
+        self._check(self.lib.itn_tensors_upload(self._ctx, code, L.ptr(a)))
+        self.dtype = a.dtype
+
+    def set_tensors_strided(self, arrays, strides, dtype):
+        """arrays[u]: any ndarray whose elements are addressed by ``strides`` (element
+        strides per canonical axis, flattened in vertex order)."""
+        dt = np.dtype(dtype)
+        arrs = [np.asarray(a, dtype=dt) for a in arrays]
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        st = np.ascontiguousarray(strides, dtype=np.int64)
+        self._check(self.lib.itn_tensors_upload_strided(self._ctx, L.DTYPE_CODE[dt], ptrs, L.ptr(st)))
+        self.dtype = dt
+
+    def tensors(self) -> np.ndarray:
+        out = np.empty(int(self.graph.toff[-1]), dtype=self.dtype)
+        self._check(self.lib.itn_tensors_download(self._ctx, L.DTYPE_CODE[self.dtype], L.ptr(out)))
+        return out
+
+    def set_messages(self, packed: np.ndarray):
+        a = np.ascontiguousarray(packed, dtype=self.dtype)
+        if a.size != int(self.graph.moff[-1]):
+            raise ValueError("packed message size does not match the network")
+        self._check(self.lib.itn_messages_upload(self._ctx, L.DTYPE_CODE[self.dtype], L.ptr(a)))
+
+    def init_messages(self, kind: str = "identity_normalized"):
+        k = {"identity_normalized": L.MSG_IDENTITY_NORMALIZED, "identity": L.MSG_IDENTITY,
+             "ones": L.MSG_ONES}[kind]
+        self._check(self.lib.itn_messages_init(self._ctx, k))
+
+    def messages(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(int(self.graph.moff[-1]), dtype=self.dtype)
+        self._check(self.lib.itn_messages_download(self._ctx, L.DTYPE_CODE[self.dtype], L.ptr(out)))
+        return out
+
+    # -- hot path ------------------------------------------------------------------------
+    def run(self, *, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
+            precision="native", split_sweeps=0) -> RunResult:
+        o = L.BpOpts()
+        o.schedule = {"parallel": L.SCHED_PARALLEL, "sequential": L.SCHED_SEQUENTIAL}[schedule]
+        o.maxiter = -1 if maxiter is None else int(maxiter)
+        o.tol = -1.0 if tol is None else float(tol)
+        o.normalize = int(bool(normalize))
+        o.precision = _PREC[precision]
+        o.split_sweeps = int(split_sweeps)
+        ed = None
+        if edges is not None:
+            ed = np.ascontiguousarray(edges, dtype=np.int64)
+            o.edges = ed.ctypes.data
+            o.n_edges = len(ed)
+        r = L.BpResult()
+        self._check(self.lib.itn_bp_run(self._ctx, ctypes.byref(o), ctypes.byref(r)))
+        return RunResult(r.iterations, r.at_iteration, r.delta, r.device_ms, r.kernel_launches)
+
+    def message_update(self, slot: int, normalize: bool = True):
+        self._check(self.lib.itn_message_update(self._ctx, int(slot), int(bool(normalize))))
+
+    def iterate_diff(self, m1, m2) -> float:
+        a = np.ascontiguousarray(m1)
+        b = np.ascontiguousarray(m2, dtype=a.dtype)
+        out = ctypes.c_double()
+        self._check(self.lib.itn_iterate_diff(self._ctx, L.DTYPE_CODE[a.dtype], L.ptr(a), L.ptr(b),
+                                              ctypes.byref(out)))
+        return out.value
+
+    def logscalars(self) -> dict:
+        g = self.graph
+        nn = g.n_nets
+        zv = np.empty(g.nv, dtype=self.dtype)
+        ze = np.empty(self.n_undirected, dtype=self.dtype)
+        lzv = np.empty((g.nv, 2))
+        lze = np.empty((self.n_undirected, 2))
+        tot = np.empty((nn, 2))
+        fl = np.empty(nn, dtype=np.int32)
+        self._check(self.lib.itn_logscalars(self._ctx, L.ptr(zv), L.ptr(ze), L.ptr(lzv), L.ptr(lze),
+                                            L.ptr(tot), L.ptr(fl)))
+        return dict(zv=zv, ze=ze, logzv=lzv, logze=lze, totals=tot, flags=fl)
+
+    def bethe_free_energy(self, net: int | None = None):
+        """bethe_free_energy (messagecache.jl:185-201) of one network (or a list for all)."""
+        r = self.logscalars()
+        out = []
+        for k in range(self.graph.n_nets):
+            f = int(r["flags"][k])
+            if f & 4:
+                out.append(-np.inf)
+                continue
+            re, im = r["totals"][k]
+            cplx = np.iscomplexobj(np.empty(0, self.dtype)) or bool(f & 1) or bool(f & 2)
+            out.append(complex(re, im) if cplx else float(re))
+        return out if net is None and len(out) != 1 else out[0 if net is None else net]

@@ -1,0 +1,61 @@
+"""C-ABI checks that need no GPU: the library builds for sm_103a, loads, exports every
+symbol include/itn_gpu.h declares, and fails cleanly (status code, no abort) when no
+device is present."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "itn_gpu.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int32_t|const char \*|void)\s*\*?\s*(itn_\w+)\s*\(", txt, re.M)))
+
+
+def test_header_lists_entry_points():
+    syms = declared_symbols()
+    assert "itn_bp_run" in syms and "itn_logscalars" in syms and len(syms) >= 15
+
+
+def test_library_exports_declared_symbols(lib_built):
+    lib = ctypes.CDLL(lib_built)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(lib_built):
+    from itn_gb300 import _lib as L
+    assert sorted(L.EXPORTED) == declared_symbols()
+
+
+def test_abi_version_and_status_strings(lib_built):
+    from itn_gb300 import _lib as L
+    lib = L.load(lib_built)
+    assert lib.itn_abi_version() == 1
+    assert lib.itn_status_string(0) == b"ok"
+    assert lib.itn_status_string(1) == b"invalid argument"
+
+
+def test_null_arguments_rejected(lib_built):
+    from itn_gb300 import _lib as L
+    lib = L.load(lib_built)
+    assert lib.itn_create(None, 0, 0) == L.ITN_ERR_ARG
+    assert lib.itn_destroy(None) == L.ITN_ERR_ARG
+    assert lib.itn_bp_run(None, None, None) == L.ITN_ERR_ARG
+    assert lib.itn_last_error(None) == b"null context"
+
+
+def test_create_without_gpu_reports_status(lib_built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from itn_gb300 import _lib as L
+    lib = L.load(lib_built)
+    ctx = ctypes.c_void_p()
+    st = lib.itn_create(ctypes.byref(ctx), 0, 0)
+    assert st == L.ITN_ERR_CUDA and not ctx.value

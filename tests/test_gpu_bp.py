@@ -1,0 +1,260 @@
+"""GPU parity of the CUDA-core BP path against the CPU oracle (C ABI, libitn_gpu.so).
+
+Tolerances: FP64 results agree with the FP64 oracle within 1e-10 relative (messages,
+per-vertex and per-edge log-scalars, total log-norm); FP32 / complex64 results within
+2e-4 relative of the FP64 oracle, measured per message.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from itn_gb300 import BPEngine, ItnArgumentError, ItnError
+from itn_gb300 import generators as GEN
+from itn_gb300 import graphs as G
+from helpers import load_golden, max_rel, msg_rel
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_TOL = 2e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib_built):
+    return lib_built
+
+
+def _engine(g, t, m0):
+    e = BPEngine(g)
+    e.set_tensors(t)
+    e.set_messages(m0)
+    return e
+
+
+def _check_scalars(g, t, m, e, tol):
+    ref = O.logscalars(g, t.astype(np.complex128 if np.iscomplexobj(t) else np.float64),
+                       m.astype(np.complex128 if np.iscomplexobj(t) else np.float64))
+    got = e.logscalars()
+    assert np.max(np.abs(got["logzv"] - ref["logzv"])) < tol * max(1.0, np.max(np.abs(ref["logzv"])))
+    assert np.max(np.abs(got["logze"] - ref["logze"])) < tol * max(1.0, np.max(np.abs(ref["logze"])))
+    assert abs(got["totals"][0][0] - ref["total"][0]) <= tol * max(1.0, abs(ref["total"][0]))
+    assert abs(got["totals"][0][1] - ref["total"][1]) <= tol * max(1.0, abs(ref["total"][1]))
+
+
+def test_golden_peps4x4_parallel_fp64():
+    g, d = load_golden("peps4x4_d2_D2_parallel20.npz")
+    with _engine(g, d["tensors"], d["messages0"]) as e:
+        r = e.run(maxiter=20)
+        assert r.iterations == 20
+        m = e.messages()
+        assert msg_rel(g, m, d["messages"]) < FP64_TOL
+        got = e.logscalars()
+        assert np.max(np.abs(got["logzv"] - d["logzv"])) < FP64_TOL
+        assert abs(got["totals"][0][0] - d["total"][0]) < FP64_TOL * abs(d["total"][0])
+
+
+def test_golden_peps4x4_sequential_fp64():
+    g, d = load_golden("peps4x4_d2_D2_sequential5.npz")
+    with _engine(g, d["tensors"], d["messages0"]) as e:
+        r = e.run(schedule="sequential", edges=d["edges"], maxiter=5)
+        assert r.iterations == 5
+        assert msg_rel(g, e.messages(), d["messages"]) < FP64_TOL
+
+
+def test_golden_complex128():
+    g, d = load_golden("peps3x3_c128_D3_parallel15.npz")
+    with _engine(g, d["tensors"], d["messages0"]) as e:
+        e.run(maxiter=15)
+        assert msg_rel(g, e.messages(), d["messages"]) < FP64_TOL
+        got = e.logscalars()
+        assert np.max(np.abs(got["logzv"] - d["logzv"])) < FP64_TOL * 10
+
+
+def test_golden_spin_ice_single_layer():
+    g, d = load_golden("spinice3_sequential.npz")
+    with _engine(g, d["tensors"], d["messages0"]) as e:
+        r = e.run(schedule="sequential", edges=d["edges"], maxiter=10, tol=1e-10)
+        assert r.iterations == int(d["iterations"])
+        assert msg_rel(g, e.messages(), d["messages"]) < 1e-9
+        z = np.exp(e.bethe_free_energy())
+        assert abs(z / 1.5 ** 9 - 1) < 1e-6
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.float64, FP64_TOL), (np.float32, FP32_TOL),
+                                       (np.complex128, FP64_TOL), (np.complex64, FP32_TOL)])
+def test_peps16x16_D4_parallel(dtype, tol):
+    """16x16 open lattice, d=2, D=4, N(0,1)/sqrt(d D^4); 50 iterations or tol 1e-10."""
+    rng = np.random.default_rng(16)
+    g = G.square_lattice(16, 16, 4, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, dtype, G.peps_scale(g))
+    m0 = G.identity_messages(g, dtype)
+    wide = np.complex128 if np.iscomplexobj(t) else np.float64
+    ref, it, delta, at = O.bp_run(g, t.astype(wide), m0.astype(wide), maxiter=50, tol=1e-10)
+    with _engine(g, t, m0) as e:
+        r = e.run(maxiter=50, tol=1e-10)
+        if dtype in (np.float64, np.complex128):
+            assert r.iterations == it and r.at_iteration == at
+            assert abs(r.delta - delta) < 1e-9
+        m = e.messages()
+        assert msg_rel(g, m, ref) < tol
+        _check_scalars(g, t.astype(wide), ref, e, tol)
+
+
+def test_sequential_matches_oracle_random_order():
+    rng = np.random.default_rng(99)
+    g = G.square_lattice(5, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m0 = G.identity_messages(g)
+    edges = rng.permutation(g.nslots)
+    edges = np.concatenate([edges, edges[:7]])  # repeated slots are allowed
+    ref, *_ = O.bp_run(g, t, m0, schedule="sequential", edges=edges, maxiter=3, tol=1e-14)
+    with _engine(g, t, m0) as e:
+        e.run(schedule="sequential", edges=edges, maxiter=3, tol=1e-14)
+        assert msg_rel(g, e.messages(), ref) < FP64_TOL
+
+
+def test_single_message_update():
+    rng = np.random.default_rng(4)
+    g = G.square_lattice(3, 3, 2, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64)
+    m0 = G.random_messages(g, rng)
+    with _engine(g, t, m0) as e:
+        for s in (0, 5, g.nslots - 1):
+            ref = O.message_update(g, t, e.messages(), s)
+            e.message_update(s)
+            assert msg_rel(g, e.messages(), ref) < FP64_TOL
+        ref = O.message_update(g, t, e.messages(), 3, normalize=False)
+        e.message_update(3, normalize=False)
+        assert msg_rel(g, e.messages(), ref) < FP64_TOL
+
+
+def test_iterate_diff_device():
+    rng = np.random.default_rng(2)
+    g = G.square_lattice(4, 3, 3, phys=2)
+    a = G.random_messages(g, rng)
+    b = G.random_messages(g, rng)
+    with BPEngine(g) as e:
+        e.set_tensors(G.random_tensors(g, rng))
+        assert abs(e.iterate_diff(a, b) - O.iterate_diff(g.moff, a, b)) < 1e-13
+        assert abs(e.iterate_diff(a, a)) <= 10 * np.finfo(float).eps
+
+
+@pytest.mark.parametrize("n", [3, 4])
+def test_spin_ice_gpu(n):
+    rng = np.random.default_rng(123)
+    g = G.square_lattice(n, n, 2, periodic=True, phys=1, layers=1)
+    t = GEN.spin_ice_tensors(g)
+    m0 = G.random_messages(g, rng)
+    with _engine(g, t, m0) as e:
+        e.run(schedule="sequential", edges=G.tree_edge_sequence(g), maxiter=10, tol=1e-10)
+        z = np.exp(e.bethe_free_energy())
+        assert abs(z / 1.5 ** (n * n) - 1) < 1e-6
+
+
+def test_tree_exact_norm_network_gpu():
+    from oracle import contract_oracle as C
+    rng = np.random.default_rng(8)
+    g = G.from_edges(12, G.comb_tree_edges(4, 3), 3, phys=2, layers=2)
+    t = G.random_tensors(g, rng, np.complex128)
+    with _engine(g, t, G.identity_messages(g, np.complex128)) as e:
+        e.run(schedule="sequential", edges=G.tree_edge_sequence(g), maxiter=1)
+        z = np.exp(e.bethe_free_energy())
+        zx = C.contract_norm(g, t)
+        assert abs(z - zx) < 1e-10 * abs(zx)
+
+
+def test_batched_uneven_networks():
+    """Several independent 3-regular networks with per-edge bond dims from {2,3,4,6,8},
+    complex64, in one launch; per-network log-norms against the oracle."""
+    rng = np.random.default_rng(256)
+    nets = []
+    for n in (16, 20, 24):
+        edges = G.random_regular_edges(n, 3, rng)
+        bonds = rng.choice([2, 3, 4, 6, 8], size=len(edges))
+        nets.append(G.from_edges(n, edges, bonds, phys=2))
+    g = G.batched(nets)
+    t = G.random_tensors(g, rng, np.complex64, G.peps_scale(g))
+    m0 = G.identity_messages(g, np.complex64)
+    with _engine(g, t, m0) as e:
+        e.run(maxiter=30)
+        got = e.logscalars()
+        m = e.messages()
+    for k, gk in enumerate(nets):
+        sl = slice(int(np.searchsorted(g.net, k)), int(np.searchsorted(g.net, k, side="right")))
+        v0 = sl.start
+        tk = t[g.toff[v0]:g.toff[sl.stop]].astype(np.complex128)
+        ref, *_ = O.bp_run(gk, tk, G.identity_messages(gk, np.complex128), maxiter=30)
+        s0 = int(g.off[v0])
+        mk = m[g.moff[s0]:g.moff[int(g.off[sl.stop])]]
+        assert msg_rel(gk, mk, ref) < FP32_TOL
+        rr = O.logscalars(gk, tk, ref)
+        assert abs(got["totals"][k][0] - rr["total"][0]) < FP32_TOL * max(1, abs(rr["total"][0]))
+
+
+def test_message_init_kinds():
+    g = G.square_lattice(3, 3, 3, phys=2)
+    with BPEngine(g) as e:
+        e.set_tensors(np.ones(int(g.toff[-1])))
+        e.init_messages("identity_normalized")
+        assert np.array_equal(e.messages(), G.identity_messages(g))
+        e.init_messages("identity")
+        assert np.array_equal(e.messages(), G.identity_messages(g, normalized=False))
+        e.init_messages("ones")
+        assert np.array_equal(e.messages(), G.ones_messages(g))
+
+
+def test_strided_upload_matches_packed():
+    """Column-major tensors with a permuted index order (as a Julia array of an ITensor
+    would arrive) permuted on the device into the canonical layout."""
+    rng = np.random.default_rng(31)
+    g = G.square_lattice(3, 4, 3, phys=2)
+    t = G.random_tensors(g, rng)
+    arrays, strides = [], []
+    for u in range(g.nv):
+        A = t[g.toff[u]:g.toff[u + 1]].reshape(g.tensor_shape(u))
+        perm = rng.permutation(A.ndim)
+        B = np.asfortranarray(np.transpose(A, perm))  # source axes = perm of canonical
+        flat = B.ravel(order="K")
+        # element stride of canonical axis a inside B
+        st_by_src = [s // B.itemsize for s in B.strides]
+        inv = np.argsort(perm)
+        strides.extend(int(st_by_src[inv[a]]) for a in range(A.ndim))
+        arrays.append(flat)
+    with BPEngine(g) as e:
+        e.set_tensors_strided(arrays, strides, np.float64)
+        assert np.array_equal(e.tensors(), t)
+
+
+def test_argument_errors():
+    g = G.square_lattice(3, 3, 2, phys=2)
+    with BPEngine(g) as e:
+        with pytest.raises(ItnError):
+            e.run(maxiter=1)  # no tensors yet
+        e.set_tensors(np.ones(int(g.toff[-1])))
+        e.init_messages()
+        with pytest.raises(ItnArgumentError):
+            e.run()  # neither maxiter nor tol
+        with pytest.raises(ItnArgumentError):
+            e.run(schedule="sequential", edges=[0, 10 ** 6], maxiter=1)
+        with pytest.raises(ItnArgumentError):
+            e.message_update(10 ** 6)
+    bad = G.Graph(2, [0, 1, 2], [1, 0], [2, 3], [1, 0], [2, 2])
+    with pytest.raises(ItnArgumentError):
+        BPEngine(bad)
+
+
+def test_zero_sum_message_is_not_normalised():
+    """A message whose entries sum to zero is stored unnormalised
+    (beliefpropagation.jl:248-253): with A = [[1, -1], [2, -2]] on a one-leg vertex the
+    outgoing message A^T A = [[5, -5], [-5, 5]] sums to zero."""
+    g = G.from_edges(2, [(0, 1)], 2, phys=2)
+    A = np.array([[1.0, -1.0], [2.0, -2.0]])
+    B = np.array([[1.0, 0.0], [0.0, 1.0]])
+    t = np.concatenate([A.ravel(), B.ravel()])
+    m0 = G.identity_messages(g)
+    with _engine(g, t, m0) as e:
+        e.message_update(0)
+        m = e.messages()
+        assert np.array_equal(m[:4], [5.0, -5.0, -5.0, 5.0])
+        ref = O.message_update(g, t, m0.copy(), 0)
+        assert np.array_equal(m, ref)
