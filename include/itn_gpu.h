@@ -147,6 +147,14 @@ int32_t itn_iterate_diff(itn_ctx *ctx, int32_t dtype, const void *m1, const void
 int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *logze,
                        double *totals, int32_t *flags);
 
+/* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product
+ * (M = 128 and M = 64, K = 64) against exact host arithmetic.  m128_ok / m64_ok report
+ * success; max_err is the largest absolute error of the M = 128 product; lane_of_row
+ * (64 entries, may be NULL) receives the TMEM lane of each row of the M = 64
+ * accumulator.  The tensor-core precision modes refuse to run when it fails. */
+int32_t itn_tc_selftest(itn_ctx *ctx, int32_t *m128_ok, int32_t *m64_ok, double *max_err,
+                        int32_t *lane_of_row);
+
 #ifdef __cplusplus
 }
 #endif

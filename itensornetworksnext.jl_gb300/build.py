@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
 SOURCES = ["itn_api.cu", "bp_generic.cu", "bp_tc.cu"]
-HEADERS = ["itn_common.cuh", "itn_internal.h", "itn_tc.h"]
+HEADERS = ["itn_common.cuh", "itn_internal.h", "itn_tc.h", "tc_ptx.cuh"]
 
 
 def nvcc() -> str:

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include "itn_common.cuh"
+#include "itn_conv.cuh"
 #include "itn_internal.h"
 
 namespace itn {
@@ -220,10 +221,10 @@ __device__ void store_message(const GenericArgs& a, const T* out, int n, int slo
     if (lane == 0) {
       const double val = 1.0 - (dre * dre + dim * dim) / (n1 * n2);
       a.slot_diff[slot] = val;
-      if (val != val) {
-        if (a.nan_flag) atomicExch(a.nan_flag, 1);
-      } else if (a.diff_max) {
-        atomicMax(a.diff_max, enc_double(val));
+      if (a.conv) {
+        if (val != val) atomicExch(&a.conv->nan_flag, 1);
+        else atomicMax(&a.conv->dmax, enc_double(val));
+        __threadfence();
       }
     }
   }
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
   const T* tens = reinterpret_cast<const T*>(a.tens);
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
 
-  if (a.done && *reinterpret_cast<const volatile int*>(a.done)) return;
+  if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
@@ -362,6 +363,7 @@ __global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
     }
     __syncthreads();
   }
+  if (a.conv && a.fused_step) conv_finish_cta(a.conv);
 }
 
 // ---- the one-layer kernel ----------------------------------------------------------------
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
   LegMeta* meta = reinterpret_cast<LegMeta*>(smem + L.meta);
   const T* tens = reinterpret_cast<const T*>(a.tens);
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
-  if (a.done && *reinterpret_cast<const volatile int*>(a.done)) return;
+  if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
@@ -450,6 +452,7 @@ __global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
       __syncthreads();
     }
   }
+  if (a.conv && a.fused_step) conv_finish_cta(a.conv);
 }
 
 // ---- edge scalars: Z_e = sum_j m_{u->v}[j] * m_{v->u}[j]  (messagecache.jl:153-157) -----
@@ -558,7 +561,7 @@ __global__ void init_messages_kernel(int layers, int kind, const long long* moff
 
 template <typename T>
 __global__ void iterate_diff_kernel(const long long* moff, int nslots, const T* m1, const T* m2,
-                                    double* slot_diff, unsigned long long* dmax, int* nan_flag) {
+                                    double* slot_diff, ConvState* conv) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nslots) return;
   double n1 = 0, n2 = 0, dre = 0, dim = 0;
@@ -576,8 +579,8 @@ __global__ void iterate_diff_kernel(const long long* moff, int nslots, const T* 
   if (lane == 0) {
     const double val = 1.0 - (dre * dre + dim * dim) / (n1 * n2);
     if (slot_diff) slot_diff[warp] = val;
-    if (val != val) atomicExch(nan_flag, 1);
-    else atomicMax(dmax, enc_double(val));
+    if (val != val) atomicExch(&conv->nan_flag, 1);
+    else atomicMax(&conv->dmax, enc_double(val));
   }
 }
 
@@ -605,21 +608,20 @@ __global__ void permute_kernel(int nv, const long long* soff, const long long* t
   }
 }
 
-__global__ void convergence_check_kernel(unsigned long long* dmax, int* nan_flag, double tol,
-                                         int iter, int* done, int* at_iter, double* delta_out,
-                                         int* iters_out) {
-  if (*done) return;
-  double delta = dec_double(*dmax);
-  if (*nan_flag) delta = nan("");
-  *iters_out = iter;
-  if (delta_out) *delta_out = delta;
-  if (tol >= 0 && delta < tol) {
-    *done = 1;
-    *at_iter = iter;
-  }
-  *dmax = enc_double(-INFINITY);
-  *nan_flag = 0;
+__global__ void reset_state_kernel(ConvState* s, double tol, int use_tol) {
+  s->dmax = enc_double(-INFINITY);
+  s->nan_flag = 0;
+  s->done = 0;
+  s->at_iter = -1;
+  s->iters = 0;
+  s->delta = INFINITY;
+  s->counter = 0;
+  s->tickets = 0;
+  s->tol = tol;
+  s->use_tol = use_tol;
 }
+
+__global__ void step_check_kernel(ConvState* s) { conv_step(s); }
 
 template <typename T>
 cudaError_t launch_generic_t(const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
@@ -720,13 +722,12 @@ cudaError_t launch_init_messages(int dtype, int layers, int kind, const long lon
 }
 
 cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, const void* m1,
-                                const void* m2, double* slot_diff, unsigned long long* dmax,
-                                int* nan_flag, cudaStream_t st) {
+                                const void* m2, double* slot_diff, ConvState* conv, cudaStream_t st) {
   if (nslots <= 0) return cudaSuccess;
   const int block = 256, grid = (nslots * 32 + block - 1) / block;
   ITN_DISPATCH(dtype, iterate_diff_kernel<T><<<grid, block, 0, st>>>(
                           moff, nslots, reinterpret_cast<const T*>(m1),
-                          reinterpret_cast<const T*>(m2), slot_diff, dmax, nan_flag);
+                          reinterpret_cast<const T*>(m2), slot_diff, conv);
                return cudaGetLastError());
 }
 
@@ -741,12 +742,13 @@ cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long 
                return cudaGetLastError());
 }
 
-cudaError_t launch_convergence_check(const unsigned long long* dmax, const int* nan_flag,
-                                     double tol, int iter, int* done, int* at_iter,
-                                     double* delta_out, int* iters_out, cudaStream_t st) {
-  convergence_check_kernel<<<1, 1, 0, st>>>(const_cast<unsigned long long*>(dmax),
-                                            const_cast<int*>(nan_flag), tol, iter, done, at_iter,
-                                            delta_out, iters_out);
+cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st) {
+  reset_state_kernel<<<1, 1, 0, st>>>(s, tol, use_tol);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_check(ConvState* s, cudaStream_t st) {
+  step_check_kernel<<<1, 1, 0, st>>>(s);
   return cudaGetLastError();
 }
 

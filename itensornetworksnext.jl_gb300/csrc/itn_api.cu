@@ -187,17 +187,6 @@ struct itn_ctx {
 
 namespace {
 
-struct ConvState {
-  unsigned long long dmax;
-  int nan_flag;
-  int done;
-  int at_iter;
-  int iters;
-  double delta;
-  int counter;
-  int pad;
-};
-
 int fail(itn_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -312,34 +301,6 @@ int check_ready(itn_ctx* c, bool need_msgs) {
   if (!c->have_tensors) return fail(c, ITN_ERR_STATE, "no site tensors uploaded");
   if (need_msgs && !c->have_messages) return fail(c, ITN_ERR_STATE, "no messages uploaded");
   return ITN_OK;
-}
-
-// Kernel launches that reset the convergence state for a new solve.
-__global__ void reset_state_kernel(ConvState* s) {
-  s->dmax = enc_double(-INFINITY);
-  s->nan_flag = 0;
-  s->done = 0;
-  s->at_iter = -1;
-  s->iters = 0;
-  s->delta = INFINITY;
-  s->counter = 0;
-}
-
-// Convergence check with a device-side iteration counter (graph-position independent).
-__global__ void step_check_kernel(ConvState* s, double tol, int use_tol) {
-  if (s->done) return;
-  const int iter = ++s->counter;
-  s->iters = iter;
-  if (!use_tol) return;
-  double delta = dec_double(s->dmax);
-  if (s->nan_flag) delta = nan("");
-  s->delta = delta;
-  if (delta < tol) {
-    s->done = 1;
-    s->at_iter = iter;
-  }
-  s->dmax = enc_double(-INFINITY);
-  s->nan_flag = 0;
 }
 
 __global__ void copy_kernel(const int4* __restrict__ src, int4* __restrict__ dst, long long n16,
@@ -801,12 +762,9 @@ int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
                              c->d_msg[in].p, c->d_msg[in ^ 1].p))
       return r;
     p.a[in].normalize = o->normalize;
-    p.a[in].done = &conv(c)->done;
-    if (use_tol) {
-      p.a[in].slot_diff = c->d_slot_diff.as<double>();
-      p.a[in].diff_max = &conv(c)->dmax;
-      p.a[in].nan_flag = &conv(c)->nan_flag;
-    }
+    p.a[in].conv = conv(c);
+    p.a[in].fused_step = 1;
+    if (use_tol) p.a[in].slot_diff = c->d_slot_diff.as<double>();
   }
   return ITN_OK;
 }
@@ -827,17 +785,13 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       tr.split = t >= nsweeps - o->split_sweeps;
       tr.normalize = o->normalize;
       tr.slot_diff = use_tol ? c->d_slot_diff.as<double>() : nullptr;
-      tr.diff_max = use_tol ? &conv(c)->dmax : nullptr;
-      tr.nan_flag = use_tol ? &conv(c)->nan_flag : nullptr;
-      tr.done = &conv(c)->done;
+      tr.conv = conv(c);
       cudaError_t e = tc_sweep(c->tc, tr, c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
     } else {
       CK(launch_generic(c->dtype, p.a[in], p.cfg[in], c->stream));
     }
-    step_check_kernel<<<1, 1, 0, c->stream>>>(conv(c), o->tol, use_tol ? 1 : 0);
-    CK(cudaGetLastError());
-    *launches += 2;
+    *launches += 1;
   }
   return ITN_OK;
 }
@@ -855,7 +809,7 @@ int make_seq_launches(itn_ctx* c, const SeqPlan& plan, const itn_bp_opts* o, std
     SeqLaunch L;
     if (int r = plan_generic(c, L.a, L.cfg, plan.items->as<int>() + 2 * b, e - b, m, m)) return r;
     L.a.normalize = o->normalize;
-    L.a.done = &conv(c)->done;
+    L.a.conv = conv(c);  // early exit once converged; the step is a separate launch
     out.push_back(L);
   }
   return ITN_OK;
@@ -885,11 +839,10 @@ int record_sequential(itn_ctx* c, const std::vector<SeqLaunch>& lv, int nsweeps,
     }
     if (use_tol) {
       CK(launch_iterate_diff(c->dtype, c->d_moff.as<long long>(), (int)c->nslots, m, prev,
-                             c->d_slot_diff.as<double>(), &conv(c)->dmax, &conv(c)->nan_flag, c->stream));
+                             c->d_slot_diff.as<double>(), conv(c), c->stream));
       *launches += 1;
     }
-    step_check_kernel<<<1, 1, 0, c->stream>>>(conv(c), o->tol, use_tol ? 1 : 0);
-    CK(cudaGetLastError());
+    CK(launch_step_check(conv(c), c->stream));
     *launches += 1;
   }
   return ITN_OK;
@@ -932,6 +885,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     }
   }
   if (int r = sync_programs(c)) return r;
+  const bool use_tol = o->tol >= 0;
   ParPlan pplan;
   std::vector<SeqLaunch> slaunch;
   if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE) {
@@ -939,10 +893,8 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {
     if (int r = make_seq_launches(c, plan, o, slaunch)) return r;
   }
-  reset_state_kernel<<<1, 1, 0, c->stream>>>(conv(c));
-  CK(cudaGetLastError());
+  CK(launch_reset_state(conv(c), use_tol ? o->tol : -1.0, use_tol ? 1 : 0, c->stream));
   int launches = 1;
-  const bool use_tol = o->tol >= 0;
   const int chunk = o->maxiter >= 0 ? o->maxiter : 64;
   const int64_t cap = o->maxiter >= 0 ? o->maxiter : 1000000;
   int64_t issued = 0;
@@ -988,11 +940,13 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     total_ms += ms;
     // every recorded sweep is 2 launches (parallel) -- count what the graph holds
-    launches += (o->schedule == ITN_SCHED_PARALLEL) ? 2 * n
+    launches += (o->schedule == ITN_SCHED_PARALLEL) ? n
                 : (int)(n * ((plan.level_off.size() - 1) + (use_tol ? 3 : 1)));
     issued += n;
     if (hs.done) break;
   }
+  if (o->precision != ITN_PREC_NATIVE && tc_error_flag(c->tc, c->stream))
+    return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
   // messages now live in buffer (cur + executed sweeps) for the parallel schedule
   if (o->schedule == ITN_SCHED_PARALLEL) c->cur = (c->cur + hs.iters) & 1;
   if (res) {
@@ -1037,13 +991,28 @@ int32_t itn_iterate_diff(itn_ctx* c, int32_t dtype, const void* m1, const void* 
     CK(cudaMemcpyAsync(a.p, m1, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(b.p, m2, bytes, cudaMemcpyHostToDevice, c->stream));
   }
-  reset_state_kernel<<<1, 1, 0, c->stream>>>(conv(c));
+  CK(launch_reset_state(conv(c), -1.0, 0, c->stream));
   CK(launch_iterate_diff(dtype, c->d_moff.as<long long>(), (int)c->nslots, a.p, b.p,
-                         c->d_slot_diff.as<double>(), &conv(c)->dmax, &conv(c)->nan_flag, c->stream));
+                         c->d_slot_diff.as<double>(), conv(c), c->stream));
   ConvState hs;
   CK(cudaMemcpyAsync(&hs, conv(c), sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   *out = hs.nan_flag ? nan("") : dec_double(hs.dmax);
+  return ITN_OK;
+}
+
+int32_t itn_tc_selftest(itn_ctx* c, int32_t* m128_ok, int32_t* m64_ok, double* max_err,
+                        int32_t* lane_of_row) {
+  if (!c) return ITN_ERR_ARG;
+  if (int r = ensure_device(c)) return r;
+  int a = 0, b = 0, lr[64];
+  double mx = 0;
+  CK(tc_run_probe(c->stream, &a, &b, &mx, lr));
+  if (m128_ok) *m128_ok = a;
+  if (m64_ok) *m64_ok = b;
+  if (max_err) *max_err = mx;
+  if (lane_of_row)
+    for (int r = 0; r < 64; ++r) lane_of_row[r] = lr[r];
   return ITN_OK;
 }
 

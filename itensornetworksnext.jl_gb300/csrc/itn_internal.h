@@ -6,6 +6,8 @@
 
 #include <vector>
 
+#include "itn_conv.cuh"
+
 namespace itn {
 
 enum Dtype { DT_F32 = 0, DT_F64 = 1, DT_C64 = 2, DT_C128 = 3 };
@@ -50,9 +52,9 @@ struct GenericArgs {
   int normalize;
   void* zv_out;            // OP_FULL writes one scalar per vertex here
   double* slot_diff;       // per-slot 1 - |<m_new, m_old>|^2 (nullable)
-  unsigned long long* diff_max;  // order-encoded max of slot_diff (nullable)
-  int* nan_flag;           // set to 1 when a diff is NaN (nullable)
-  const int* done;         // when non-null and *done != 0 the launch does no work
+  ConvState* conv;         // outer-loop state: early exit when done and the diff max
+                           // (nullable: neither)
+  int fused_step;          // non-zero: the last CTA performs the outer-loop step
 };
 
 struct LaunchCfg {
@@ -76,13 +78,11 @@ cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int
 cudaError_t launch_init_messages(int dtype, int layers, int kind, const long long* moff,
                                  const int* bond, int nslots, void* msgs, cudaStream_t st);
 cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, const void* m1,
-                                const void* m2, double* slot_diff, unsigned long long* dmax,
-                                int* nan_flag, cudaStream_t st);
+                                const void* m2, double* slot_diff, ConvState* conv, cudaStream_t st);
 cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long long* toff,
                            const int* rank_off, const int* dims, const long long* sstride,
                            const void* src, void* dst, cudaStream_t st);
-cudaError_t launch_convergence_check(const unsigned long long* dmax, const int* nan_flag,
-                                     double tol, int iter, int* done, int* at_iter,
-                                     double* delta_out, int* iters_out, cudaStream_t st);
+cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st);
+cudaError_t launch_step_check(ConvState* s, cudaStream_t st);
 
 }  // namespace itn

@@ -6,6 +6,7 @@
 namespace itn {
 
 struct TcEngine;
+struct ConvState;
 
 struct TcRun {
   const void* msg_in;
@@ -13,10 +14,8 @@ struct TcRun {
   int precision;  // ITN_PREC_BF16 or ITN_PREC_TF32
   bool split;     // hi/lo split-precision sweep
   int normalize;
-  double* slot_diff;
-  unsigned long long* diff_max;
-  int* nan_flag;
-  const int* done;
+  double* slot_diff;  // per-slot diffs (null: no convergence test)
+  ConvState* conv;    // outer-loop state (done flag, diff max, iteration step)
 };
 
 TcEngine* tc_create();
@@ -31,5 +30,10 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
                        int precision, cudaStream_t st, const char** why);
 // Enqueue one sweep (all directed messages) on the stream.
 cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st);
+// Non-zero when a bounded wait inside the tensor-core kernel gave up.
+int tc_error_flag(TcEngine* e, cudaStream_t st);
+// One-CTA tcgen05 self-test (cached per process): M=128 product exact, M=64
+// accumulator lane map found.  lane_of_row may be null (64 entries otherwise).
+cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max_err, int* lane_of_row);
 
 }  // namespace itn

@@ -31,7 +31,7 @@ EXPORTED = [
     "itn_synchronize", "itn_graph_upload", "itn_graph_info", "itn_tensors_upload",
     "itn_tensors_upload_strided", "itn_tensors_download", "itn_messages_upload",
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
-    "itn_iterate_diff", "itn_logscalars",
+    "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest",
 ]
 
 
@@ -87,6 +87,7 @@ def _declare(lib):
         "itn_message_update": (_I32, [_VP, _I64, _I32]),
         "itn_iterate_diff": (_I32, [_VP, _I32, _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logscalars": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+        "itn_tc_selftest": (_I32, [_VP, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -142,6 +142,17 @@ class BPEngine:
                                               ctypes.byref(out)))
         return out.value
 
+    def tc_selftest(self) -> dict:
+        """Run the one-CTA tcgen05 self-test (exact BF16 products, M=64 lane map)."""
+        a = ctypes.c_int32()
+        b = ctypes.c_int32()
+        err = ctypes.c_double()
+        lanes = np.empty(64, dtype=np.int32)
+        self._check(self.lib.itn_tc_selftest(self._ctx, ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(err), L.ptr(lanes)))
+        return dict(m128_ok=bool(a.value), m64_ok=bool(b.value), max_err=err.value,
+                    lane_of_row=lanes)
+
     def logscalars(self) -> dict:
         g = self.graph
         nn = g.n_nets
