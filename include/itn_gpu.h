@@ -147,6 +147,40 @@ int32_t itn_iterate_diff(itn_ctx *ctx, int32_t dtype, const void *m1, const void
 int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *logze,
                        double *totals, int32_t *flags);
 
+/* Gradient of the Bethe log-norm (bethe_free_energy, messagecache.jl:185-201) with
+ * respect to every site tensor, for the converged messages currently held.  No
+ * counterpart in the reference (it has no AD); this is the backward rule the Julia
+ * shim's ChainRulesCore.rrule(bethe_free_energy ∘ beliefpropagation) calls.
+ * The direct term dlogZ_u/dA_u is always computed; with adjoint != 0 the implicit
+ * (adjoint BP) correction lambda^T dF/dA is added, lambda solving
+ * lambda = dL/dm + J^T lambda by fixed-point iteration until the relative change is
+ * below tol (ITN_ERR_TIMEOUT after maxiter).  normalized: the messages come from
+ * SimpleMessageUpdate(normalize = true).  Real dtypes, norm networks (layers = 2). */
+typedef struct {
+  int32_t adjoint;
+  int32_t maxiter;
+  double tol;
+  int32_t normalized;
+  int32_t reserved0;
+} itn_grad_opts;
+
+typedef struct {
+  int32_t adjoint_iterations;
+  int32_t reserved0;
+  double adjoint_residual;
+  double device_ms;
+} itn_grad_result;
+
+int32_t itn_bp_grad(itn_ctx *ctx, const itn_grad_opts *opts, void *grad_packed,
+                    itn_grad_result *result);
+
+/* Vector-Jacobian product of one parallel sweep m -> F(m) (every message recomputed
+ * by message_update!, beliefpropagation.jl:242-257, divided by its sum when normalized)
+ * at the current messages: cot_in = J^T cot_out, both packed like the messages.  No
+ * counterpart in the reference (no AD); it is the pullback an rrule of a BP sweep needs
+ * and the inner step of the adjoint iteration of itn_bp_grad.  Real dtypes, layers = 2. */
+int32_t itn_sweep_vjp(itn_ctx *ctx, int32_t normalized, const void *cot_out, void *cot_in);
+
 /* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product
  * (M = 128 and M = 64, K = 64) against exact host arithmetic.  m128_ok / m64_ok report
  * success; max_err is the largest absolute error of the M = 128 product; lane_of_row

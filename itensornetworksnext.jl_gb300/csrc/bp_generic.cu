@@ -21,6 +21,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "itn_common.cuh"
 #include "itn_conv.cuh"
 #include "itn_internal.h"
@@ -364,6 +366,236 @@ __global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
     __syncthreads();
   }
   if (a.conv && a.fused_step) conv_finish_cta(a.conv);
+}
+
+// ---- dual-number interpreter (real types): value and tangent planes ------------------------
+// Forward-mode companion of bp2_kernel used by the adjoint / gradient path.  Every logical
+// buffer b has a value plane (b) and a tangent plane (b + nbuf); the site tensor (buffer 0)
+// has no tangent.  Leg l is absorbed with (m_l, dm_l): the value message m_{w->u} from the
+// incoming slot and the tangent from d.tan_in at the *outgoing* slot u -> w.
+//   FINAL(src, w): the tangent part of the message on leg w, unnormalised, stored at the
+//                  incoming slot rev(u -> w) of d.tan_out (the cotangent of m_{w->u});
+//   DUMP(src)    : grad[u] += plane(src) * (dump_tangent ? 1 : 1 / Z_u).
+template <typename T, int D>
+__device__ __forceinline__ void absorb_dual_fixed(const T* __restrict__ src, const T* __restrict__ srcT,
+                                                  T* __restrict__ dst, T* __restrict__ dstT, int outer,
+                                                  int inner, const T* __restrict__ m,
+                                                  const T* __restrict__ dm) {
+  T mr[D * D], dr[D * D];
+#pragma unroll
+  for (int j = 0; j < D * D; ++j) {
+    mr[j] = m[j];
+    dr[j] = dm[j];
+  }
+  const int n = outer * inner;
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    const int o = p / inner, i = p - o * inner;
+    const int base = o * D * inner + i;
+    T t[D], dt[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      t[k] = src[base + k * inner];
+      dt[k] = srcT ? srcT[base + k * inner] : T(0);
+    }
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      T acc = 0, dacc = 0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        acc = fmac(t[k], mr[b * D + k], acc);
+        dacc = fmac(dt[k], mr[b * D + k], fmac(t[k], dr[b * D + k], dacc));
+      }
+      dst[base + b * inner] = acc;
+      dstT[base + b * inner] = dacc;
+    }
+  }
+}
+
+template <typename T>
+__device__ void absorb_dual_rt(const T* __restrict__ src, const T* __restrict__ srcT, T* __restrict__ dst,
+                               T* __restrict__ dstT, int outer, int D, int inner, const T* __restrict__ m,
+                               const T* __restrict__ dm) {
+  const int n = outer * inner;
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    const int o = p / inner, i = p - o * inner;
+    const int base = o * D * inner + i;
+    for (int b = 0; b < D; ++b) {
+      T acc = 0, dacc = 0;
+      for (int k = 0; k < D; ++k) {
+        const T t = src[base + k * inner], dt = srcT ? srcT[base + k * inner] : T(0);
+        acc = fmac(t, m[b * D + k], acc);
+        dacc = fmac(dt, m[b * D + k], fmac(t, dm[b * D + k], dacc));
+      }
+      dst[base + b * inner] = acc;
+      dstT[base + b * inner] = dacc;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dispatch_absorb_dual(const T* src, const T* srcT, T* dst, T* dstT, int outer,
+                                                     int D, int inner, const T* m, const T* dm) {
+  switch (D) {
+    case 2: absorb_dual_fixed<T, 2>(src, srcT, dst, dstT, outer, inner, m, dm); break;
+    case 3: absorb_dual_fixed<T, 3>(src, srcT, dst, dstT, outer, inner, m, dm); break;
+    case 4: absorb_dual_fixed<T, 4>(src, srcT, dst, dstT, outer, inner, m, dm); break;
+    case 6: absorb_dual_fixed<T, 6>(src, srcT, dst, dstT, outer, inner, m, dm); break;
+    case 8: absorb_dual_fixed<T, 8>(src, srcT, dst, dstT, outer, inner, m, dm); break;
+    default: absorb_dual_rt<T>(src, srcT, dst, dstT, outer, D, inner, m, dm); break;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  // the dual launch sizes nbuf for both planes: nbuf = 2 * logical buffers
+  const SmemLayout L = smem_layout<T>(a, blockDim.x, a.gscratch == nullptr);
+  const int nb = a.nbuf / 2;
+  T* bufs = a.gscratch ? reinterpret_cast<T*>(a.gscratch) + (size_t)blockIdx.x * a.nbuf * a.buf_elems
+                       : reinterpret_cast<T*>(smem + L.bufs);
+  T* msgs = reinterpret_cast<T*>(smem + L.msgs);  // [value | tangent] staging
+  T* out = reinterpret_cast<T*>(smem + L.out);
+  T* red = reinterpret_cast<T*>(smem + L.red);
+  LegMeta* meta = reinterpret_cast<LegMeta*>(smem + L.meta);
+  const T* tens = reinterpret_cast<const T*>(a.tens);
+  const T* min_ = reinterpret_cast<const T*>(a.msg_in);
+  const T* tin = reinterpret_cast<const T*>(d.tan_in);
+  const int half = a.msg_cap / 2;
+
+  for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
+    const int u = a.items[2 * it];
+    const unsigned* prog = a.prog + a.items[2 * it + 1];
+    if (threadIdx.x == 0) {
+      const int s0 = a.off[u];
+      const int z = a.off[u + 1] - s0;
+      meta->z = z;
+      meta->d = a.phys[u];
+      int n = meta->d, mo = 0;
+      for (int l = 0; l < z; ++l) {
+        meta->dims[l] = a.bond[s0 + l];
+        n *= meta->dims[l];
+        meta->moffs[l] = mo;
+        mo += meta->dims[l] * meta->dims[l];
+      }
+      meta->n = n;
+      int inner = 1;
+      for (int l = z - 1; l >= 0; --l) {
+        meta->inner[l] = inner;
+        inner *= meta->dims[l];
+      }
+      for (int l = 0; l < z; ++l) meta->outer[l] = n / (meta->inner[l] * meta->dims[l]);
+    }
+    __syncthreads();
+    const int z = meta->z, n = meta->n;
+    const T* A_g = tens + a.toff[u];
+    T* A = bufs;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+    const int s0 = a.off[u];
+    for (int l = 0; l < z; ++l) {
+      const int Dl = meta->dims[l], D2 = Dl * Dl;
+      const T* src = min_ + a.moff[a.rev[s0 + l]];
+      const T* tsrc = tin ? tin + a.moff[s0 + l] : nullptr;
+      for (int j = threadIdx.x; j < D2; j += blockDim.x) {
+        const int jj = d.transpose ? (j % Dl) * Dl + j / Dl : j;
+        msgs[meta->moffs[l] + j] = src[jj];
+        msgs[half + meta->moffs[l] + j] = tsrc ? tsrc[jj] : T(0);
+      }
+    }
+    __syncthreads();
+    const int nops = (int)prog[0];
+    for (int q = 1; q <= nops; ++q) {
+      const unsigned op = prog[q];
+      const int type = op >> 28, srcb = (op >> 20) & 0xff, dstb = (op >> 12) & 0xff,
+                leg = op & 0xfff;
+      const T* src = bufs + (size_t)srcb * a.buf_elems;
+      const T* srcT = srcb == 0 ? nullptr : bufs + (size_t)(srcb + nb) * a.buf_elems;
+      if (type == OP_ABSORB) {
+        T* dst = bufs + (size_t)dstb * a.buf_elems;
+        T* dstT = bufs + (size_t)(dstb + nb) * a.buf_elems;
+        dispatch_absorb_dual<T>(src, srcT, dst, dstT, meta->outer[leg], meta->dims[leg], meta->inner[leg],
+                                msgs + meta->moffs[leg], msgs + half + meta->moffs[leg]);
+        __syncthreads();
+      } else if (type == OP_FINAL) {
+        const int D = meta->dims[leg];
+        if (srcT) {
+          dispatch_final<T>(srcT, A, meta->outer[leg], D, meta->inner[leg], out, red);
+        } else {
+          for (int e = threadIdx.x; e < D * D; e += blockDim.x) out[e] = T(0);
+          __syncthreads();
+        }
+        T* dst = reinterpret_cast<T*>(d.tan_out) + a.moff[a.rev[s0 + leg]];
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+          dst[e] = d.transpose ? out[(e % D) * D + e / D] : out[e];
+        __syncthreads();
+      } else if (type == OP_DUMP) {
+        const T* plane = d.dump_tangent ? srcT : src;
+        const T scale = d.dump_tangent ? T(1) : T(1) / reinterpret_cast<const T*>(d.zv)[u];
+        T* g = reinterpret_cast<T*>(d.grad_out) + a.toff[u];
+        if (plane)
+          for (int j = threadIdx.x; j < n; j += blockDim.x) g[j] += plane[j] * scale;
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// per slot s: S_s = sum(U_s); F_s = U_s / S_s (U_s when S_s == 0 or not normalising)
+template <typename T>
+__global__ void grad_prep_kernel(const long long* moff, int nslots, const T* U, T* F, T* S, int normalize) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nslots) return;
+  T sum = 0;
+  for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) sum += U[j];
+  sum = warp_sum(sum);
+  const bool sc = normalize && sum != T(0);
+  for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) F[j] = sc ? U[j] / sum : U[j];
+  if (lane == 0) S[warp] = sc ? sum : T(1);
+}
+
+// g_t = U_{rev t} / Z_{nbr t} - m_{rev t} / Z_{e(t)}   (dL/dm for the message on slot t)
+template <typename T>
+__global__ void grad_g_kernel(const long long* moff, const int* rev, const int* dst_vertex, const int* eidx,
+                              int nslots, const T* U, const T* m, const T* zv, const T* ze, T* g) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nslots) return;
+  const int r = rev[warp];
+  const T iz = T(1) / zv[dst_vertex[warp]], ie = T(1) / ze[eidx[warp]];
+  const long long n = moff[warp + 1] - moff[warp];
+  for (long long j = lane; j < n; j += 32) g[moff[warp] + j] = U[moff[r] + j] * iz - m[moff[r] + j] * ie;
+}
+
+// mu_s = (lambda_s - <lambda_s, F_s>) / S_s  (normalised updates) or lambda_s
+template <typename T>
+__global__ void grad_mu_kernel(const long long* moff, int nslots, const T* lam, const T* F, const T* S, T* mu,
+                               int normalize) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nslots) return;
+  T dot = 0;
+  if (normalize)
+    for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) dot += lam[j] * F[j];
+  dot = warp_sum(dot);
+  const T is = T(1) / S[warp];
+  for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) mu[j] = (lam[j] - dot) * is;
+}
+
+// lambda <- g + cot; stats[0] = max |change|, stats[1] = max |lambda| (order-encoded)
+template <typename T>
+__global__ void grad_update_kernel(long long n, const T* g, const T* cot, T* lam, unsigned long long* stats) {
+  double dmax = 0, lmax = 0;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    const T v = g[j] + cot[j];
+    dmax = fmax(dmax, fabs((double)(v - lam[j])));
+    lmax = fmax(lmax, fabs((double)v));
+    lam[j] = v;
+  }
+  dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
+  for (int o = 8; o >= 1; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+  for (int o = 16; o >= 1; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&stats[0], enc_double(dmax));
+    atomicMax(&stats[1], enc_double(lmax));
+  }
 }
 
 // ---- the one-layer kernel ----------------------------------------------------------------
@@ -740,6 +972,79 @@ cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long 
                           nv, soff, toff, rank_off, dims, sstride,
                           reinterpret_cast<const T*>(src), reinterpret_cast<T*>(dst));
                return cudaGetLastError());
+}
+
+
+cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg, cudaStream_t st) {
+  if (cfg.grid <= 0 || a.n_items <= 0) return cudaSuccess;
+  if (dtype == DT_F32) {
+    cudaError_t e = cudaFuncSetAttribute(bp2_dual_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    bp2_dual_kernel<float><<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
+  } else if (dtype == DT_F64) {
+    cudaError_t e = cudaFuncSetAttribute(bp2_dual_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    bp2_dual_kernel<double><<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+int dual_max_active(int dtype, int block, size_t smem) {
+  int n = 0;
+  if (dtype == DT_F32) {
+    cudaFuncSetAttribute(bp2_dual_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_dual_kernel<float>, block, smem);
+  } else {
+    cudaFuncSetAttribute(bp2_dual_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_dual_kernel<double>, block, smem);
+  }
+  return n;
+}
+
+#define ITN_REAL_DISPATCH(dtype, ...)                    \
+  switch (dtype) {                                       \
+    case DT_F32: { using T = float; __VA_ARGS__; }       \
+    case DT_F64: { using T = double; __VA_ARGS__; }      \
+    default: return cudaErrorInvalidValue;               \
+  }
+
+cudaError_t launch_grad_prep(int dtype, const long long* moff, int nslots, const void* U, void* F, void* S,
+                             int normalize, cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  const int grid = (nslots * 32 + 255) / 256;
+  ITN_REAL_DISPATCH(dtype, grad_prep_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)U, (T*)F, (T*)S,
+                                                                    normalize);
+                    return cudaGetLastError());
+}
+
+cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, const int* dst_vertex, const int* eidx,
+                          int nslots, const void* U, const void* m, const void* zv, const void* ze, void* g,
+                          cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  const int grid = (nslots * 32 + 255) / 256;
+  ITN_REAL_DISPATCH(dtype, grad_g_kernel<T><<<grid, 256, 0, st>>>(moff, rev, dst_vertex, eidx, nslots, (const T*)U,
+                                                                 (const T*)m, (const T*)zv, (const T*)ze, (T*)g);
+                    return cudaGetLastError());
+}
+
+cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const void* lam, const void* F,
+                           const void* S, void* mu, int normalize, cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  const int grid = (nslots * 32 + 255) / 256;
+  ITN_REAL_DISPATCH(dtype, grad_mu_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)lam, (const T*)F,
+                                                                  (const T*)S, (T*)mu, normalize);
+                    return cudaGetLastError());
+}
+
+cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
+                               unsigned long long* stats, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 1024);
+  ITN_REAL_DISPATCH(dtype, grad_update_kernel<T><<<grid, 256, 0, st>>>(n, (const T*)g, (const T*)cot, (T*)lam,
+                                                                      stats);
+                    return cudaGetLastError());
 }
 
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st) {

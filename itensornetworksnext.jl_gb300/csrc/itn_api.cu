@@ -102,13 +102,15 @@ struct ProgGen {
   }
 };
 
-Program make_program(int z, uint32_t mask, bool full) {
+// kind 0: outgoing messages for the legs in mask (leave-one-out); 1: vertex scalar
+// (absorb every leg, FULL); 2: absorb every leg, DUMP (gradient of Z_u).
+Program make_program(int z, uint32_t mask, int kind) {
   ProgGen g;
-  if (full) {
+  if (kind != 0) {
     std::vector<int> all;
     for (int l = 0; l < z; ++l) all.push_back(l);
     int b = g.absorb_chain(0, all);
-    g.ops.push_back(make_op(OP_FULL, b, 0, 0));
+    g.ops.push_back(make_op(kind == 1 ? OP_FULL : OP_DUMP, b, 0, 0));
   } else {
     std::vector<int> others, req;
     for (int l = 0; l < z; ++l) ((mask >> l) & 1u ? req : others).push_back(l);
@@ -153,8 +155,12 @@ struct itn_ctx {
   bool prog_dirty = true;
   int nbuf = 1;
   int msg_cap = 1;
-  std::vector<int> items_par, items_scal;
-  DevBuf d_items_par, d_items_scal;
+  std::vector<int> items_par, items_scal, items_dump;
+  DevBuf d_items_par, d_items_scal, d_items_dump;
+  std::vector<int> slot_dst, slot_eidx;  // per slot: destination vertex, undirected edge index
+  DevBuf d_slot_dst, d_slot_eidx;
+  // gradient work buffers
+  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_cot, d_stats;
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
   // data
@@ -222,11 +228,11 @@ int upload_vec(itn_ctx* c, DevBuf& b, const std::vector<T>& v, cudaStream_t st) 
   return ITN_OK;
 }
 
-int program_offset(itn_ctx* c, int z, uint32_t mask, bool full) {
-  const uint32_t key = full ? 0x80000000u : mask;
+int program_offset(itn_ctx* c, int z, uint32_t mask, int kind) {
+  const uint32_t key = kind == 1 ? 0x80000000u : kind == 2 ? 0x40000000u : mask;
   auto it = c->prog_index.find({z, key});
   if (it != c->prog_index.end()) return it->second;
-  Program p = make_program(z, mask, full);
+  Program p = make_program(z, mask, kind);
   const int offv = (int)c->prog_host.size();
   c->prog_host.push_back((uint32_t)p.ops.size());
   c->prog_host.insert(c->prog_host.end(), p.ops.begin(), p.ops.end());
@@ -502,6 +508,7 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
   c->nbuf = 1;
   c->items_par.clear();
   c->items_scal.clear();
+  c->items_dump.clear();
   c->seq_plans.clear();
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
@@ -511,10 +518,12 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
     if (layers == 2) {
       if (z > 0) {
         c->items_par.push_back((int)u);
-        c->items_par.push_back(program_offset(c, z, full, false));
+        c->items_par.push_back(program_offset(c, z, full, 0));
       }
       c->items_scal.push_back((int)u);
-      c->items_scal.push_back(program_offset(c, z, 0, true));
+      c->items_scal.push_back(program_offset(c, z, 0, 1));
+      c->items_dump.push_back((int)u);
+      c->items_dump.push_back(program_offset(c, z, 0, 2));
     } else {
       if (z > 0) {
         c->items_par.push_back((int)u);
@@ -536,8 +545,22 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       (r = upload_vec(c, c->d_net_voff, voff, c->stream)) || (r = upload_vec(c, c->d_net_vlist, vlist, c->stream)) ||
       (r = upload_vec(c, c->d_net_eoff, eoff, c->stream)) || (r = upload_vec(c, c->d_net_elist, elist, c->stream)) ||
       (r = upload_vec(c, c->d_items_par, c->items_par, c->stream)) ||
-      (r = upload_vec(c, c->d_items_scal, c->items_scal, c->stream)) || (r = sync_programs(c)))
+      (r = upload_vec(c, c->d_items_scal, c->items_scal, c->stream)) ||
+      (r = upload_vec(c, c->d_items_dump, c->items_dump, c->stream)) || (r = sync_programs(c)))
     return r;
+  {
+    std::vector<int> epos(ns, -1);
+    for (size_t e = 0; e < c->eslots.size(); ++e) epos[c->eslots[e]] = (int)e;
+    c->slot_dst.assign(ns, 0);
+    c->slot_eidx.assign(ns, 0);
+    for (int64_t t = 0; t < ns; ++t) {
+      c->slot_dst[t] = (int)c->nbr[t];
+      c->slot_eidx[t] = epos[std::min<int64_t>(t, c->rev[t])];
+    }
+    if ((r = upload_vec(c, c->d_slot_dst, c->slot_dst, c->stream)) ||
+        (r = upload_vec(c, c->d_slot_eidx, c->slot_eidx, c->stream)))
+      return r;
+  }
   CK(c->d_slot_diff.ensure(std::max<int64_t>(ns, 1) * sizeof(double)));
   CK(cudaStreamSynchronize(c->stream));
   c->have_graph = true;
@@ -735,7 +758,7 @@ int get_seq_plan(itn_ctx* c, const int64_t* edges, int64_t n, SeqPlan& plan) {
       const int z = (int)(c->off[u + 1] - c->off[u]);
       const int leg = (int)(s - c->off[u]);
       items.push_back((int)u);
-      items.push_back(c->layers == 2 ? program_offset(c, z, 1u << leg, false) : (int)(1u << leg));
+      items.push_back(c->layers == 2 ? program_offset(c, z, 1u << leg, 0) : (int)(1u << leg));
     }
     loff.push_back((int)items.size() / 2);
   }
@@ -1001,6 +1024,214 @@ int32_t itn_iterate_diff(itn_ctx* c, int32_t dtype, const void* m1, const void* 
   return ITN_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Z_u (vertex_scalar) into d_zv and Z_e (edge_scalar) into d_ze for the messages m.
+int compute_scalars(itn_ctx* c, const void* m) {
+  const size_t es = dtype_size(c->dtype);
+  const int ne = (int)c->eslots.size();
+  CK(c->d_zv.ensure(std::max<int64_t>(c->nv, 1) * es));
+  CK(c->d_ze.ensure(std::max(ne, 1) * es));
+  if (c->nv > 0) {
+    GenericArgs a;
+    LaunchCfg cfg;
+    if (int r = plan_generic(c, a, cfg, c->d_items_scal.as<int>(), (int)c->items_scal.size() / 2, m,
+                             const_cast<void*>(m)))
+      return r;
+    a.zv_out = c->d_zv.p;
+    CK(launch_generic(c->dtype, a, cfg, c->stream));
+  }
+  CK(launch_edge_scalars(c->dtype, c->layers, c->d_moff.as<long long>(), c->d_rev.as<int>(),
+                         c->d_eslots.as<int>(), ne, m, c->d_ze.p, c->stream));
+  return ITN_OK;
+}
+
+// Launch plan of the dual-number interpreter (two planes per buffer, two message stagings).
+int plan_dual(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items, int n_items, const void* m) {
+  memset(&a, 0, sizeof(a));
+  a.layers = 2;
+  a.off = c->d_off.as<int>();
+  a.rev = c->d_rev.as<int>();
+  a.bond = c->d_bond.as<int>();
+  a.phys = c->d_phys.as<int>();
+  a.toff = c->d_toff.as<long long>();
+  a.moff = c->d_moff.as<long long>();
+  a.tens = c->d_tens.p;
+  a.msg_in = m;
+  a.items = d_items;
+  a.n_items = n_items;
+  a.prog = c->d_prog.as<unsigned>();
+  a.nbuf = 2 * c->nbuf;
+  a.buf_elems = (c->max_tensor + 15) & ~15LL;
+  a.msg_cap = 2 * c->msg_cap;
+  a.max_d2 = c->max_d2;
+  cfg.block = block_for(c);
+  bool in_smem = true;
+  size_t smem = generic_smem_bytes(c->dtype, a, cfg.block, true);
+  if (smem > (size_t)c->smem_optin) {
+    in_smem = false;
+    smem = generic_smem_bytes(c->dtype, a, cfg.block, false);
+    if (smem > (size_t)c->smem_optin)
+      return fail(c, ITN_ERR_UNSUPPORTED, "vertex needs %zu bytes of shared staging", smem);
+  }
+  int per_sm = dual_max_active(c->dtype, cfg.block, smem);
+  if (per_sm <= 0) per_sm = 1;
+  cfg.grid = std::max(1, std::min(n_items, c->sm_count * per_sm));
+  cfg.smem = smem;
+  if (!in_smem) {
+    const size_t need = (size_t)cfg.grid * a.nbuf * a.buf_elems * dtype_size(c->dtype);
+    CK(c->d_scratch.ensure(need));
+    a.gscratch = c->d_scratch.p;
+  }
+  return ITN_OK;
+}
+
+// Unnormalised updates U = M(m) of one parallel sweep, their sums S and F = U / S.
+int adjoint_prepare(itn_ctx* c, const void* m, int normalized) {
+  const size_t mb = (size_t)c->moff[c->nslots] * dtype_size(c->dtype);
+  const int ns = (int)c->nslots, np = (int)c->items_par.size() / 2;
+  CK(c->d_U.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_F.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_mu.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_cot.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_S.ensure(std::max<size_t>(ns, 1) * dtype_size(c->dtype)));
+  GenericArgs pa;
+  LaunchCfg pcfg;
+  if (int r = plan_generic(c, pa, pcfg, c->d_items_par.as<int>(), np, m, c->d_U.p)) return r;
+  pa.normalize = 0;
+  CK(launch_generic(c->dtype, pa, pcfg, c->stream));
+  CK(launch_grad_prep(c->dtype, c->d_moff.as<long long>(), ns, c->d_U.p, c->d_F.p, c->d_S.p, normalized,
+                      c->stream));
+  return ITN_OK;
+}
+
+// cot = J^T lam for the sweep m -> F(m) (needs adjoint_prepare): lam is projected through
+// the normalisation (mu = (lam - <lam, F>) / S) and pushed back through the products by
+// the dual interpreter (tangent of the leave-one-out contraction on every leg).
+int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normalized) {
+  const int ns = (int)c->nslots, np = (int)c->items_par.size() / 2;
+  CK(launch_grad_mu(c->dtype, c->d_moff.as<long long>(), ns, lam, c->d_F.p, c->d_S.p, c->d_mu.p, normalized,
+                    c->stream));
+  GenericArgs da;
+  LaunchCfg dcfg;
+  if (int r = plan_dual(c, da, dcfg, c->d_items_par.as<int>(), np, m)) return r;
+  DualArgs dd;
+  memset(&dd, 0, sizeof(dd));
+  dd.tan_in = c->d_mu.p;
+  dd.tan_out = cot;
+  CK(launch_dual(c->dtype, da, dd, dcfg, c->stream));
+  return ITN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t itn_sweep_vjp(itn_ctx* c, int32_t normalized, const void* cot_out, void* cot_in) {
+  if (int r = check_ready(c, true)) return r;
+  if (!cot_out || !cot_in) return fail(c, ITN_ERR_ARG, "null cotangent pointer");
+  if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
+    return fail(c, ITN_ERR_UNSUPPORTED, "the sweep VJP is implemented for real site tensors");
+  if (c->layers != 2) return fail(c, ITN_ERR_UNSUPPORTED, "the sweep VJP is implemented for norm networks");
+  if (int r = ensure_device(c)) return r;
+  const size_t mb = (size_t)c->moff[c->nslots] * dtype_size(c->dtype);
+  const void* m = c->d_msg[c->cur].p;
+  if (int r = adjoint_prepare(c, m, normalized)) return r;
+  CK(c->d_lam.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_g.ensure(std::max<size_t>(mb, 16)));
+  if (mb) CK(cudaMemcpyAsync(c->d_lam.p, cot_out, mb, cudaMemcpyHostToDevice, c->stream));
+  if (int r = apply_jt(c, m, c->d_lam.p, c->d_g.p, normalized)) return r;
+  if (mb) CK(cudaMemcpyAsync(cot_in, c->d_g.p, mb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ITN_OK;
+}
+
+int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_result* res) {
+  if (int r = check_ready(c, true)) return r;
+  if (!grad) return fail(c, ITN_ERR_ARG, "null gradient pointer");
+  if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
+    return fail(c, ITN_ERR_UNSUPPORTED, "the gradient is implemented for real site tensors");
+  if (c->layers != 2) return fail(c, ITN_ERR_UNSUPPORTED, "the gradient is implemented for norm networks");
+  if (int r = ensure_device(c)) return r;
+  itn_grad_opts def = {1, 200, 1e-10, 1, 0};
+  if (!o) o = &def;
+  const int dt = c->dtype;
+  const size_t es = dtype_size(dt);
+  const size_t tb = (size_t)c->toff[c->nv] * es, mb = (size_t)c->moff[c->nslots] * es;
+  const int ns = (int)c->nslots;
+  const void* m = c->d_msg[c->cur].p;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  if (int r = compute_scalars(c, m)) return r;
+  CK(c->d_grad.ensure(std::max<size_t>(tb, 16)));
+  CK(cudaMemsetAsync(c->d_grad.p, 0, tb, c->stream));
+  const int nd = (int)c->items_dump.size() / 2, np = (int)c->items_par.size() / 2;
+  // direct term: dlogZ_u/dA_u = (T_u(m) + T_u(m^T)) / Z_u
+  GenericArgs a;
+  LaunchCfg cfg;
+  if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
+  DualArgs d;
+  memset(&d, 0, sizeof(d));
+  d.grad_out = c->d_grad.p;
+  d.zv = c->d_zv.p;
+  for (int tr = 0; tr < 2; ++tr) {
+    d.transpose = tr;
+    CK(launch_dual(dt, a, d, cfg, c->stream));
+  }
+  int iters = 0;
+  double resid = 0.0;
+  if (o->adjoint) {
+    CK(c->d_g.ensure(std::max<size_t>(mb, 16)));
+    CK(c->d_lam.ensure(std::max<size_t>(mb, 16)));
+    CK(c->d_stats.ensure(2 * sizeof(unsigned long long)));
+    if (int r = adjoint_prepare(c, m, o->normalized)) return r;
+    // g = dL/dm, lambda_0 = g
+    CK(launch_grad_g(dt, c->d_moff.as<long long>(), c->d_rev.as<int>(), c->d_slot_dst.as<int>(),
+                     c->d_slot_eidx.as<int>(), ns, c->d_U.p, m, c->d_zv.p, c->d_ze.p, c->d_g.p, c->stream));
+    CK(cudaMemcpyAsync(c->d_lam.p, c->d_g.p, mb, cudaMemcpyDeviceToDevice, c->stream));
+    const unsigned long long init[2] = {0x8000000000000000ull, 0x8000000000000000ull};  // enc(+0.0)
+    // adjoint BP: lambda <- g + J^T lambda  until the relative change is below tol
+    for (iters = 0; iters < std::max(o->maxiter, 0);) {
+      if (int r = apply_jt(c, m, c->d_lam.p, c->d_cot.p, o->normalized)) return r;
+      CK(cudaMemcpyAsync(c->d_stats.p, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+      CK(launch_grad_update(dt, (long long)c->moff[c->nslots], c->d_g.p, c->d_cot.p, c->d_lam.p,
+                            c->d_stats.as<unsigned long long>(), c->stream));
+      unsigned long long hs[2];
+      CK(cudaMemcpyAsync(hs, c->d_stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      ++iters;
+      const double dmax = dec_double(hs[0]), lmax = dec_double(hs[1]);
+      resid = lmax > 0 ? dmax / lmax : 0.0;
+      if (!(resid == resid)) return fail(c, ITN_ERR_NAN, "adjoint iteration produced NaN");
+      if (resid < o->tol) break;
+    }
+    // correction lambda^T dF/dA: tangent part of the all-legs contraction with mu
+    CK(launch_grad_mu(dt, c->d_moff.as<long long>(), ns, c->d_lam.p, c->d_F.p, c->d_S.p, c->d_mu.p,
+                      o->normalized, c->stream));
+    d.tan_in = c->d_mu.p;
+    d.dump_tangent = 1;
+    for (int tr = 0; tr < 2; ++tr) {
+      d.transpose = tr;
+      CK(launch_dual(dt, a, d, cfg, c->stream));
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  if (tb) CK(cudaMemcpyAsync(grad, c->d_grad.p, tb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (res) {
+    res->adjoint_iterations = iters;
+    res->adjoint_residual = resid;
+    res->device_ms = ms;
+  }
+  if (o->adjoint && o->maxiter > 0 && !(resid < o->tol))
+    return fail(c, ITN_ERR_TIMEOUT, "adjoint iteration did not reach tol %g in %d iterations (residual %g)",
+                o->tol, o->maxiter, resid);
+  return ITN_OK;
+}
+
 int32_t itn_tc_selftest(itn_ctx* c, int32_t* m128_ok, int32_t* m64_ok, double* max_err,
                         int32_t* lane_of_row) {
   if (!c) return ITN_ERR_ARG;
@@ -1022,22 +1253,11 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
   if (int r = ensure_device(c)) return r;
   const size_t es = dtype_size(c->dtype);
   const int ne = (int)c->eslots.size();
-  CK(c->d_zv.ensure(std::max<int64_t>(c->nv, 1) * es));
-  CK(c->d_ze.ensure(std::max(ne, 1) * es));
   CK(c->d_logzv.ensure(std::max<int64_t>(c->nv, 1) * 2 * sizeof(double)));
   CK(c->d_logze.ensure(std::max(ne, 1) * 2 * sizeof(double)));
   CK(c->d_tot.ensure(c->n_nets * 2 * sizeof(double)));
   CK(c->d_flags.ensure(c->n_nets * sizeof(int)));
-  void* m = c->d_msg[c->cur].p;
-  if (c->nv > 0) {
-    GenericArgs a;
-    LaunchCfg cfg;
-    if (int r = plan_generic(c, a, cfg, c->d_items_scal.as<int>(), (int)c->items_scal.size() / 2, m, m)) return r;
-    a.zv_out = c->d_zv.p;
-    CK(launch_generic(c->dtype, a, cfg, c->stream));
-  }
-  CK(launch_edge_scalars(c->dtype, c->layers, c->d_moff.as<long long>(), c->d_rev.as<int>(),
-                         c->d_eslots.as<int>(), ne, m, c->d_ze.p, c->stream));
+  if (int r = compute_scalars(c, c->d_msg[c->cur].p)) return r;
   CK(launch_logsum(c->dtype, c->d_zv.p, c->d_ze.p, (int)c->nv, ne, c->d_net_voff.as<int>(),
                    c->d_net_vlist.as<int>(), c->d_net_eoff.as<int>(), c->d_net_elist.as<int>(), c->n_nets,
                    c->d_logzv.as<double>(), c->d_logze.as<double>(), c->d_tot.as<double>(),

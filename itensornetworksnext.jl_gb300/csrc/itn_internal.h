@@ -22,7 +22,7 @@ inline size_t dtype_size(int dt) {
 }
 
 // Op-program opcodes for the two-layer vertex interpreter (bp_generic.cu).
-enum OpCode { OP_ABSORB = 0, OP_FINAL = 1, OP_FULL = 2 };
+enum OpCode { OP_ABSORB = 0, OP_FINAL = 1, OP_FULL = 2, OP_DUMP = 3 };
 inline uint32_t make_op(int type, int src, int dst, int leg) {
   return ((uint32_t)type << 28) | ((uint32_t)src << 20) | ((uint32_t)dst << 12) | (uint32_t)leg;
 }
@@ -57,6 +57,16 @@ struct GenericArgs {
   int fused_step;          // non-zero: the last CTA performs the outer-loop step
 };
 
+// Extra arguments of the dual-number (forward-mode) interpreter used by the gradient.
+struct DualArgs {
+  const void* tan_in;  // tangent per outgoing slot (mu_{u->v}); null = zero tangents
+  void* tan_out;       // FINAL: tangent of the message on leg w, stored at slot rev(u->w)
+  int transpose;       // stage m^T and mu^T (second orientation of the real gradient)
+  void* grad_out;      // DUMP target (packed canonical tensors)
+  const void* zv;      // per-vertex Z_u (DUMP of the value plane scales by 1/Z_u)
+  int dump_tangent;    // DUMP the tangent plane (unscaled) instead of the value plane
+};
+
 struct LaunchCfg {
   int grid;
   int block;
@@ -82,6 +92,18 @@ cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, co
 cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long long* toff,
                            const int* rank_off, const int* dims, const long long* sstride,
                            const void* src, void* dst, cudaStream_t st);
+cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg,
+                        cudaStream_t st);
+int dual_max_active(int dtype, int block, size_t smem);
+cudaError_t launch_grad_prep(int dtype, const long long* moff, int nslots, const void* U, void* F, void* S,
+                             int normalize, cudaStream_t st);
+cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, const int* dst_vertex,
+                          const int* eidx, int nslots, const void* U, const void* m, const void* zv,
+                          const void* ze, void* g, cudaStream_t st);
+cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const void* lam, const void* F,
+                           const void* S, void* mu, int normalize, cudaStream_t st);
+cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
+                               unsigned long long* stats, cudaStream_t st);
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st);
 cudaError_t launch_step_check(ConvState* s, cudaStream_t st);
 

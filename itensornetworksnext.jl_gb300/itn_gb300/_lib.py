@@ -31,7 +31,8 @@ EXPORTED = [
     "itn_synchronize", "itn_graph_upload", "itn_graph_info", "itn_tensors_upload",
     "itn_tensors_upload_strided", "itn_tensors_download", "itn_messages_upload",
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
-    "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest",
+    "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest", "itn_bp_grad",
+    "itn_sweep_vjp",
 ]
 
 
@@ -51,6 +52,16 @@ class BpOpts(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("split_sweeps", ctypes.c_int32),
                 ("reserved0", ctypes.c_int32), ("edges", ctypes.c_void_p),
                 ("n_edges", ctypes.c_int64)]
+
+
+class GradOpts(ctypes.Structure):
+    _fields_ = [("adjoint", ctypes.c_int32), ("maxiter", ctypes.c_int32), ("tol", ctypes.c_double),
+                ("normalized", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
+
+
+class GradResult(ctypes.Structure):
+    _fields_ = [("adjoint_iterations", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("adjoint_residual", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
 class BpResult(ctypes.Structure):
@@ -88,6 +99,8 @@ def _declare(lib):
         "itn_iterate_diff": (_I32, [_VP, _I32, _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logscalars": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
         "itn_tc_selftest": (_I32, [_VP, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP]),
+        "itn_bp_grad": (_I32, [_VP, ctypes.POINTER(GradOpts), _VP, ctypes.POINTER(GradResult)]),
+        "itn_sweep_vjp": (_I32, [_VP, _I32, _VP, _VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

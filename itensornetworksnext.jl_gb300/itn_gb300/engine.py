@@ -142,6 +142,23 @@ class BPEngine:
                                               ctypes.byref(out)))
         return out.value
 
+    def grad(self, *, adjoint=True, maxiter=200, tol=1e-10, normalized=True):
+        """Gradient of bethe_free_energy w.r.t. every site tensor at the current
+        (converged) messages; returns (packed gradient, info dict)."""
+        o = L.GradOpts(int(bool(adjoint)), int(maxiter), float(tol), int(bool(normalized)), 0)
+        r = L.GradResult()
+        out = np.empty(int(self.graph.toff[-1]), dtype=self.dtype)
+        self._check(self.lib.itn_bp_grad(self._ctx, ctypes.byref(o), L.ptr(out), ctypes.byref(r)))
+        return out, dict(adjoint_iterations=r.adjoint_iterations, adjoint_residual=r.adjoint_residual,
+                         device_ms=r.device_ms)
+
+    def sweep_vjp(self, cot_out, normalized=True) -> np.ndarray:
+        """J^T cot_out for one parallel sweep at the current messages."""
+        a = np.ascontiguousarray(cot_out, dtype=self.dtype)
+        out = np.empty_like(a)
+        self._check(self.lib.itn_sweep_vjp(self._ctx, int(bool(normalized)), L.ptr(a), L.ptr(out)))
+        return out
+
     def tc_selftest(self) -> dict:
         """Run the one-CTA tcgen05 self-test (exact BF16 products, M=64 lane map)."""
         a = ctypes.c_int32()

@@ -1,0 +1,145 @@
+"""Gradient of the converged BP log-norm w.r.t. every site tensor (itn_bp_grad).
+
+The reference has no gradient, so the check is central finite differences (step 1e-4,
+FP64) of the converged Bethe log-norm, evaluated by FP64 GPU solves whose parity with
+the oracle is covered by test_gpu_bp.py.  Bounds: FP64 gradient within 1e-6 relative of
+FD per direction; the 12x12 D=6 FP32 gradient (FP64 log-scalars) within 1e-5.
+"""
+import numpy as np
+import pytest
+
+from itn_gb300 import BPEngine
+from itn_gb300 import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib_built):
+    return lib_built
+
+
+def _logz(g, t, tol=1e-14, maxiter=2000):
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=maxiter, tol=tol)
+        return e.bethe_free_energy()
+
+
+def _numpy_direct(g, t, m):
+    """(T_u(m) + T_u(m^T)) / Z_u with T_u = A_u absorbed with all incoming messages."""
+    grad = np.zeros_like(t)
+    for u in range(g.nv):
+        A = t[g.toff[u]:g.toff[u + 1]].reshape(g.tensor_shape(u))
+        for tr in (0, 1):
+            T = A.copy()
+            for l in range(g.degree(u)):
+                s = g.off[u] + l
+                mm = m[g.moff[g.rev[s]]:g.moff[g.rev[s] + 1]].reshape(g.bond[s], g.bond[s])
+                T = np.moveaxis(np.tensordot(T, mm.T if tr else mm, axes=([1 + l], [1])), -1, 1 + l)
+            grad[g.toff[u]:g.toff[u + 1]] += (T / np.sum(T * A)).ravel()
+    return grad
+
+
+def test_direct_term_matches_numpy():
+    rng = np.random.default_rng(1)
+    g = G.square_lattice(3, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m0 = G.identity_messages(g) + 0.01 * G.random_messages(g, rng)  # non-symmetric
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.set_messages(m0)
+        e.run(maxiter=3)
+        m = e.messages()
+        grad, info = e.grad(adjoint=False)
+    ref = _numpy_direct(g, t, m)
+    assert np.max(np.abs(grad - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_fp64_gradient_against_finite_differences():
+    rng = np.random.default_rng(2)
+    g = G.square_lattice(4, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=2000, tol=1e-14)
+        grad, info = e.grad(adjoint=True, tol=1e-12)
+    h = 1e-4
+    for _ in range(6):
+        d = rng.standard_normal(t.size)
+        d /= np.linalg.norm(d)
+        fd = (_logz(g, t + h * d) - _logz(g, t - h * d)) / (2 * h)
+        assert abs(grad @ d - fd) <= 1e-6 * abs(fd), (grad @ d, fd)
+
+
+@pytest.mark.parametrize("normalized", [True, False])
+def test_sweep_vjp_against_finite_differences(normalized):
+    """<lam, J v> from central differences of one sweep equals <J^T lam, v>."""
+    rng = np.random.default_rng(3)
+    g = G.square_lattice(3, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m0 = G.identity_messages(g) + 0.05 * G.random_messages(g, rng)
+    lam = rng.standard_normal(m0.size)
+    v = rng.standard_normal(m0.size)
+    h = 1e-6
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.set_messages(m0)
+        jt = e.sweep_vjp(lam, normalized=normalized)
+        outs = []
+        for sgn in (1, -1):
+            e.set_messages(m0 + sgn * h * v)
+            e.run(maxiter=1, normalize=normalized)
+            outs.append(e.messages())
+    jv = (outs[0] - outs[1]) / (2 * h)
+    assert abs(lam @ jv - jt @ v) <= 1e-7 * max(abs(lam @ jv), 1e-12)
+
+
+def test_adjoint_fixed_point_equation():
+    """The adjoint solution satisfies lambda = dL/dm + J^T lambda; at a BP fixed point
+    dL/dm vanishes, so the gradient equals its direct term."""
+    rng = np.random.default_rng(4)
+    g = G.square_lattice(4, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=6)
+        g_direct, _ = e.grad(adjoint=False)
+        g_adj, info = e.grad(adjoint=True, tol=1e-13)
+        e.run(maxiter=2000, tol=1e-15)
+        g_conv_d, _ = e.grad(adjoint=False)
+        g_conv_a, info2 = e.grad(adjoint=True, tol=1e-13)
+    assert info["adjoint_iterations"] >= 1
+    assert np.max(np.abs(g_adj - g_direct)) > 1e-8  # the correction is active off the fixed point
+    # the fidelity tolerance 1e-15 pins message directions to ~sqrt(1e-15) ~ 3e-8, so the
+    # remaining correction is of that order
+    assert np.max(np.abs(g_conv_a - g_conv_d)) <= 1e-6 * np.max(np.abs(g_conv_d))
+
+
+def test_peps12x12_D6_fp32_gradient():
+    """12x12 open PEPS, d=2, D=6, FP32 messages and gradient, FP64 log-scalars; checked
+    against central FD (step 1e-4, FP64 solves) on 32 random unit directions."""
+    rng = np.random.default_rng(12)
+    g = G.square_lattice(12, 12, 6, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    with BPEngine(g) as e:
+        e.set_tensors(t.astype(np.float32))
+        e.init_messages()
+        r = e.run(maxiter=500, tol=1e-12)
+        grad, info = e.grad(adjoint=True, tol=1e-6)
+    h = 1e-4
+    gd, fds = [], []
+    for _ in range(32):
+        d = rng.standard_normal(t.size)
+        d /= np.linalg.norm(d)
+        fds.append((_logz(g, t + h * d) - _logz(g, t - h * d)) / (2 * h))
+        gd.append(grad.astype(np.float64) @ d)
+    gd, fds = np.array(gd), np.array(fds)
+    rel = np.linalg.norm(gd - fds) / np.linalg.norm(fds)
+    print(f"12x12 D=6 fp32 gradient: BP {r.iterations} sweeps, adjoint {info['adjoint_iterations']} its, "
+          f"grad {info['device_ms']:.3f} ms, rel err vs FD over 32 directions {rel:.2e} "
+          f"(worst direction {np.max(np.abs(gd - fds)) / np.max(np.abs(fds)):.2e} of the largest)")
+    assert rel <= 1e-5
