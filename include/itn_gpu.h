@@ -181,6 +181,29 @@ int32_t itn_bp_grad(itn_ctx *ctx, const itn_grad_opts *opts, void *grad_packed,
  * and the inner step of the adjoint iteration of itn_bp_grad.  Real dtypes, layers = 2. */
 int32_t itn_sweep_vjp(itn_ctx *ctx, int32_t normalized, const void *cot_out, void *cot_in);
 
+/* Bethe log-norm (bethe_free_energy) of a network whose graph, tensors and messages are
+ * already in device memory, computed without allocating device memory.  No counterpart
+ * in the reference.  For callers whose GPU memory is owned by their own pooling allocator
+ * (a CUDA.jl memory pool, a serving process that reserves HBM up front), where a library
+ * cudaMalloc would fail or escape the pool.  All intermediates live in one process-wide
+ * 16 MiB __device__ array: every GPU that loads the library holds it until exit, and
+ * networks needing more (vertex + edge scalars + two contraction planes of
+ * max_tensor_elems for one CTA) are rejected with ITN_ERR_ARG and a message in errbuf.
+ * The first call on a device sets up the array's address (call it before any stream
+ * capture); calls that overlap on the GPU race on the array and must be ordered.
+ * Device arrays use the layout of itn_graph_upload / itn_tensors_upload: int32 d_off
+ * (nv+1), d_rev, d_bond (per slot), d_phys (nv); int64 d_toff (nv+1), d_moff (nslots+1);
+ * max_tensor_elems bounds every vertex's tensor.  Outputs: d_total = (re, im) of
+ * sum log Zv - sum log Ze, d_flags as in itn_logscalars.  Work is enqueued on `stream`
+ * (a cudaStream_t, may be NULL) and the outputs are ready when it completes. */
+int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int32_t layers,
+                                int64_t nv, int64_t nslots, int64_t max_tensor_elems,
+                                const int32_t *d_off, const int32_t *d_rev, const int32_t *d_bond,
+                                const int32_t *d_phys, const int64_t *d_toff,
+                                const int64_t *d_moff, const void *d_tensors,
+                                const void *d_messages, double *d_total, int32_t *d_flags,
+                                char *errbuf, int32_t errbuf_len);
+
 /* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product
  * (M = 128 and M = 64, K = 64) against exact host arithmetic.  m128_ok / m64_ok report
  * success; max_err is the largest absolute error of the M = 128 product; lane_of_row

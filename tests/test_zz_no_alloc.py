@@ -1,0 +1,102 @@
+"""itn_logz_static_scratch: the Bethe log-norm computed without any device allocation.
+
+It serves callers whose GPU memory is owned by their own pooling allocator (a CUDA.jl
+memory pool, a serving process that reserves HBM at start-up), where a cudaMalloc inside
+the library would fail or bypass the pool.  The test hands it device buffers (allocated
+here by torch, standing in for such a pool) and checks its result against the context
+entry point itn_logscalars on two calls in a row -- the second call reuses the shared
+static scratch left by the first.  Tolerances as elsewhere: 1e-10 relative in FP64,
+2e-4 in FP32.  Collected last on purpose (file name) so a stop-at-first-failure run has
+already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from itn_gb300 import BPEngine
+from itn_gb300 import _lib as L
+from itn_gb300 import generators as GEN
+from itn_gb300 import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib(lib_built):
+    return L.load(lib_built)
+
+
+def _dev(torch, arr):
+    return torch.from_numpy(np.ascontiguousarray(arr)).cuda()
+
+
+def _static_logz(lib, torch, g, t, m, code):
+    dev = dict(
+        off=_dev(torch, g.off.astype(np.int32)), rev=_dev(torch, g.rev.astype(np.int32)),
+        bond=_dev(torch, g.bond.astype(np.int32)), phys=_dev(torch, g.phys.astype(np.int32)),
+        toff=_dev(torch, g.toff.astype(np.int64)), moff=_dev(torch, g.moff.astype(np.int64)),
+        tens=_dev(torch, t), msgs=_dev(torch, m))
+    total = torch.zeros(2, dtype=torch.float64, device="cuda")
+    flags = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    err = ctypes.create_string_buffer(256)
+    stream = torch.cuda.current_stream().cuda_stream
+    max_tensor = int(np.max(np.diff(g.toff)))
+    results = []
+    for _ in range(2):  # two calls in a row share the static scratch
+        total.zero_()
+        st = lib.itn_logz_static_scratch(
+            0, stream, code, int(g.layers), g.nv, g.nslots, max_tensor,
+            dev["off"].data_ptr(), dev["rev"].data_ptr(), dev["bond"].data_ptr(), dev["phys"].data_ptr(),
+            dev["toff"].data_ptr(), dev["moff"].data_ptr(), dev["tens"].data_ptr(), dev["msgs"].data_ptr(),
+            total.data_ptr(), flags.data_ptr(), err, len(err))
+        assert st == L.ITN_OK, err.value
+        torch.cuda.synchronize()
+        results.append((total.cpu().numpy().copy(), int(flags.cpu().item())))
+    return results
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.float64, 1e-10), (np.float32, 2e-4)])
+def test_static_scratch_matches_logscalars(lib, dtype, tol):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(7)
+    g = G.square_lattice(6, 6, 4, periodic=True, phys=2)
+    t = G.random_tensors(g, rng, dtype, G.peps_scale(g))
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=25)
+        m = e.messages()
+        ref = e.logscalars()
+    code = L.DTYPE_CODE[np.dtype(dtype)]
+    for total, flags in _static_logz(lib, torch, g, t, m, code):
+        assert flags == int(ref["flags"][0])
+        assert abs(total[0] - ref["totals"][0][0]) <= tol * abs(ref["totals"][0][0])
+        assert abs(total[1] - ref["totals"][0][1]) <= tol * max(1.0, abs(ref["totals"][0][1]))
+
+
+def test_static_scratch_plain_network(lib):
+    """One-layer network (spin ice on a 4x4 torus) through the same entry point."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(123)
+    g = G.square_lattice(4, 4, 2, periodic=True, phys=1, layers=1)
+    t = GEN.spin_ice_tensors(g)
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.set_messages(G.random_messages(g, rng))
+        e.run(schedule="sequential", edges=G.tree_edge_sequence(g), maxiter=10, tol=1e-10)
+        m = e.messages()
+        ref = e.logscalars()
+    for total, flags in _static_logz(lib, torch, g, t, m, L.F64):
+        assert abs(total[0] - ref["totals"][0][0]) <= 1e-10 * abs(ref["totals"][0][0])
+
+
+def test_static_scratch_rejects_oversized_network(lib):
+    torch = pytest.importorskip("torch")
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    err = ctypes.create_string_buffer(256)
+    p = x.data_ptr()
+    st = lib.itn_logz_static_scratch(0, None, L.F64, 2, 4, 8, 10 ** 7, p, p, p, p, p, p, p, p, p, p,
+                                     err, len(err))
+    assert st == L.ITN_ERR_ARG
+    assert b"static scratch" in err.value
