@@ -147,6 +147,30 @@ int32_t itn_iterate_diff(itn_ctx *ctx, int32_t dtype, const void *m1, const void
 int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *logze,
                        double *totals, int32_t *flags);
 
+/* contract_network ordering: contraction_order(tn; alg) (src/contract_network.jl:39-58) on
+ * host data only (no device work).  Tensor t has ranks[t] indices; labels/dims list them
+ * tensor after tensor; an index shared by two tensors is contracted, one on a single tensor
+ * stays open.  alg 0 = Greedy (pair with the smallest growth, pairs sharing an index first),
+ * 1 = LeftAssociative.  steps_out (2 * (n - 1) ints): step k contracts positions
+ * (steps_out[2k], steps_out[2k+1]) of a working list from which both are removed and to
+ * which the result (labels: free of the first ++ free of the second) is appended. */
+int32_t itn_contraction_order(int32_t n_tensors, const int32_t *ranks, const int64_t *labels,
+                              const int64_t *dims, int32_t alg, int32_t *steps_out);
+
+/* contract_network(tn; alg = Exact(order, order_alg)) (src/contract_network.jl:7-37): exact
+ * contraction by pairwise GPU contractions (device permute + GEMM).  tensors[t] are host
+ * row-major arrays in the order of their labels.  alg 0 = Greedy, 1 = LeftAssociative,
+ * 2 = explicit `steps` (the itn_contraction_order format).  precision: ITN_PREC_NATIVE
+ * (dtype arithmetic on CUDA cores) or ITN_PREC_BF16 (float32 data, tcgen05 GEMM with BF16
+ * hi/lo split operands).  The result (row-major in the order of out_labels, at most 48
+ * indices) is copied to `out` if out_capacity elements suffice; device_ms (may be NULL)
+ * receives the device time of the pairwise steps. */
+int32_t itn_contract_network(itn_ctx *ctx, int32_t dtype, int32_t n_tensors, const int32_t *ranks,
+                             const int64_t *labels, const int64_t *dims, const void *const *tensors,
+                             int32_t alg, const int32_t *steps, int32_t precision, void *out,
+                             int64_t out_capacity, int32_t *out_rank, int64_t *out_labels,
+                             int64_t *out_dims, double *device_ms);
+
 /* Gradient of the Bethe log-norm (bethe_free_energy, messagecache.jl:185-201) with
  * respect to every site tensor, for the converged messages currently held.  No
  * counterpart in the reference (it has no AD); this is the backward rule the Julia

@@ -23,6 +23,7 @@
 #include "itn_common.cuh"
 #include "itn_internal.h"
 #include "itn_tc.h"
+#include "itn_contract.h"
 
 using namespace itn;
 
@@ -1270,6 +1271,213 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
   if (flags) CK(cudaMemcpyAsync(flags, c->d_flags.p, c->n_nets * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return ITN_OK;
+}
+
+}  // extern "C"
+
+// ---- contract_network -------------------------------------------------------------------------
+namespace {
+
+struct NetIn {
+  std::vector<std::vector<int64_t>> labels, dims;
+  std::map<int64_t, int64_t> dim;
+};
+
+int read_network(itn_ctx* c, int32_t n, const int32_t* ranks, const int64_t* labels, const int64_t* dims,
+                 NetIn& net) {
+  if (n < 1) return fail(c, ITN_ERR_ARG, "contract_network needs at least one tensor");
+  if (!ranks || (!labels && n > 0) || !dims) return fail(c, ITN_ERR_ARG, "null label/dim arrays");
+  std::map<int64_t, int> count;
+  int64_t pos = 0;
+  for (int32_t t = 0; t < n; ++t) {
+    if (ranks[t] < 0 || ranks[t] > 48) return fail(c, ITN_ERR_ARG, "tensor %d has rank %d (max 48)", t, ranks[t]);
+    std::vector<int64_t> l(labels + pos, labels + pos + ranks[t]), d(dims + pos, dims + pos + ranks[t]);
+    for (int a = 0; a < ranks[t]; ++a) {
+      if (d[a] < 1) return fail(c, ITN_ERR_ARG, "non-positive dimension");
+      auto it = net.dim.find(l[a]);
+      if (it != net.dim.end() && it->second != d[a])
+        return fail(c, ITN_ERR_ARG, "index %lld has dimensions %lld and %lld", (long long)l[a],
+                    (long long)it->second, (long long)d[a]);
+      net.dim[l[a]] = d[a];
+      if (++count[l[a]] > 2) return fail(c, ITN_ERR_UNSUPPORTED, "index %lld appears on more than two tensors", (long long)l[a]);
+      for (int b = 0; b < a; ++b)
+        if (l[b] == l[a]) return fail(c, ITN_ERR_UNSUPPORTED, "repeated index %lld within one tensor", (long long)l[a]);
+    }
+    net.labels.push_back(l);
+    net.dims.push_back(d);
+    pos += ranks[t];
+  }
+  return ITN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t itn_contraction_order(int32_t n, const int32_t* ranks, const int64_t* labels, const int64_t* dims,
+                              int32_t alg, int32_t* steps_out) {
+  if (!steps_out && n > 1) return ITN_ERR_ARG;
+  if (alg != 0 && alg != 1) return ITN_ERR_ARG;
+  NetIn net;
+  if (int r = read_network(nullptr, n, ranks, labels, dims, net)) return r;
+  std::vector<std::pair<int, int>> steps;
+  contraction_order(net.labels, net.dim, alg, steps);
+  for (size_t k = 0; k < steps.size(); ++k) {
+    steps_out[2 * k] = steps[k].first;
+    steps_out[2 * k + 1] = steps[k].second;
+  }
+  return ITN_OK;
+}
+
+int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t* ranks, const int64_t* labels,
+                             const int64_t* dims, const void* const* tensors, int32_t alg, const int32_t* steps_in,
+                             int32_t precision, void* out, int64_t out_capacity, int32_t* out_rank,
+                             int64_t* out_labels, int64_t* out_dims, double* device_ms) {
+  if (!c) return ITN_ERR_ARG;
+  if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
+  if (precision != ITN_PREC_NATIVE && !(precision == ITN_PREC_BF16 && dtype == ITN_F32))
+    return fail(c, ITN_ERR_UNSUPPORTED, "contract_network precision %d needs float32 data (BF16 split)", precision);
+  if (!tensors || !out_rank) return fail(c, ITN_ERR_ARG, "null pointer");
+  if (alg != 0 && alg != 1 && alg != 2) return fail(c, ITN_ERR_ARG, "unknown order algorithm %d", alg);
+  if (int r = ensure_device(c)) return r;
+  NetIn net;
+  if (int r = read_network(c, n, ranks, labels, dims, net)) return r;
+  std::vector<std::pair<int, int>> steps;
+  if (alg == 2) {
+    if (!steps_in && n > 1) return fail(c, ITN_ERR_ARG, "explicit order needs steps");
+    int live = n;
+    for (int k = 0; k + 1 < n; ++k) {
+      const int i = steps_in[2 * k], j = steps_in[2 * k + 1];
+      if (i < 0 || j < 0 || i >= live || j >= live || i == j) return fail(c, ITN_ERR_ARG, "bad contraction step %d", k);
+      steps.push_back({i, j});
+      --live;
+    }
+  } else {
+    contraction_order(net.labels, net.dim, alg, steps);
+  }
+  const size_t es = dtype_size(dtype);
+  struct Item {
+    void* p;
+    std::vector<int64_t> l, d;
+  };
+  std::vector<Item> W;
+  auto numel = [](const std::vector<int64_t>& d) {
+    int64_t x = 1;
+    for (int64_t v : d) x *= v;
+    return x;
+  };
+  auto release_all = [&]() {
+    for (auto& it : W)
+      if (it.p) cudaFreeAsync(it.p, c->stream);
+    W.clear();
+  };
+  for (int t = 0; t < n; ++t) {
+    Item it{nullptr, net.labels[t], net.dims[t]};
+    const size_t bytes = (size_t)numel(it.d) * es;
+    if (!tensors[t]) {
+      release_all();
+      return fail(c, ITN_ERR_ARG, "null tensor %d", t);
+    }
+    cudaError_t e = cudaMallocAsync(&it.p, std::max<size_t>(bytes, 16), c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(it.p, tensors[t], bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+      W.push_back(it);
+      release_all();
+      return cuda_fail(c, e, "contract_network upload");
+    }
+    W.push_back(it);
+  }
+  CK(cudaEventRecord(c->ev0, c->stream));
+  for (auto& st : steps) {
+    Item& A = W[st.first];
+    Item& B = W[st.second];
+    std::vector<int64_t> shared, fa, fb, dfa, dfb, dsh;
+    std::vector<int> pa, pb;
+    for (size_t a = 0; a < A.l.size(); ++a) {
+      if (std::find(B.l.begin(), B.l.end(), A.l[a]) == B.l.end()) {
+        fa.push_back(A.l[a]);
+        dfa.push_back(A.d[a]);
+        pa.push_back((int)a);
+      }
+    }
+    for (size_t a = 0; a < A.l.size(); ++a)
+      if (std::find(B.l.begin(), B.l.end(), A.l[a]) != B.l.end()) {
+        shared.push_back(A.l[a]);
+        dsh.push_back(A.d[a]);
+        pa.push_back((int)a);
+      }
+    for (int64_t x : shared) pb.push_back((int)(std::find(B.l.begin(), B.l.end(), x) - B.l.begin()));
+    for (size_t b = 0; b < B.l.size(); ++b)
+      if (std::find(shared.begin(), shared.end(), B.l[b]) == shared.end()) {
+        fb.push_back(B.l[b]);
+        dfb.push_back(B.d[b]);
+        pb.push_back((int)b);
+      }
+    const long long M = numel(dfa), K = numel(dsh), N = numel(dfb);
+    auto is_id = [](const std::vector<int>& p) {
+      for (size_t k = 0; k < p.size(); ++k)
+        if (p[k] != (int)k) return false;
+      return true;
+    };
+    void *ta = A.p, *tb = B.p, *tc = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!is_id(pa)) {
+      e = cudaMallocAsync(&ta, std::max<size_t>((size_t)M * K * es, 16), c->stream);
+      if (e == cudaSuccess) e = contract_permute(dtype, A.p, ta, A.d, pa, c->stream);
+    }
+    if (e == cudaSuccess && !is_id(pb)) {
+      e = cudaMallocAsync(&tb, std::max<size_t>((size_t)K * N * es, 16), c->stream);
+      if (e == cudaSuccess) e = contract_permute(dtype, B.p, tb, B.d, pb, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMallocAsync(&tc, std::max<size_t>((size_t)M * N * es, 16), c->stream);
+    if (e == cudaSuccess) {
+      if (precision == ITN_PREC_BF16)
+        e = contract_gemm_tc(reinterpret_cast<const float*>(ta), reinterpret_cast<const float*>(tb),
+                             reinterpret_cast<float*>(tc), M, N, K, c->stream);
+      else
+        e = contract_gemm(dtype, ta, tb, tc, M, N, K, c->stream);
+    }
+    if (ta != A.p && ta) cudaFreeAsync(ta, c->stream);
+    if (tb != B.p && tb) cudaFreeAsync(tb, c->stream);
+    if (e != cudaSuccess) {
+      if (tc) cudaFreeAsync(tc, c->stream);
+      release_all();
+      return cuda_fail(c, e, "contract_network step");
+    }
+    Item R{tc, fa, dfa};
+    R.l.insert(R.l.end(), fb.begin(), fb.end());
+    R.d.insert(R.d.end(), dfb.begin(), dfb.end());
+    cudaFreeAsync(A.p, c->stream);
+    cudaFreeAsync(B.p, c->stream);
+    const int i = st.first, j = st.second;
+    std::vector<Item> nw;
+    for (int k = 0; k < (int)W.size(); ++k)
+      if (k != i && k != j) nw.push_back(W[k]);
+    nw.push_back(R);
+    W.swap(nw);
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  Item& F = W[0];
+  const int64_t total = numel(F.d);
+  *out_rank = (int32_t)F.l.size();
+  for (size_t a = 0; a < F.l.size() && a < 48; ++a) {
+    if (out_labels) out_labels[a] = F.l[a];
+    if (out_dims) out_dims[a] = F.d[a];
+  }
+  int rc = ITN_OK;
+  if (out && out_capacity >= total) {
+    cudaError_t e = cudaMemcpyAsync(out, F.p, (size_t)total * es, cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "contract_network download");
+  } else {
+    rc = fail(c, ITN_ERR_ARG, "output capacity %lld < result size %lld", (long long)out_capacity, (long long)total);
+  }
+  release_all();
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "contract_network");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  if (device_ms) *device_ms = ms;
+  return rc;
 }
 
 }  // extern "C"

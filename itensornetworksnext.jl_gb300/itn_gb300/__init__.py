@@ -7,9 +7,10 @@ Layers:
 * ``graphs``     CSR network description + seeded synthetic generators
 * ``generators`` known-answer single-layer networks (Ising, spin ice, deltas)
 """
-from . import graphs, generators  # noqa: F401
+from . import graphs, generators, contract  # noqa: F401
+from .contract import contract_network, contraction_order  # noqa: F401
 from ._lib import ItnError, ItnArgumentError, load as load_library  # noqa: F401
 from .engine import BPEngine, RunResult  # noqa: F401
 
-__all__ = ["graphs", "generators", "BPEngine", "RunResult", "ItnError", "ItnArgumentError",
+__all__ = ["graphs", "generators", "contract", "contract_network", "contraction_order", "BPEngine", "RunResult", "ItnError", "ItnArgumentError",
            "load_library"]

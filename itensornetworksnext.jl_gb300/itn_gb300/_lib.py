@@ -32,7 +32,7 @@ EXPORTED = [
     "itn_tensors_upload_strided", "itn_tensors_download", "itn_messages_upload",
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
     "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest", "itn_bp_grad",
-    "itn_sweep_vjp", "itn_logz_static_scratch",
+    "itn_sweep_vjp", "itn_logz_static_scratch", "itn_contraction_order", "itn_contract_network",
 ]
 
 
@@ -101,6 +101,9 @@ def _declare(lib):
         "itn_tc_selftest": (_I32, [_VP, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP]),
         "itn_bp_grad": (_I32, [_VP, ctypes.POINTER(GradOpts), _VP, ctypes.POINTER(GradResult)]),
         "itn_sweep_vjp": (_I32, [_VP, _I32, _VP, _VP]),
+        "itn_contraction_order": (_I32, [_I32, _VP, _VP, _VP, _I32, _VP]),
+        "itn_contract_network": (_I32, [_VP, _I32, _I32, _VP, _VP, _VP, _VP, _I32, _VP, _I32, _VP, _I64,
+                                        ctypes.POINTER(_I32), _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logz_static_scratch": (_I32, [_I32, _VP, _I32, _I32, _I64, _I64, _I64, _VP, _VP, _VP, _VP,
                                            _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_char_p, _I32]),
     }
