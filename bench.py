@@ -353,9 +353,126 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "wall_s": wall,
     }
+    if args.extra and world == 1:
+        line["grad"] = bench_grad(device)
+        line["batched"] = bench_batched(device)
+        line["bp_16x16_D4"] = bench_16x16(device)
     print(json.dumps(line))
     eng.close()
     return 0
+
+
+def bench_grad(device):
+    """12x12 open PEPS, d=2, D=6, FP32 BP to convergence + implicit (adjoint) gradient of
+    the Bethe log-norm; error against central FD (step 1e-4, FP64 solves) on 32 random unit
+    directions, reported as |g.d - fd| over the vector of FD derivatives."""
+    from itn_gb300 import BPEngine
+    from itn_gb300 import graphs as G
+    g = G.square_lattice(12, 12, 6, periodic=False, phys=2)
+    rng = np.random.default_rng(12)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    e = BPEngine(g, device=device)
+    e.set_tensors(t.astype(np.float32))
+    times = []
+    for rep in range(4):  # first repetition warms up (graph capture, autotune)
+        t0 = time.perf_counter()
+        e.init_messages()
+        r = e.run(maxiter=500, tol=1e-12)
+        grad, info = e.grad(adjoint=True, tol=1e-6)
+        times.append(time.perf_counter() - t0)
+    e.close()
+    f = BPEngine(g, device=device)
+
+    def logz(x):
+        f.set_tensors(x)
+        f.init_messages()
+        f.run(maxiter=2000, tol=1e-14)
+        return f.bethe_free_energy()
+    gd, fds = [], []
+    h = 1e-4
+    for _ in range(32):
+        d = rng.standard_normal(t.size)
+        d /= np.linalg.norm(d)
+        fds.append((logz(t + h * d) - logz(t - h * d)) / (2 * h))
+        gd.append(float(grad.astype(np.float64) @ d))
+    f.close()
+    gd, fds = np.array(gd), np.array(fds)
+    return {"workload": "peps 12x12 open D=6 d=2, fp32 messages/gradient, fp64 log-scalars",
+            "bp_sweeps": r.iterations, "adjoint_iterations": info["adjoint_iterations"],
+            "grad_device_ms": info["device_ms"], "solve_plus_grad_wall_ms": 1e3 * min(times[1:]),
+            "fd_rel_err": float(np.linalg.norm(gd - fds) / np.linalg.norm(fds)), "fd_directions": 32,
+            "fd_step": h}
+
+
+def bench_batched(device, steps=3):
+    """256 independent random 3-regular networks, N ~ U{16..256} (even), per-edge bond
+    dims from {2,3,4,6,8}, complex64 N(0,1) entries; 30 parallel sweeps, every edge of every
+    network in one persistent launch per sweep, the solve captured as a CUDA graph."""
+    from itn_gb300 import BPEngine
+    from itn_gb300 import graphs as G
+    rng = np.random.default_rng(256)
+    nets = []
+    for _ in range(256):
+        n = int(rng.integers(8, 129)) * 2
+        edges = G.random_regular_edges(n, 3, rng)
+        bonds = rng.choice([2, 3, 4, 6, 8], size=len(edges))
+        nets.append(G.from_edges(n, edges, bonds, phys=2))
+    g = G.batched(nets)
+    t = G.random_tensors(g, rng, np.complex64)
+    e = BPEngine(g, device=device)
+    e.set_tensors(t)
+    ms = []
+    for rep in range(steps + 1):
+        e.init_messages()
+        r = e.run(maxiter=30)
+        if rep:
+            ms.append(r.device_ms)
+    logz = e.bethe_free_energy()
+    e.close()
+    upd = 30 * g.nslots
+    flops = 30 * sum(4 * len(g.legs(u)) * 2.0 * 2 * np.prod(g.legs(u)) * np.sum(g.legs(u)) for u in range(g.nv))
+    best = min(ms)
+    return {"workload": "256 random 3-regular norm networks, N in [16,256], D_e in {2,3,4,6,8}, c64, 30 sweeps",
+            "vertices": g.nv, "updates_per_solve": upd, "value": upd / (best * 1e-3),
+            "unit": "message updates/s", "ms_per_solve": best,
+            "achieved_tflops_complex_alg": flops / (best * 1e-3) / 1e12,
+            "logz_finite": bool(np.all(np.isfinite(np.real(np.asarray(logz)))))}
+
+
+def bench_16x16(device):
+    """16x16 open PEPS, d=2, D=4, N(0,1)/sqrt(d D^4): 50 parallel sweeps or tol 1e-10, FP32
+    and FP64; plus the BP error of a 6x6 D=3 network against its exact contraction."""
+    from itn_gb300 import BPEngine
+    from itn_gb300 import graphs as G
+    from itn_gb300.contract import contract_network, norm_network_tensors
+    g = G.square_lattice(16, 16, 4, periodic=False, phys=2)
+    rng = np.random.default_rng(16)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    out = {"workload": "peps 16x16 open D=4 d=2, maxiter 50 / tol 1e-10"}
+    for name, dt in (("fp32", np.float32), ("fp64", np.float64)):
+        e = BPEngine(g, device=device)
+        e.set_tensors(t.astype(dt))
+        best = None
+        for rep in range(3):
+            e.init_messages()
+            r = e.run(maxiter=50, tol=1e-10)
+            best = r if best is None or r.device_ms < best.device_ms else best
+        out[name] = {"iterations": best.iterations, "ms": best.device_ms,
+                     "updates_per_s": best.iterations * g.nslots / (best.device_ms * 1e-3)}
+        e.close()
+    g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
+    t6 = G.random_tensors(g6, np.random.default_rng(63), np.float64, G.peps_scale(g6))
+    e = BPEngine(g6, device=device)
+    e.set_tensors(t6)
+    e.init_messages()
+    e.run(maxiter=200, tol=1e-12)
+    lz_bp = e.bethe_free_energy()
+    e.close()
+    ts, ls = norm_network_tensors(g6, t6)
+    z, _, ms = contract_network(ts, ls, return_time=True)
+    out["exact_6x6_D3"] = {"logz_exact": float(np.log(z[()])), "logz_bp": lz_bp,
+                           "bp_abs_err": abs(lz_bp - float(np.log(z[()]))), "contract_ms": ms}
+    return out
 
 
 def G_identity(g):
@@ -369,9 +486,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "native"),
+    ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-extra", dest="extra", action="store_false",
+                    help="skip the secondary configurations (gradient, batched, 16x16, exact 6x6)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -73,7 +73,7 @@ __host__ __device__ constexpr TcSmem tc_smem() {
   TcSmem L{};
   uint32_t o = 0;
   L.aimg = o; o += (SPLIT ? 8 : 4) * kBlk;
-  L.reg = o;  o += (SPLIT ? 8 : 4) * kBlk;
+  L.reg = o;  o += 4 * kBlk;  // split: P (hi+lo), then XT (hi+lo), then YT (hi+lo) in turn
   L.msg = o;  o += 4 * 64 * 4;
   L.outs = o; o += 2 * 64 * 4;
   L.part = o; o += 2 * 4 * 64 * 4;
@@ -82,10 +82,12 @@ __host__ __device__ constexpr TcSmem tc_smem() {
   L.total = o;
   return L;
 }
-// offsets inside `reg`
-constexpr uint32_t kP01 = 0, kP23 = kBlk;             // + 2*kBlk for the lo parts
+// offsets inside `reg`: P01 | P23 (+ 2 blocks of lo parts when split).  Plain sweeps keep
+// XT and YT side by side (G2 and G4 issued together); split sweeps store XT (hi | lo), run
+// G2, then reuse the region for YT (hi | lo) and run G4.
+constexpr uint32_t kP01 = 0, kP23 = kBlk;
 template <bool SPLIT> __host__ __device__ constexpr uint32_t kXT() { return 0; }
-template <bool SPLIT> __host__ __device__ constexpr uint32_t kYT() { return SPLIT ? 4 * kBlk : 2 * kBlk; }
+template <bool SPLIT> __host__ __device__ constexpr uint32_t kYT() { return SPLIT ? 0 : 2 * kBlk; }
 
 struct TcArgs {
   const int* off;
@@ -188,17 +190,34 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
   // M = 64 accumulator row held by this thread (-1: lane unused)
   const int zrow = c_row_of_lane[warp * 32 + lane];
 
+  // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
+  // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
+  // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next vertex are
+  // prefetched into registers while the current one is processed.
+  const int l0 = tid >> 6, e0 = tid & 63;
+  float pre0 = 0.f, pre1 = 0.f;
+  if (blockIdx.x < a.nv) {
+    const int u = blockIdx.x;
+    pre0 = a.msg_in[64 * a.rev[4 * u + l0] + e0];
+    pre1 = a.msg_in[64 * a.rev[4 * u + l0 + 2] + e0];
+  }
+  // the operand image of the first vertex; later images are requested as soon as the
+  // previous vertex's last MMAs (their only readers) have completed
+  if (tid == 0 && blockIdx.x < a.nv) {
+    ptx::mbar_arrive_expect_tx(bar_load, img_bytes);
+    ptx::bulk_g2s(sm + L.aimg, a.image + (size_t)blockIdx.x * img_bytes, img_bytes, bar_load);
+  }
   for (int u = blockIdx.x; u < a.nv; u += gridDim.x) {
-    const int s0 = a.off[u];
-    // 1. bulk copy of the vertex's operand image; incoming messages m_l = m_{nbr_l -> u}
-    if (tid == 0) {
-      ptx::mbar_arrive_expect_tx(bar_load, img_bytes);
-      ptx::bulk_g2s(sm + L.aimg, a.image + (size_t)u * img_bytes, img_bytes, bar_load);
-    }
+    const int s0 = 4 * u;
+    // 1. incoming messages m_l = m_{nbr_l -> u} (prefetched); the image copy is in flight
+    msg[l0 * 64 + e0] = pre0;
+    msg[(l0 + 2) * 64 + e0] = pre1;
     {
-      const int l0 = tid >> 6, e = tid & 63;  // threads 0..63: legs 0,2; 64..127: legs 1,3
-      msg[l0 * 64 + e] = a.msg_in[a.moff[a.rev[s0 + l0]] + e];
-      msg[(l0 + 2) * 64 + e] = a.msg_in[a.moff[a.rev[s0 + l0 + 2]] + e];
+      const int un = u + gridDim.x;
+      if (un < a.nv) {
+        pre0 = a.msg_in[64 * a.rev[4 * un + l0] + e0];
+        pre1 = a.msg_in[64 * a.rev[4 * un + l0 + 2] + e0];
+      }
     }
     __syncthreads();
     // 2. Kronecker operands P01 = m0 (x) m1, P23 = m2 (x) m3 (core layout, BF16 hi [+lo])
@@ -246,24 +265,45 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
     ph_mma ^= 1;
     ptx::tc_fence_after();
     // 4. epilogue 1: X row (s,q) -> XT[s] row q;  Y row (s,p) -> YT[s] row p
+    // 5. G2: Z23 = A_qp XT^T (M=64) -> cols 0..63;  G4: Z01 = A_pq YT^T -> cols 64..127
     {
       const int row = warp * 32 + lane, s = row >> 6, r = row & 63;
+      const uint32_t XT = R + kXT<SPLIT>(), YT = R + kYT<SPLIT>();
       float v[64];
       tmem_ld64(tq + 0, v);
       store_row_bf16<SPLIT>(reg + kXT<SPLIT>() + s * kBlk, reg + kXT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
-      tmem_ld64(tq + 64, v);
-      store_row_bf16<SPLIT>(reg + kYT<SPLIT>() + s * kBlk, reg + kYT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
-    }
-    ptx::tc_fence_before();
-    ptx::fence_proxy_async_smem();
-    __syncthreads();
-    // 5. G2: Z23 = A_qp XT^T (M=64) -> cols 0..63;  G4: Z01 = A_pq YT^T -> cols 64..127
-    if (tid == 0) {
-      ptx::tc_fence_after();
-      const uint32_t XT = R + kXT<SPLIT>(), YT = R + kYT<SPLIT>();
-      mma_chain<SPLIT>(tmem + 0, Aqp, Aqp + Alo, XT, XT + 2 * kBlk, idesc64, 8, true);
-      mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, YT, YT + 2 * kBlk, idesc64, 8, true);
-      ptx::mma_commit(bar_mma);
+      if constexpr (!SPLIT) {
+        tmem_ld64(tq + 64, v);
+        store_row_bf16<SPLIT>(reg + kYT<SPLIT>() + s * kBlk, reg + kYT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
+      }
+      ptx::tc_fence_before();
+      ptx::fence_proxy_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        ptx::tc_fence_after();
+        mma_chain<SPLIT>(tmem + 0, Aqp, Aqp + Alo, XT, XT + 2 * kBlk, idesc64, 8, true);
+        if constexpr (!SPLIT) mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, YT, YT + 2 * kBlk, idesc64, 8, true);
+        ptx::mma_commit(bar_mma);
+      }
+      if constexpr (SPLIT) {
+        // Y leaves TMEM while G2 runs; YT may only overwrite XT once G2 is done
+        tmem_ld64(tq + 64, v);
+        if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
+          if (tid == 0) atomicExch(a.err, 1);
+          ok = false;
+          break;
+        }
+        ph_mma ^= 1;
+        store_row_bf16<SPLIT>(reg + kYT<SPLIT>() + s * kBlk, reg + kYT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
+        ptx::tc_fence_before();
+        ptx::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+          ptx::tc_fence_after();
+          mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, YT, YT + 2 * kBlk, idesc64, 8, true);
+          ptx::mma_commit(bar_mma);
+        }
+      }
     }
     if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
       if (tid == 0) atomicExch(a.err, 1);
@@ -272,6 +312,10 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
     }
     ph_mma ^= 1;
     ptx::tc_fence_after();
+    if (tid == 0 && u + (int)gridDim.x < a.nv) {
+      ptx::mbar_arrive_expect_tx(bar_load, img_bytes);
+      ptx::bulk_g2s(sm + L.aimg, a.image + (size_t)(u + gridDim.x) * img_bytes, img_bytes, bar_load);
+    }
     // 6. epilogue 2 from registers.  Row zrow = (bh, bl) of Z23 = (b2, b3) and of
     //    Z01 = (b0, b1); columns (kh, kl).  For the pair (hi leg H, lo leg L):
     //      outH[bh][kh] = sum_{bl,kl} Z[(bh,bl)][(kh,kl)] mL[bl][kl]   (sum over 8 rows)
@@ -339,8 +383,8 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
       for (int k = 16; k >= 1; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
       const bool scale = a.normalize && sum != 0.f;
       const int slot = s0 + warp;
-      float* dst = a.msg_out + a.moff[slot];
-      const float* old = a.msg_in + a.moff[slot];
+      float* dst = a.msg_out + 64 * slot;
+      const float* old = a.msg_in + 64 * slot;
       double n1 = 0, n2 = 0, dd = 0;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
@@ -603,7 +647,7 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
     return cudaSuccess;
   }
   for (int64_t u = 0; u < nv; ++u) {
-    if (off[u + 1] - off[u] != 4 || phys[u] != 2) {
+    if (off[u] != 4 * u || off[u + 1] - off[u] != 4 || phys[u] != 2) {
       *why = "tensor-core sweep needs every vertex to have 4 legs and physical dimension 2";
       return cudaSuccess;
     }

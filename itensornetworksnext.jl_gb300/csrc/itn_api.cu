@@ -11,6 +11,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -179,6 +180,8 @@ struct itn_ctx {
 
   // cached solve graphs
   std::map<std::string, cudaGraphExec_t> graphs;
+  // CTA size chosen by the autotuner for the parallel sweep, per dtype (0: not tuned)
+  std::vector<int> tuned_block = std::vector<int>(4, 0);
 
   // tensor-core engine (bp_tc.cu), created on first use
   TcEngine* tc = nullptr;
@@ -252,6 +255,7 @@ int sync_programs(itn_ctx* c) {
 }
 
 int block_for(itn_ctx* c) {
+  if (c->dtype >= 0 && c->dtype < 4 && c->tuned_block[c->dtype] > 0) return c->tuned_block[c->dtype];
   if (c->max_tensor <= 256) return 64;
   if (c->max_tensor <= 2048) return 128;
   return 256;
@@ -534,6 +538,21 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       c->items_scal.push_back(0);
     }
   }
+  {
+    // largest vertices first: persistent CTAs take items round-robin, so a descending
+    // cost order keeps uneven networks balanced
+    std::vector<std::pair<int, int>> it;
+    for (size_t k = 0; k + 1 < c->items_par.size(); k += 2) it.push_back({c->items_par[k], c->items_par[k + 1]});
+    std::stable_sort(it.begin(), it.end(), [&](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+      return (c->toff[x.first + 1] - c->toff[x.first]) > (c->toff[y.first + 1] - c->toff[y.first]);
+    });
+    c->items_par.clear();
+    for (auto& p : it) {
+      c->items_par.push_back(p.first);
+      c->items_par.push_back(p.second);
+    }
+  }
+  c->tuned_block.assign(4, 0);
   if (c->prog_host.empty()) c->prog_host.push_back(0);
   c->prog_dirty = true;
   std::vector<int> off32(c->off.begin(), c->off.end()), rev32(c->rev.begin(), c->rev.end());
@@ -779,6 +798,46 @@ struct ParPlan {
   LaunchCfg cfg[2];
 };
 
+// Autotuner for the parallel sweep: time one sweep per candidate CTA size (64, 128, 256
+// threads; each with its own residency) from the current messages into the other
+// ping-pong buffer and keep the fastest for this network and dtype.
+int autotune_sweep(itn_ctx* c) {
+  if (c->tuned_block[c->dtype] > 0 || c->items_par.empty()) return ITN_OK;
+  if (getenv("ITN_NO_AUTOTUNE")) {
+    c->tuned_block[c->dtype] = -1;
+    return ITN_OK;
+  }
+  const int cands[3] = {64, 128, 256};
+  float best = 1e30f;
+  int best_b = 0;
+  for (int b : cands) {
+    c->tuned_block[c->dtype] = b;
+    GenericArgs a;
+    LaunchCfg cfg;
+    if (plan_generic(c, a, cfg, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, c->d_msg[c->cur].p,
+                     c->d_msg[c->cur ^ 1].p))
+      continue;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {  // first launch warms the caches
+      CK(cudaEventRecord(c->ev0, c->stream));
+      CK(launch_generic(c->dtype, a, cfg, c->stream));
+      CK(cudaEventRecord(c->ev1, c->stream));
+      CK(cudaEventSynchronize(c->ev1));
+      CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    }
+    if (ms < best) {
+      best = ms;
+      best_b = b;
+    }
+  }
+  c->tuned_block[c->dtype] = best_b > 0 ? best_b : -1;
+  if (getenv("ITN_DEBUG")) fprintf(stderr, "[itn] autotune: sweep CTA size %d (%.3f ms)\n", best_b, best);
+  // cached graphs were captured with the previous launch shape
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+  return ITN_OK;
+}
+
 int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   const bool use_tol = o->tol >= 0;
   for (int in = 0; in < 2; ++in) {
@@ -913,6 +972,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   ParPlan pplan;
   std::vector<SeqLaunch> slaunch;
   if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE) {
+    if (int r = autotune_sweep(c)) return r;
     if (int r = make_par_plan(c, o, pplan)) return r;
   } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {
     if (int r = make_seq_launches(c, plan, o, slaunch)) return r;
