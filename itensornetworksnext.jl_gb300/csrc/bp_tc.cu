@@ -40,7 +40,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kBlk = 8192;                 // bytes of one 64 x 64 BF16 operand block
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
-constexpr int kTmemCols = 128;
+constexpr int kTmemCols = 64;
 
 // row -> TMEM lane for an M = 64 accumulator (filled from the self-test probe)
 __constant__ signed char c_row_of_lane[128];
@@ -61,39 +61,35 @@ __device__ __forceinline__ void split_bf16(float x, float& hi, float& lo) {
 
 struct TcSmem {
   // offsets in bytes from the dynamic shared memory base
-  uint32_t aimg, reg, msg, outs, part, bars, taddr, total;
+  uint32_t img, reg, msg, outs, part, bars, taddr, total;
 };
 
-// aimg : [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ lo]              32 KB [64 KB]
-// reg  : P01 | P23 (hi [+lo]) while G1/G3 run, then XT | YT (hi [+lo])  32 KB [64 KB]
-// msg  : incoming messages m0..m3 (FP32)                    1 KB
-// outs : outgoing messages 0 and 2 (complete), 1 and 3 (per-warp partials)
+// Work item = half of a vertex.  Half 0 builds P01 = m0 (x) m1, computes
+//   X[(s,q), b01] = sum_p A[s,p,q] P01[b01,p]               (G1: A_qp, M=128 N=64 K=64)
+//   Z23[b23, k23] = sum_{s,b01} A[s,b01,b23] X[(s,k23),b01]  (G2: A_qp, M=64 N=64 K=128)
+// and emits the messages on legs 2 and 3; half 1 does the same with P23, A_pq (Y, Z01)
+// for legs 0 and 1.  A half needs one operand layout only (16 KB of BF16, 32 KB split).
+// img : A_qp (half 0) or A_pq (half 1): hi [+ lo]          16 KB [32 KB]
+// reg : P (hi [+ lo]) while G1 runs, then XT (hi [+ lo])   16 KB [32 KB]
+// msg : incoming messages m0..m3 (FP32)                     1 KB
 template <bool SPLIT>
 __host__ __device__ constexpr TcSmem tc_smem() {
   TcSmem L{};
   uint32_t o = 0;
-  L.aimg = o; o += (SPLIT ? 8 : 4) * kBlk;
-  L.reg = o;  o += 4 * kBlk;  // split: P (hi+lo), then XT (hi+lo), then YT (hi+lo) in turn
+  L.img = o;  o += (SPLIT ? 4 : 2) * kBlk;
+  L.reg = o;  o += (SPLIT ? 4 : 2) * kBlk;
   L.msg = o;  o += 4 * 64 * 4;
-  L.outs = o; o += 2 * 64 * 4;
-  L.part = o; o += 2 * 4 * 64 * 4;
+  L.outs = o; o += 64 * 4;
+  L.part = o; o += 4 * 64 * 4;
   L.bars = o; o += 16;
   L.taddr = o; o += 16;
   L.total = o;
   return L;
 }
-// offsets inside `reg`: P01 | P23 (+ 2 blocks of lo parts when split).  Plain sweeps keep
-// XT and YT side by side (G2 and G4 issued together); split sweeps store XT (hi | lo), run
-// G2, then reuse the region for YT (hi | lo) and run G4.
-constexpr uint32_t kP01 = 0, kP23 = kBlk;
-template <bool SPLIT> __host__ __device__ constexpr uint32_t kXT() { return 0; }
-template <bool SPLIT> __host__ __device__ constexpr uint32_t kYT() { return SPLIT ? 0 : 2 * kBlk; }
 
 struct TcArgs {
-  const int* off;
   const int* rev;
-  const long long* moff;
-  const unsigned char* image;  // per vertex: (SPLIT ? 64 : 32) KB operand image
+  const unsigned char* image;  // per vertex: [A_pq hi | A_qp hi | A_pq lo | A_qp lo], 16 KB each
   const float* msg_in;
   float* msg_out;
   int nv;
@@ -110,6 +106,34 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
   ptx::tmem_ld16(taddr + 32, *reinterpret_cast<float(*)[16]>(p + 32));
   ptx::tmem_ld16(taddr + 48, *reinterpret_cast<float(*)[16]>(p + 48));
   ptx::tmem_wait_ld();
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  float* p = v;
+  ptx::tmem_ld16(taddr + 0, *reinterpret_cast<float(*)[16]>(p + 0));
+  ptx::tmem_ld16(taddr + 16, *reinterpret_cast<float(*)[16]>(p + 16));
+  ptx::tmem_wait_ld();
+}
+
+// Store 32 entries (columns c0 .. c0+31) of an accumulator row as BF16 (hi [+ lo]) into
+// row r of a 64 x 64 block.
+template <bool SPLIT>
+__device__ __forceinline__ void store_half_bf16(unsigned char* blk, unsigned char* blk_lo, int r, int c0,
+                                                const float (&v)[32]) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float hi[8], lo[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) split_bf16(v[c * 8 + e], hi[e], lo[e]);
+    const uint32_t off = blk_off(r, c0 + c * 8);
+    *reinterpret_cast<uint4*>(blk + off) =
+        make_uint4(pack_bf16(hi[0], hi[1]), pack_bf16(hi[2], hi[3]), pack_bf16(hi[4], hi[5]),
+                   pack_bf16(hi[6], hi[7]));
+    if constexpr (SPLIT)
+      *reinterpret_cast<uint4*>(blk_lo + off) =
+          make_uint4(pack_bf16(lo[0], lo[1]), pack_bf16(lo[2], lo[3]), pack_bf16(lo[4], lo[5]),
+                     pack_bf16(lo[6], lo[7]));
+  }
 }
 
 // Store one 64-entry accumulator row as BF16 (hi [+ lo]) into row r of a 64 x 64 block.
@@ -149,19 +173,32 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo,
   }
 }
 
+template <bool SPLIT>
+__device__ __forceinline__ void issue_image(unsigned char* sm_img, const unsigned char* image, int item,
+                                            uint64_t* bar) {
+  const int u = item >> 1, h = item & 1;
+  // half 0 uses A_qp (second 16 KB of the hi image), half 1 A_pq (first)
+  const unsigned char* base = image + (size_t)u * 4 * (2 * kBlk);
+  const uint32_t hi_off = (h ? 0u : 2u) * kBlk;
+  ptx::mbar_arrive_expect_tx(bar, (SPLIT ? 4 : 2) * kBlk);
+  ptx::bulk_g2s(sm_img, base + hi_off, 2 * kBlk, bar);
+  if constexpr (SPLIT) ptx::bulk_g2s(sm_img + 2 * kBlk, base + 4 * kBlk + hi_off, 2 * kBlk, bar);
+}
+
 // ---- the sweep kernel --------------------------------------------------------------------
 template <bool SPLIT>
-__global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
+__global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   constexpr TcSmem L = tc_smem<SPLIT>();
   uint64_t* bar_load = reinterpret_cast<uint64_t*>(sm + L.bars);
   uint64_t* bar_mma = bar_load + 1;
   uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm + L.taddr);
   float* msg = reinterpret_cast<float*>(sm + L.msg);    // [4][64] incoming
-  float* outs = reinterpret_cast<float*>(sm + L.outs);  // [2][64]: out0, out2
-  float* part = reinterpret_cast<float*>(sm + L.part);  // [2][4 warps][64]: out1, out3 partials
+  float* outs = reinterpret_cast<float*>(sm + L.outs);  // [64] message on the pair's first leg
+  float* part = reinterpret_cast<float*>(sm + L.part);  // [4 warps][64] partials, second leg
   unsigned char* reg = sm + L.reg;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n_items = 2 * a.nv;
 
   if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
 
@@ -180,11 +217,10 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
   const uint32_t tmem = *taddr_s;
   const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
   const uint32_t sbase = ptx::smem_u32(sm);
-  const uint32_t Apq = sbase + L.aimg, Aqp = Apq + 2 * kBlk, Alo = 4 * kBlk;
+  const uint32_t Aimg = sbase + L.img, Alo = 2 * kBlk;
   const uint32_t R = sbase + L.reg;
   uint32_t ph_load = 0, ph_mma = 0;
   bool ok = true;  // false after a bounded wait gave up (block-uniform)
-  constexpr uint32_t img_bytes = (SPLIT ? 8 : 4) * kBlk;
   constexpr uint32_t idesc128 = ptx::idesc_bf16_f32(128, 64);
   constexpr uint32_t idesc64 = ptx::idesc_bf16_f32(64, 64);
   // M = 64 accumulator row held by this thread (-1: lane unused)
@@ -192,59 +228,59 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
 
   // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
   // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
-  // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next vertex are
+  // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next item are
   // prefetched into registers while the current one is processed.
   const int l0 = tid >> 6, e0 = tid & 63;
   float pre0 = 0.f, pre1 = 0.f;
-  if (blockIdx.x < a.nv) {
-    const int u = blockIdx.x;
+  if ((int)blockIdx.x < n_items) {
+    const int u = blockIdx.x >> 1;
     pre0 = a.msg_in[64 * a.rev[4 * u + l0] + e0];
     pre1 = a.msg_in[64 * a.rev[4 * u + l0 + 2] + e0];
+    if (tid == 0) issue_image<SPLIT>(sm + L.img, a.image, blockIdx.x, bar_load);
   }
-  // the operand image of the first vertex; later images are requested as soon as the
-  // previous vertex's last MMAs (their only readers) have completed
-  if (tid == 0 && blockIdx.x < a.nv) {
-    ptx::mbar_arrive_expect_tx(bar_load, img_bytes);
-    ptx::bulk_g2s(sm + L.aimg, a.image + (size_t)blockIdx.x * img_bytes, img_bytes, bar_load);
-  }
-  for (int u = blockIdx.x; u < a.nv; u += gridDim.x) {
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int u = item >> 1, h = item & 1;
     const int s0 = 4 * u;
-    // 1. incoming messages m_l = m_{nbr_l -> u} (prefetched); the image copy is in flight
+    // pair (A, B) builds P; pair (H, Lg) receives the outgoing messages
+    const int pa = h ? 2 : 0, pb = pa + 1, H = h ? 0 : 2, Lg = H + 1;
     msg[l0 * 64 + e0] = pre0;
     msg[(l0 + 2) * 64 + e0] = pre1;
     {
-      const int un = u + gridDim.x;
-      if (un < a.nv) {
+      const int nx = item + gridDim.x;
+      if (nx < n_items) {
+        const int un = nx >> 1;
         pre0 = a.msg_in[64 * a.rev[4 * un + l0] + e0];
         pre1 = a.msg_in[64 * a.rev[4 * un + l0 + 2] + e0];
       }
     }
     __syncthreads();
-    // 2. Kronecker operands P01 = m0 (x) m1, P23 = m2 (x) m3 (core layout, BF16 hi [+lo])
+    // 1. P = m_pa (x) m_pb in core layout: thread t writes row bi = t & 7 of the cores
+    //    (bo = (t >> 3) & 7, ko = 4 (t >> 6) .. +3); 8 consecutive threads fill one
+    //    128-byte core, so the 16-byte stores are free of bank conflicts
     {
-      const int pair = tid >> 6;
-      const int t = tid & 63;
-      const int bo = t >> 3, ko = t & 7;
-      const float* mo = msg + (pair * 2) * 64;
-      const float* mi = msg + (pair * 2 + 1) * 64;
-      unsigned char* P = reg + (pair ? kP23 : kP01);
-      const float w = mo[bo * 8 + ko];
+      const int bi = tid & 7, bo = (tid >> 3) & 7, kq = (tid >> 6) * 4;
+      const float* ma = msg + pa * 64;
+      float mb[8];
 #pragma unroll
-      for (int bi = 0; bi < 8; ++bi) {
-        float h[8], lo[8];
+      for (int k = 0; k < 8; ++k) mb[k] = msg[pb * 64 + bi * 8 + k];
 #pragma unroll
-        for (int ki = 0; ki < 8; ++ki) split_bf16(w * mi[bi * 8 + ki], h[ki], lo[ki]);
+      for (int j = 0; j < 4; ++j) {
+        const int ko = kq + j;
+        const float w = ma[bo * 8 + ko];
+        float hv[8], lv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) split_bf16(w * mb[k], hv[k], lv[k]);
         const uint32_t off = blk_off(bo * 8 + bi, ko * 8);
-        *reinterpret_cast<uint4*>(P + off) = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]),
-                                                        pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+        *reinterpret_cast<uint4*>(reg + off) = make_uint4(pack_bf16(hv[0], hv[1]), pack_bf16(hv[2], hv[3]),
+                                                          pack_bf16(hv[4], hv[5]), pack_bf16(hv[6], hv[7]));
         if constexpr (SPLIT)
-          *reinterpret_cast<uint4*>(P + 2 * kBlk + off) =
-              make_uint4(pack_bf16(lo[0], lo[1]), pack_bf16(lo[2], lo[3]), pack_bf16(lo[4], lo[5]),
-                         pack_bf16(lo[6], lo[7]));
+          *reinterpret_cast<uint4*>(reg + kBlk + off) =
+              make_uint4(pack_bf16(lv[0], lv[1]), pack_bf16(lv[2], lv[3]), pack_bf16(lv[4], lv[5]),
+                         pack_bf16(lv[6], lv[7]));
       }
     }
     ptx::fence_proxy_async_smem();
-    // 3. G1: X = A_qp P01^T -> TMEM cols 0..63;  G3: Y = A_pq P23^T -> cols 64..127
+    // 2. first GEMM: rows (s, r) of the image times P^T -> TMEM cols 0..63
     if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls))) {
       if (tid == 0) atomicExch(a.err, 1);
       ok = false;
@@ -253,8 +289,7 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
     ph_load ^= 1;
     if (tid == 0) {
       ptx::tc_fence_after();
-      mma_chain<SPLIT>(tmem + 0, Aqp, Aqp + Alo, R + kP01, R + kP01 + 2 * kBlk, idesc128, 4, false);
-      mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, R + kP23, R + kP23 + 2 * kBlk, idesc128, 4, false);
+      mma_chain<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc128, 4, false);
       ptx::mma_commit(bar_mma);
     }
     if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
@@ -264,46 +299,24 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
     }
     ph_mma ^= 1;
     ptx::tc_fence_after();
-    // 4. epilogue 1: X row (s,q) -> XT[s] row q;  Y row (s,p) -> YT[s] row p
-    // 5. G2: Z23 = A_qp XT^T (M=64) -> cols 0..63;  G4: Z01 = A_pq YT^T -> cols 64..127
+    // 3. epilogue 1: accumulator row (s, r) -> XT[s] row r (BF16 hi [+ lo]), over P
     {
       const int row = warp * 32 + lane, s = row >> 6, r = row & 63;
-      const uint32_t XT = R + kXT<SPLIT>(), YT = R + kYT<SPLIT>();
-      float v[64];
-      tmem_ld64(tq + 0, v);
-      store_row_bf16<SPLIT>(reg + kXT<SPLIT>() + s * kBlk, reg + kXT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
-      if constexpr (!SPLIT) {
-        tmem_ld64(tq + 64, v);
-        store_row_bf16<SPLIT>(reg + kYT<SPLIT>() + s * kBlk, reg + kYT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float v[32];
+        tmem_ld32(tq + 32 * half, v);
+        store_half_bf16<SPLIT>(reg + s * kBlk, reg + 2 * kBlk + s * kBlk, r, 32 * half, v);
       }
-      ptx::tc_fence_before();
-      ptx::fence_proxy_async_smem();
-      __syncthreads();
-      if (tid == 0) {
-        ptx::tc_fence_after();
-        mma_chain<SPLIT>(tmem + 0, Aqp, Aqp + Alo, XT, XT + 2 * kBlk, idesc64, 8, true);
-        if constexpr (!SPLIT) mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, YT, YT + 2 * kBlk, idesc64, 8, true);
-        ptx::mma_commit(bar_mma);
-      }
-      if constexpr (SPLIT) {
-        // Y leaves TMEM while G2 runs; YT may only overwrite XT once G2 is done
-        tmem_ld64(tq + 64, v);
-        if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
-          if (tid == 0) atomicExch(a.err, 1);
-          ok = false;
-          break;
-        }
-        ph_mma ^= 1;
-        store_row_bf16<SPLIT>(reg + kYT<SPLIT>() + s * kBlk, reg + kYT<SPLIT>() + 2 * kBlk + s * kBlk, r, v);
-        ptx::tc_fence_before();
-        ptx::fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-          ptx::tc_fence_after();
-          mma_chain<SPLIT>(tmem + 64, Apq, Apq + Alo, YT, YT + 2 * kBlk, idesc64, 8, true);
-          ptx::mma_commit(bar_mma);
-        }
-      }
+    }
+    ptx::tc_fence_before();
+    ptx::fence_proxy_async_smem();
+    __syncthreads();
+    // 4. second GEMM: Z = image (rows of the other pair, K = (s, this pair)) x XT^T, M = 64
+    if (tid == 0) {
+      ptx::tc_fence_after();
+      mma_chain<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + 2 * kBlk, idesc64, 8, true);
+      ptx::mma_commit(bar_mma);
     }
     if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
       if (tid == 0) atomicExch(a.err, 1);
@@ -312,36 +325,35 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
     }
     ph_mma ^= 1;
     ptx::tc_fence_after();
-    if (tid == 0 && u + (int)gridDim.x < a.nv) {
-      ptx::mbar_arrive_expect_tx(bar_load, img_bytes);
-      ptx::bulk_g2s(sm + L.aimg, a.image + (size_t)(u + gridDim.x) * img_bytes, img_bytes, bar_load);
-    }
-    // 6. epilogue 2 from registers.  Row zrow = (bh, bl) of Z23 = (b2, b3) and of
-    //    Z01 = (b0, b1); columns (kh, kl).  For the pair (hi leg H, lo leg L):
-    //      outH[bh][kh] = sum_{bl,kl} Z[(bh,bl)][(kh,kl)] mL[bl][kl]   (sum over 8 rows)
-    //      outL[bl][kl] = sum_{bh,kh} Z[(bh,bl)][(kh,kl)] mH[bh][kh]   (sum over 8 rows)
-#pragma unroll
-    for (int pr = 0; pr < 2; ++pr) {  // pr 0: Z23 (legs 2,3), 1: Z01 (legs 0,1)
-      const int H = pr ? 0 : 2, Lg = H + 1;
-      float z[64];
-      tmem_ld64(tq + pr * 64, z);
+    // the image's only readers are done: fetch the next item's image now
+    if (tid == 0 && item + (int)gridDim.x < n_items) issue_image<SPLIT>(sm + L.img, a.image, item + gridDim.x, bar_load);
+    // 5. epilogue 2 from registers.  Row zrow = (bh, bl) of Z (bra indices of legs H, Lg),
+    //    columns (kh, kl):
+    //      outH[bh][kh] = sum_{bl,kl} Z[(bh,bl)][(kh,kl)] m_Lg[bl][kl]   (sum over 8 rows)
+    //      outL[bl][kl] = sum_{bh,kh} Z[(bh,bl)][(kh,kl)] m_H[bh][kh]    (sum over 8 rows)
+    {
       const int bh = zrow >> 3, bl = zrow & 7;
-      float th[8], tl[8];
+      float th[8], tl[8], ml[8], mh[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) th[k] = tl[k] = 0.f;
-      if (zrow >= 0) {
-        const float* mL = msg + Lg * 64 + bl * 8;
-        const float* mH = msg + H * 64 + bh * 8;
-        float ml[8], mh[8];
+      for (int k = 0; k < 8; ++k) {
+        th[k] = tl[k] = 0.f;
+        ml[k] = msg[Lg * 64 + (bl & 7) * 8 + k];
+        mh[k] = msg[H * 64 + (bh & 7) * 8 + k];
+      }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) { ml[k] = mL[k]; mh[k] = mH[k]; }
+      for (int half = 0; half < 2; ++half) {  // columns kh = 4 half .. 4 half + 3
+        float z[32];
+        tmem_ld32(tq + 32 * half, z);
+        if (zrow >= 0) {
 #pragma unroll
-        for (int kh = 0; kh < 8; ++kh)
+          for (int j = 0; j < 4; ++j)
 #pragma unroll
-          for (int kl = 0; kl < 8; ++kl) {
-            th[kh] = fmaf(z[kh * 8 + kl], ml[kl], th[kh]);
-            tl[kl] = fmaf(z[kh * 8 + kl], mh[kh], tl[kl]);
-          }
+            for (int kl = 0; kl < 8; ++kl) {
+              const int kh = 4 * half + j;
+              th[kh] = fmaf(z[j * 8 + kl], ml[kl], th[kh]);
+              tl[kl] = fmaf(z[j * 8 + kl], mh[kh], tl[kl]);
+            }
+        }
       }
       // rows 16w + lane (lane < 16): bl = lane & 7, bh = 2w + (lane >> 3)
 #pragma unroll
@@ -354,44 +366,38 @@ __global__ void __launch_bounds__(kThreads) bp_tc_kernel(TcArgs a) {
       if (zrow >= 0) {
         if ((lane & 7) == 0) {
 #pragma unroll
-          for (int k = 0; k < 8; ++k) outs[pr * 64 + bh * 8 + k] = th[k];
+          for (int k = 0; k < 8; ++k) outs[bh * 8 + k] = th[k];
         }
         if (lane < 8) {
 #pragma unroll
-          for (int k = 0; k < 8; ++k) part[(pr * 4 + warp) * 64 + bl * 8 + k] = tl[k];
+          for (int k = 0; k < 8; ++k) part[warp * 64 + bl * 8 + k] = tl[k];
         }
       }
     }
     ptx::tc_fence_before();
     __syncthreads();
-    // 7. warp w finalises the message on leg w: normalise, store, convergence diff
-    {
+    // 6. warp 0 finalises the message on leg H, warp 1 the one on leg Lg
+    if (warp < 2) {
       float o[2];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int e = lane + 32 * h;
-        if (warp == 0) o[h] = outs[64 + e];
-        else if (warp == 2) o[h] = outs[e];
-        else {
-          const int pr = warp == 1 ? 1 : 0;
-          o[h] = part[(pr * 4 + 0) * 64 + e] + part[(pr * 4 + 1) * 64 + e] + part[(pr * 4 + 2) * 64 + e] +
-                 part[(pr * 4 + 3) * 64 + e];
-        }
+      for (int hh = 0; hh < 2; ++hh) {
+        const int e = lane + 32 * hh;
+        o[hh] = warp == 0 ? outs[e] : part[e] + part[64 + e] + part[128 + e] + part[192 + e];
       }
       float sum = o[0] + o[1];
 #pragma unroll
       for (int k = 16; k >= 1; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
       const bool scale = a.normalize && sum != 0.f;
-      const int slot = s0 + warp;
+      const int slot = s0 + (warp == 0 ? H : Lg);
       float* dst = a.msg_out + 64 * slot;
       const float* old = a.msg_in + 64 * slot;
       double n1 = 0, n2 = 0, dd = 0;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float v = scale ? o[h] / sum : o[h];
-        dst[lane + 32 * h] = v;
+      for (int hh = 0; hh < 2; ++hh) {
+        const float v = scale ? o[hh] / sum : o[hh];
+        dst[lane + 32 * hh] = v;
         if (a.slot_diff) {
-          const double ov = old[lane + 32 * h];
+          const double ov = old[lane + 32 * hh];
           n1 += (double)v * v;
           n2 += ov * ov;
           dd += (double)v * ov;
@@ -609,9 +615,8 @@ struct TcEngine {
   const int* d_off = nullptr;
   const int* d_rev = nullptr;
   const long long* d_moff = nullptr;
-  unsigned char* image = nullptr;  // split image (hi + lo); the hi half doubles as the plain one
-  unsigned char* image_hi = nullptr;
-  size_t image_bytes = 0, image_hi_bytes = 0;
+  unsigned char* image = nullptr;  // per vertex [A_pq hi | A_qp hi | A_pq lo | A_qp lo]
+  size_t image_bytes = 0;
   int* d_err = nullptr;
   int sm_count = 0;
   int occ[2] = {0, 0};
@@ -622,7 +627,6 @@ TcEngine* tc_create() { return new TcEngine(); }
 void tc_destroy(TcEngine* e) {
   if (!e) return;
   if (e->image) cudaFree(e->image);
-  if (e->image_hi) cudaFree(e->image_hi);
   if (e->d_err) cudaFree(e->d_err);
   delete e;
 }
@@ -667,20 +671,13 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  const size_t split_bytes = (size_t)nv * 8 * kBlk, hi_bytes = (size_t)nv * 4 * kBlk;
+  const size_t split_bytes = (size_t)nv * 8 * kBlk;
   if (e->image_bytes < split_bytes) {
     if (e->image) cudaFree(e->image);
     e->image = nullptr;
     err = cudaMalloc(&e->image, split_bytes);
     if (err != cudaSuccess) return err;
     e->image_bytes = split_bytes;
-  }
-  if (e->image_hi_bytes < hi_bytes) {
-    if (e->image_hi) cudaFree(e->image_hi);
-    e->image_hi = nullptr;
-    err = cudaMalloc(&e->image_hi, hi_bytes);
-    if (err != cudaSuccess) return err;
-    e->image_hi_bytes = hi_bytes;
   }
   if (!e->d_err) {
     err = cudaMalloc(&e->d_err, sizeof(int));
@@ -689,7 +686,6 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
   const int grid = (int)std::min<long long>((nv * 8192 + 255) / 256, 4096);
   tc_image_kernel<true><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image);
-  tc_image_kernel<false><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image_hi);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   constexpr TcSmem L0 = tc_smem<false>();
@@ -730,10 +726,8 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
 cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
   if (!e || !e->valid) return cudaErrorInvalidValue;
   TcArgs a;
-  a.off = e->d_off;
   a.rev = e->d_rev;
-  a.moff = e->d_moff;
-  a.image = r.split ? e->image : e->image_hi;
+  a.image = e->image;
   a.msg_in = reinterpret_cast<const float*>(r.msg_in);
   a.msg_out = reinterpret_cast<float*>(r.msg_out);
   a.nv = e->nv;
@@ -742,7 +736,7 @@ cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
   a.conv = r.conv;
   a.err = e->d_err;
   const int k = r.split ? 1 : 0;
-  const int grid = std::max(1, std::min(e->nv, e->sm_count * e->occ[k]));
+  const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[k]));
   if (r.split) {
     constexpr TcSmem L = tc_smem<true>();
     bp_tc_kernel<true><<<grid, kThreads, L.total, st>>>(a);

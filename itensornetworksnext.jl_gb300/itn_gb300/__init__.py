@@ -11,6 +11,7 @@ from . import graphs, generators, contract  # noqa: F401
 from .contract import contract_network, contraction_order  # noqa: F401
 from ._lib import ItnError, ItnArgumentError, load as load_library  # noqa: F401
 from .engine import BPEngine, RunResult  # noqa: F401
+from . import network  # noqa: F401
 
 __all__ = ["graphs", "generators", "contract", "contract_network", "contraction_order", "BPEngine", "RunResult", "ItnError", "ItnArgumentError",
-           "load_library"]
+           "load_library", "network"]

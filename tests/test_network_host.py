@@ -1,0 +1,80 @@
+"""Host logic of the named-tensor API mirror (no GPU): flattening of ITensorNetwork /
+NormNetwork onto the C-ABI layout and back, message environments, and the reference's
+argument errors (beliefpropagation.jl:16-55, contract_network.jl:12-14)."""
+import numpy as np
+import pytest
+
+from itn_gb300 import ItnArgumentError
+from itn_gb300 import network as N
+
+
+def _triangle(rng, site=True):
+    i, j, k = N.Index(2), N.Index(3), N.Index(2)
+    s = [N.Index(2) for _ in range(3)]
+    A = N.itensor(rng.standard_normal((2, 2, 3) if site else (2, 3)), *(([s[0]] if site else []) + [i, j]))
+    B = N.itensor(rng.standard_normal((3, 2, 2) if site else (3, 2)), *([j] + ([s[1]] if site else []) + [k]))
+    C = N.itensor(rng.standard_normal((2, 2, 2) if site else (2, 2)), *([k, i] + ([s[2]] if site else [])))
+    return N.ITensorNetwork({"a": A, "b": B, "c": C})
+
+
+def test_network_structure():
+    tn = _triangle(np.random.default_rng(0))
+    assert sorted(tn.edges()) == [("a", "b"), ("a", "c"), ("b", "c")]
+    assert len(tn.sitenames("a")) == 1
+    nn = N.normnetwork(tn)
+    # link names are renamed in the bra layer, site names map to themselves
+    for n, vs in tn.dimname_vertices.items():
+        assert (nn.bra(n) != n) == (len(vs) == 2)
+
+
+def test_flatten_roundtrip():
+    tn = _triangle(np.random.default_rng(1))
+    nn = N.normnetwork(tn)
+    env = N.message_environment("one", nn)
+    f = N._Flat(nn)
+    assert f.g.layers == 2 and list(f.g.phys) == [2, 2, 2]
+    back = f.unpack_messages(f.pack_messages(env, nn), env, nn)
+    for e in env.edges():
+        assert np.array_equal(back[e].data, env[e].data)
+    # canonical tensor of vertex "b": [site, legs in CSR order]
+    k = f.vidx["b"]
+    legs = [f.vs[int(f.g.nbr[s])] for s in range(f.g.off[k], f.g.off[k + 1])]
+    order = tn.sitenames("b") + sum((tn.linknames("b", w) for w in legs), [])
+    ref = tn["b"].permute(order).ravel()
+    assert np.array_equal(f.tensors[f.g.toff[k]:f.g.toff[k + 1]], ref)
+
+
+def test_message_environment_shapes():
+    tn = _triangle(np.random.default_rng(2))
+    nn = N.normnetwork(tn)
+    env = N.message_environment("one", nn)
+    assert len(env) == 6
+    m = env[("a", "b")]
+    ket = tn.linknames("a", "b")
+    assert m.dimnames == tuple(nn.bra(n) for n in ket) + tuple(ket)
+    assert np.array_equal(m.data.reshape(3, 3), np.eye(3))
+
+
+def test_stopping_criterion_errors():
+    tn = _triangle(np.random.default_rng(3), site=False)
+    msgs = N.messagecache(lambda e: N.itensor(np.ones(2), N.Index(2)), [])
+    with pytest.raises(ItnArgumentError, match="must be specified"):
+        N.beliefpropagation(tn, msgs)
+    with pytest.raises(ItnArgumentError, match="At least one"):
+        N.beliefpropagation(tn, msgs, stopping_criterion={})
+    with pytest.raises(ItnArgumentError, match="Unrecognized"):
+        N.beliefpropagation(tn, msgs, stopping_criterion={"maxiter": 2, "foo": 1})
+    assert N.select_beliefpropagation_stopping_criterion(
+        N.StopWhenAny(N.StopAfterIteration(3), N.StopWhenConverged(1e-9))) == (3, 1e-9)
+
+
+def test_contract_network_unknown_algorithm():
+    with pytest.raises(ItnArgumentError, match="not implemented"):
+        N.contract_network([], alg="optimal")
+
+
+def test_incoming_messages_exclude_reverse():
+    cache = N.messagecache(lambda e: e, [(1, 2), (2, 1), (2, 3), (3, 2)])
+    assert N.incoming_messages(cache, (2, 3)) == [(1, 2)]
+    assert N.incoming_messages(cache, (1, 2)) == []
+    assert N.incoming_messages(cache, (2, 1)) == [(3, 2)]
