@@ -956,6 +956,19 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core prepare");
   }
   if (o->split_sweeps < 0) return fail(c, ITN_ERR_ARG, "split_sweeps < 0");
+  if (c->nslots == 0) {
+    // No directed edges: every sweep is empty.  iterate_diff would be a maximum over an
+    // empty cache, which the reference rejects; with maxiter alone the loop just counts.
+    if (o->tol >= 0) return fail(c, ITN_ERR_ARG, "iterate_diff of an empty message cache (no edges)");
+    if (res) {
+      res->iterations = o->maxiter;
+      res->at_iteration = -1;
+      res->delta = INFINITY;
+      res->device_ms = 0.0;
+      res->kernel_launches = 0;
+    }
+    return ITN_OK;
+  }
   SeqPlan plan;
   if (o->schedule == ITN_SCHED_SEQUENTIAL) {
     if (!o->edges && o->n_edges > 0) return fail(c, ITN_ERR_ARG, "null edge list");

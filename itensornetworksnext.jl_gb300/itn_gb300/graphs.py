@@ -63,7 +63,8 @@ class Graph:
 
     @property
     def n_nets(self) -> int:
-        return int(self.net.max()) + 1 if self.nv else 0
+        """Number of networks (at least one, as the C ABI counts an empty network as one)."""
+        return int(self.net.max()) + 1 if self.nv else 1
 
     def degree(self, u: int) -> int:
         return int(self.off[u + 1] - self.off[u])
