@@ -165,12 +165,11 @@ def barrier(pg, device):
 
 
 def max_over_ranks(pg, x, device):
+    """Replica timing: the slowest rank defines the job time (itn_gb300.distributed)."""
     if pg is None:
         return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
+    from itn_gb300 import distributed as D
+    return D.max_over_ranks(x, device=f"cuda:{device}")
 
 
 def flush_l2(device):
