@@ -26,6 +26,7 @@
 #include "itn_common.cuh"
 #include "itn_conv.cuh"
 #include "itn_internal.h"
+#include "tc_ptx.cuh"
 
 namespace itn {
 
@@ -34,6 +35,8 @@ namespace {
 constexpr int kRedWidth = 64;  // per-warp partial-sum slots for D*D <= 64
 
 struct LegMeta {
+  uint64_t bar;            // mbarrier of the bulk copy of the site tensor
+  unsigned phase;          // its current phase parity
   int z, d, n;          // legs, physical dim, tensor elements
   int dims[kMaxLegs];
   int inner[kMaxLegs];  // prod of dims after the leg
@@ -92,6 +95,35 @@ __device__ T block_sum(T v, T* red) {
   return r;
 }
 
+// Row of D contiguous elements (the innermost leg): 16-byte vector accesses when the row
+// length is a multiple of 16 bytes (rows then start 16-byte aligned in the buffers).
+template <typename T, int D>
+__device__ __forceinline__ void load_row(const T* __restrict__ p, T (&t)[D]) {
+  if constexpr ((D * sizeof(T)) % 16 == 0) {
+    constexpr int nv = D * sizeof(T) / 16;
+    uint4 v[nv];
+#pragma unroll
+    for (int j = 0; j < nv; ++j) v[j] = reinterpret_cast<const uint4*>(p)[j];
+    memcpy(t, v, sizeof(v));
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; ++k) t[k] = p[k];
+  }
+}
+template <typename T, int D>
+__device__ __forceinline__ void store_row(T* __restrict__ p, const T (&t)[D]) {
+  if constexpr ((D * sizeof(T)) % 16 == 0) {
+    constexpr int nv = D * sizeof(T) / 16;
+    uint4 v[nv];
+    memcpy(v, t, sizeof(v));
+#pragma unroll
+    for (int j = 0; j < nv; ++j) reinterpret_cast<uint4*>(p)[j] = v[j];
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; ++k) p[k] = t[k];
+  }
+}
+
 // ---- ABSORB with compile-time bond dimension ---------------------------------------
 template <typename T, int D>
 __device__ __forceinline__ void absorb_fixed(const T* __restrict__ src, T* __restrict__ dst,
@@ -100,6 +132,21 @@ __device__ __forceinline__ void absorb_fixed(const T* __restrict__ src, T* __res
 #pragma unroll
   for (int j = 0; j < D * D; ++j) mr[j] = m[j];
   const int n = outer * inner;
+  if (inner == 1) {  // innermost leg: whole rows per thread, vector accesses
+    for (int o = threadIdx.x; o < outer; o += blockDim.x) {
+      T t[D], r[D];
+      load_row<T, D>(src + o * D, t);
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        T acc = mul(t[0], mr[b * D]);
+#pragma unroll
+        for (int k = 1; k < D; ++k) acc = fmac(t[k], mr[b * D + k], acc);
+        r[b] = acc;
+      }
+      store_row<T, D>(dst + o * D, r);
+    }
+    return;
+  }
   for (int p = threadIdx.x; p < n; p += blockDim.x) {
     const int o = p / inner, i = p - o * inner;
     const T* s = src + o * D * inner + i;
@@ -148,10 +195,17 @@ __device__ __forceinline__ void final_fixed(const T* __restrict__ src, const T* 
     const T* s = src + o * D * inner + i;
     const T* a = A + o * D * inner + i;
     T t[D], c[D];
+    if (inner == 1) {
+      load_row<T, D>(s, t);
+      load_row<T, D>(a, c);
 #pragma unroll
-    for (int k = 0; k < D; ++k) t[k] = s[k * inner];
+      for (int b = 0; b < D; ++b) c[b] = conjx(c[b]);
+    } else {
 #pragma unroll
-    for (int b = 0; b < D; ++b) c[b] = conjx(a[b * inner]);
+      for (int k = 0; k < D; ++k) t[k] = s[k * inner];
+#pragma unroll
+      for (int b = 0; b < D; ++b) c[b] = conjx(a[b * inner]);
+    }
 #pragma unroll
     for (int b = 0; b < D; ++b)
 #pragma unroll
@@ -302,6 +356,12 @@ __global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
 
   if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(&meta->bar, 1);
+    ptx::fence_mbar_init();
+    meta->phase = 0;
+  }
+  __syncthreads();
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
@@ -328,15 +388,33 @@ __global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
     }
     __syncthreads();
     const int z = meta->z, n = meta->n;
-    // stage the site tensor (buffer 0) and the incoming messages m_{w->u}
+    // stage the site tensor (buffer 0) and the incoming messages m_{w->u}; a 16-byte
+    // aligned tensor in shared-memory buffers arrives by one bulk (TMA) copy
     const T* A_g = tens + a.toff[u];
     T* A = bufs;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+    const bool bulk = a.gscratch == nullptr && ((a.toff[u] * sizeof(T)) & 15) == 0 &&
+                      ((n * sizeof(T)) & 15) == 0 && n * sizeof(T) >= 4096 && n * sizeof(T) < (1u << 20);
+    if (bulk) {
+      if (threadIdx.x == 0) {
+        ptx::fence_proxy_async_smem();  // earlier generic accesses to buffer 0 come first
+        ptx::mbar_arrive_expect_tx(&meta->bar, (uint32_t)(n * sizeof(T)));
+        ptx::bulk_g2s(A, A_g, (uint32_t)(n * sizeof(T)), &meta->bar);
+      }
+    } else {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+    }
     const int s0 = a.off[u];
     for (int l = 0; l < z; ++l) {
       const int D2 = meta->dims[l] * meta->dims[l];
       const T* src = min_ + a.moff[a.rev[s0 + l]];
       for (int j = threadIdx.x; j < D2; j += blockDim.x) msgs[meta->moffs[l] + j] = src[j];
+    }
+    if (bulk) {
+      // bounded wait; on timeout the copy is re-done with plain loads
+      if (!__syncthreads_and(ptx::mbar_wait_bounded(&meta->bar, meta->phase, 1u << 26))) {
+        for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+      }
+      if (threadIdx.x == 0) meta->phase ^= 1;
     }
     __syncthreads();
     const int nops = (int)prog[0];
