@@ -120,6 +120,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 template <bool SPLIT>
 __device__ __forceinline__ void store_half_bf16(unsigned char* blk, unsigned char* blk_lo, int r, int c0,
                                                 const float (&v)[32]) {
+  if constexpr (!SPLIT) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      *reinterpret_cast<uint4*>(blk + blk_off(r, c0 + c * 8)) =
+          make_uint4(pack_bf16(v[c * 8 + 0], v[c * 8 + 1]), pack_bf16(v[c * 8 + 2], v[c * 8 + 3]),
+                     pack_bf16(v[c * 8 + 4], v[c * 8 + 5]), pack_bf16(v[c * 8 + 6], v[c * 8 + 7]));
+    return;
+  }
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float hi[8], lo[8];
@@ -267,16 +275,21 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
       for (int j = 0; j < 4; ++j) {
         const int ko = kq + j;
         const float w = ma[bo * 8 + ko];
-        float hv[8], lv[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) split_bf16(w * mb[k], hv[k], lv[k]);
         const uint32_t off = blk_off(bo * 8 + bi, ko * 8);
-        *reinterpret_cast<uint4*>(reg + off) = make_uint4(pack_bf16(hv[0], hv[1]), pack_bf16(hv[2], hv[3]),
-                                                          pack_bf16(hv[4], hv[5]), pack_bf16(hv[6], hv[7]));
-        if constexpr (SPLIT)
+        if constexpr (SPLIT) {
+          float hv[8], lv[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) split_bf16(w * mb[k], hv[k], lv[k]);
+          *reinterpret_cast<uint4*>(reg + off) = make_uint4(pack_bf16(hv[0], hv[1]), pack_bf16(hv[2], hv[3]),
+                                                            pack_bf16(hv[4], hv[5]), pack_bf16(hv[6], hv[7]));
           *reinterpret_cast<uint4*>(reg + kBlk + off) =
               make_uint4(pack_bf16(lv[0], lv[1]), pack_bf16(lv[2], lv[3]), pack_bf16(lv[4], lv[5]),
                          pack_bf16(lv[6], lv[7]));
+        } else {
+          *reinterpret_cast<uint4*>(reg + off) =
+              make_uint4(pack_bf16(w * mb[0], w * mb[1]), pack_bf16(w * mb[2], w * mb[3]),
+                         pack_bf16(w * mb[4], w * mb[5]), pack_bf16(w * mb[6], w * mb[7]));
+        }
       }
     }
     ptx::fence_proxy_async_smem();
