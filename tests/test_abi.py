@@ -59,3 +59,16 @@ def test_create_without_gpu_reports_status(lib_built):
     ctx = ctypes.c_void_p()
     st = lib.itn_create(ctypes.byref(ctx), 0, 0)
     assert st == L.ITN_ERR_CUDA and not ctx.value
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without libitn_gpu.so there is no fallback: loading raises."""
+    import importlib
+    from itn_gb300 import _lib as L
+    saved = L._lib
+    try:
+        L._lib = None
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            L.load(str(tmp_path / "libitn_gpu.so"))
+    finally:
+        L._lib = saved
