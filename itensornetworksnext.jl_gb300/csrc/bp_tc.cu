@@ -69,15 +69,18 @@ struct TcSmem {
 //   Z23[b23, k23] = sum_{s,b01} A[s,b01,b23] X[(s,k23),b01]  (G2: A_qp, M=64 N=64 K=128)
 // and emits the messages on legs 2 and 3; half 1 does the same with P23, A_pq (Y, Z01)
 // for legs 0 and 1.  A half needs one operand layout only (16 KB of BF16, 32 KB split).
+// G2 runs as two K = 64 halves (s = 0, then s = 1) so that one 64 x 64 operand buffer
+// holds P, then XT0, then XT1: 8 CTAs fit on an SM (4 for the split variant), which
+// covers the 2 V half-vertex items of the 32 x 32 lattice in two waves instead of three.
 // img : A_qp (half 0) or A_pq (half 1): hi [+ lo]          16 KB [32 KB]
-// reg : P (hi [+ lo]) while G1 runs, then XT (hi [+ lo])   16 KB [32 KB]
+// reg : P, then XT0, then XT1 (hi [+ lo])                   8 KB [16 KB]
 // msg : incoming messages m0..m3 (FP32)                     1 KB
 template <bool SPLIT>
 __host__ __device__ constexpr TcSmem tc_smem() {
   TcSmem L{};
   uint32_t o = 0;
   L.img = o;  o += (SPLIT ? 4 : 2) * kBlk;
-  L.reg = o;  o += (SPLIT ? 4 : 2) * kBlk;
+  L.reg = o;  o += (SPLIT ? 2 : 1) * kBlk;
   L.msg = o;  o += 4 * 64 * 4;
   L.outs = o; o += 64 * 4;
   L.part = o; o += 4 * 64 * 4;
@@ -99,15 +102,6 @@ struct TcArgs {
   int* err;
 };
 
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
-  float* p = v;
-  ptx::tmem_ld16(taddr + 0, *reinterpret_cast<float(*)[16]>(p + 0));
-  ptx::tmem_ld16(taddr + 16, *reinterpret_cast<float(*)[16]>(p + 16));
-  ptx::tmem_ld16(taddr + 32, *reinterpret_cast<float(*)[16]>(p + 32));
-  ptx::tmem_ld16(taddr + 48, *reinterpret_cast<float(*)[16]>(p + 48));
-  ptx::tmem_wait_ld();
-}
-
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   float* p = v;
   ptx::tmem_ld16(taddr + 0, *reinterpret_cast<float(*)[16]>(p + 0));
@@ -115,65 +109,40 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   ptx::tmem_wait_ld();
 }
 
-// Store 32 entries (columns c0 .. c0+31) of an accumulator row as BF16 (hi [+ lo]) into
-// row r of a 64 x 64 block.
+// Pack 32 accumulator entries as BF16 pairs: hi (and, when SPLIT, the BF16 residual lo).
 template <bool SPLIT>
-__device__ __forceinline__ void store_half_bf16(unsigned char* blk, unsigned char* blk_lo, int r, int c0,
-                                                const float (&v)[32]) {
-  if constexpr (!SPLIT) {
+__device__ __forceinline__ void pack_row32(const float (&v)[32], uint32_t* hk, uint32_t* lk) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
-      *reinterpret_cast<uint4*>(blk + blk_off(r, c0 + c * 8)) =
-          make_uint4(pack_bf16(v[c * 8 + 0], v[c * 8 + 1]), pack_bf16(v[c * 8 + 2], v[c * 8 + 3]),
-                     pack_bf16(v[c * 8 + 4], v[c * 8 + 5]), pack_bf16(v[c * 8 + 6], v[c * 8 + 7]));
-    return;
-  }
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    float hi[8], lo[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) split_bf16(v[c * 8 + e], hi[e], lo[e]);
-    const uint32_t off = blk_off(r, c0 + c * 8);
-    *reinterpret_cast<uint4*>(blk + off) =
-        make_uint4(pack_bf16(hi[0], hi[1]), pack_bf16(hi[2], hi[3]), pack_bf16(hi[4], hi[5]),
-                   pack_bf16(hi[6], hi[7]));
-    if constexpr (SPLIT)
-      *reinterpret_cast<uint4*>(blk_lo + off) =
-          make_uint4(pack_bf16(lo[0], lo[1]), pack_bf16(lo[2], lo[3]), pack_bf16(lo[4], lo[5]),
-                     pack_bf16(lo[6], lo[7]));
+  for (int e = 0; e < 16; ++e) {
+    if constexpr (SPLIT) {
+      float h0, l0, h1, l1;
+      split_bf16(v[2 * e], h0, l0);
+      split_bf16(v[2 * e + 1], h1, l1);
+      hk[e] = pack_bf16(h0, h1);
+      lk[e] = pack_bf16(l0, l1);
+    } else {
+      hk[e] = pack_bf16(v[2 * e], v[2 * e + 1]);
+    }
   }
 }
 
-// Store one 64-entry accumulator row as BF16 (hi [+ lo]) into row r of a 64 x 64 block.
-template <bool SPLIT>
-__device__ __forceinline__ void store_row_bf16(unsigned char* blk, unsigned char* blk_lo, int r,
-                                               const float (&v)[64]) {
+// Store a packed 64-entry row (32 BF16 pairs) into row r of a 64 x 64 block.
+__device__ __forceinline__ void store_row_packed(unsigned char* blk, int r, const uint32_t (&w)[32]) {
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    float hi[8], lo[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) split_bf16(v[c * 8 + e], hi[e], lo[e]);
-    const uint32_t off = blk_off(r, c * 8);
-    *reinterpret_cast<uint4*>(blk + off) =
-        make_uint4(pack_bf16(hi[0], hi[1]), pack_bf16(hi[2], hi[3]), pack_bf16(hi[4], hi[5]),
-                   pack_bf16(hi[6], hi[7]));
-    if constexpr (SPLIT)
-      *reinterpret_cast<uint4*>(blk_lo + off) =
-          make_uint4(pack_bf16(lo[0], lo[1]), pack_bf16(lo[2], lo[3]), pack_bf16(lo[4], lo[5]),
-                     pack_bf16(lo[6], lo[7]));
-  }
+  for (int c = 0; c < 8; ++c)
+    *reinterpret_cast<uint4*>(blk + blk_off(r, c * 8)) =
+        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
 }
 
-// Issue D (+)= A * B^T over `nk` K-steps of 16 with the split terms when SPLIT.
+// Issue D (+)= A * B^T over K = 64 (four K-steps of 16), with the split terms when SPLIT.
 template <bool SPLIT>
-__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t b, uint32_t b_lo,
-                                          uint32_t idesc, int nk, bool blocked_k) {
-#pragma unroll 1
-  for (int j = 0; j < nk; ++j) {
-    // K-step j: core columns 2j, 2j+1; for K = 128 (blocked_k) the s-block changes at j = 4
-    const uint32_t ko = blocked_k ? (uint32_t)(j >> 2) * kBlk + (uint32_t)(2 * (j & 3)) * 128
-                                  : (uint32_t)(2 * j) * 128;
-    ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc, j > 0);
+__device__ __forceinline__ void mma_k64(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t b, uint32_t b_lo,
+                                        uint32_t idesc, bool accumulate) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t ko = (uint32_t)(2 * j) * 128;  // core columns 2j, 2j+1
+    ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc,
+                  accumulate || j > 0);
     if constexpr (SPLIT) {
       ptx::mma_bf16(d, ptx::smem_desc(a_lo + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc, 1);
       ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b_lo + ko, 128, 1024), idesc, 1);
@@ -195,7 +164,7 @@ __device__ __forceinline__ void issue_image(unsigned char* sm_img, const unsigne
 
 // ---- the sweep kernel --------------------------------------------------------------------
 template <bool SPLIT>
-__global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
+__global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   constexpr TcSmem L = tc_smem<SPLIT>();
   uint64_t* bar_load = reinterpret_cast<uint64_t*>(sm + L.bars);
@@ -207,8 +176,6 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
   unsigned char* reg = sm + L.reg;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n_items = 2 * a.nv;
-
-  if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
 
   if (warp == 0) {
     ptx::tmem_alloc(taddr_s, kTmemCols);
@@ -240,13 +207,16 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
   // prefetched into registers while the current one is processed.
   const int l0 = tid >> 6, e0 = tid & 63;
   float pre0 = 0.f, pre1 = 0.f;
-  if ((int)blockIdx.x < n_items) {
+  // the operand image is static: its copy starts before the done flag is read
+  const bool first = (int)blockIdx.x < n_items;
+  if (first && tid == 0) issue_image<SPLIT>(sm + L.img, a.image, blockIdx.x, bar_load);
+  const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
+  if (first && !skip) {
     const int u = blockIdx.x >> 1;
     pre0 = a.msg_in[64 * a.rev[4 * u + l0] + e0];
     pre1 = a.msg_in[64 * a.rev[4 * u + l0 + 2] + e0];
-    if (tid == 0) issue_image<SPLIT>(sm + L.img, a.image, blockIdx.x, bar_load);
   }
-  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+  for (int item = skip ? n_items : (int)blockIdx.x; item < n_items; item += gridDim.x) {
     const int u = item >> 1, h = item & 1;
     const int s0 = 4 * u;
     // pair (A, B) builds P; pair (H, Lg) receives the outgoing messages
@@ -302,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
     ph_load ^= 1;
     if (tid == 0) {
       ptx::tc_fence_after();
-      mma_chain<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc128, 4, false);
+      mma_k64<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc128, false);
       ptx::mma_commit(bar_mma);
     }
     if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
@@ -312,32 +282,50 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
     }
     ph_mma ^= 1;
     ptx::tc_fence_after();
-    // 3. epilogue 1: accumulator row (s, r) -> XT[s] row r (BF16 hi [+ lo]), over P
-    {
-      const int row = warp * 32 + lane, s = row >> 6, r = row & 63;
+    // 3. epilogue 1: accumulator row (s, r) -> row r of XT_s (BF16 hi [+ lo]).  Warps 0, 1
+    //    hold s = 0 and store XT0 now; warps 2, 3 keep s = 1 packed in registers until the
+    //    first half of G2 has consumed XT0 (G2's accumulator overwrites their TMEM lanes).
+    const int xr = (warp * 32 + lane) & 63;
+    uint32_t hk[32], lk[SPLIT ? 32 : 1];
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        float v[32];
-        tmem_ld32(tq + 32 * half, v);
-        store_half_bf16<SPLIT>(reg + s * kBlk, reg + 2 * kBlk + s * kBlk, r, 32 * half, v);
-      }
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(tq + 32 * half, v);
+      pack_row32<SPLIT>(v, hk + 16 * half, lk + (SPLIT ? 16 * half : 0));
+    }
+    if (warp < 2) {
+      store_row_packed(reg, xr, hk);
+      if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
     }
     ptx::tc_fence_before();
     ptx::fence_proxy_async_smem();
     __syncthreads();
-    // 4. second GEMM: Z = image (rows of the other pair, K = (s, this pair)) x XT^T, M = 64
-    if (tid == 0) {
+    // 4. second GEMM, Z = image (rows of the other pair, K = (s, this pair)) x XT^T with
+    //    M = 64, in two K halves: s = 0 from XT0, then s = 1 from XT1 in the same buffer
+#pragma unroll 1
+    for (int sh = 0; sh < 2; ++sh) {
+      if (sh == 1) {
+        if (warp >= 2) {
+          store_row_packed(reg, xr, hk);
+          if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
+        }
+        ptx::fence_proxy_async_smem();
+        __syncthreads();
+      }
+      if (tid == 0) {
+        ptx::tc_fence_after();
+        mma_k64<SPLIT>(tmem, Aimg + sh * kBlk, Aimg + Alo + sh * kBlk, R, R + kBlk, idesc64, sh == 1);
+        ptx::mma_commit(bar_mma);
+      }
+      if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
+        if (tid == 0) atomicExch(a.err, 1);
+        ok = false;
+        break;
+      }
+      ph_mma ^= 1;
       ptx::tc_fence_after();
-      mma_chain<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + 2 * kBlk, idesc64, 8, true);
-      ptx::mma_commit(bar_mma);
     }
-    if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
-      if (tid == 0) atomicExch(a.err, 1);
-      ok = false;
-      break;
-    }
-    ph_mma ^= 1;
-    ptx::tc_fence_after();
+    if (!ok) break;
     // the image's only readers are done: fetch the next item's image now
     if (tid == 0 && item + (int)gridDim.x < n_items) issue_image<SPLIT>(sm + L.img, a.image, item + gridDim.x, bar_load);
     // 5. epilogue 2 from registers.  Row zrow = (bh, bl) of Z (bra indices of legs H, Lg),
@@ -354,15 +342,16 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
         mh[k] = msg[H * 64 + (bh & 7) * 8 + k];
       }
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {  // columns kh = 4 half .. 4 half + 3
-        float z[32];
-        tmem_ld32(tq + 32 * half, z);
+      for (int qc = 0; qc < 4; ++qc) {  // columns kh = 2 qc, 2 qc + 1
+        float z[16];
+        ptx::tmem_ld16(tq + 16 * qc, z);
+        ptx::tmem_wait_ld();
         if (zrow >= 0) {
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
+          for (int j = 0; j < 2; ++j)
 #pragma unroll
             for (int kl = 0; kl < 8; ++kl) {
-              const int kh = 4 * half + j;
+              const int kh = 2 * qc + j;
               th[kh] = fmaf(z[j * 8 + kl], ml[kl], th[kh]);
               tl[kl] = fmaf(z[j * 8 + kl], mh[kh], tl[kl]);
             }
@@ -389,34 +378,37 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
     }
     ptx::tc_fence_before();
     __syncthreads();
-    // 6. warp 0 finalises the message on leg H, warp 1 the one on leg Lg
-    if (warp < 2) {
+    // 6. finalise: warps 0, 1 the message on leg H, warps 2, 3 the one on leg Lg; every
+    //    warp sums all 64 entries of its message and stores the half (32 entries) it owns
+    {
+      const bool lo_leg = warp >= 2;
       float o[2];
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
         const int e = lane + 32 * hh;
-        o[hh] = warp == 0 ? outs[e] : part[e] + part[64 + e] + part[128 + e] + part[192 + e];
+        o[hh] = !lo_leg ? outs[e] : part[e] + part[64 + e] + part[128 + e] + part[192 + e];
       }
       float sum = o[0] + o[1];
 #pragma unroll
       for (int k = 16; k >= 1; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
       const bool scale = a.normalize && sum != 0.f;
-      const int slot = s0 + (warp == 0 ? H : Lg);
+      const int slot = s0 + (!lo_leg ? H : Lg);
+      const int own = warp & 1;  // which half of the 64 entries this warp stores
       float* dst = a.msg_out + 64 * slot;
       const float* old = a.msg_in + 64 * slot;
-      double n1 = 0, n2 = 0, dd = 0;
+      const float v = scale ? o[own] / sum : o[own];
+      dst[lane + 32 * own] = v;
+      // the convergence diff needs all 64 entries: the even warp of each leg computes it
+      if (a.slot_diff && own == 0) {
+        double n1 = 0, n2 = 0, dd = 0;
 #pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const float v = scale ? o[hh] / sum : o[hh];
-        dst[lane + 32 * hh] = v;
-        if (a.slot_diff) {
+        for (int hh = 0; hh < 2; ++hh) {
+          const float vv = scale ? o[hh] / sum : o[hh];
           const double ov = old[lane + 32 * hh];
-          n1 += (double)v * v;
+          n1 += (double)vv * vv;
           n2 += ov * ov;
-          dd += (double)v * ov;
+          dd += (double)vv * ov;
         }
-      }
-      if (a.slot_diff) {
 #pragma unroll
         for (int k = 16; k >= 1; k >>= 1) {
           n1 += __shfl_xor_sync(0xffffffffu, n1, k);
@@ -442,13 +434,14 @@ __global__ void __launch_bounds__(kThreads, 6) bp_tc_kernel(TcArgs a) {
     ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);
     ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls);
   }
+  if (skip && first && tid == 0) ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);  // unused image copy
   ptx::tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, kTmemCols);
   }
-  if (a.conv) conv_finish_cta(a.conv);
+  if (a.conv && !skip) conv_finish_cta(a.conv);
 }
 
 // ---- operand image: per vertex [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ the same for lo] ---------
