@@ -40,7 +40,10 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kBlk = 8192;                 // bytes of one 64 x 64 BF16 operand block
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
+constexpr uint32_t kMaxDepPolls = 1u << 22; // bounded waits on another item (64 ns apart)
 constexpr int kTmemCols = 64;
+constexpr int kGroupsBf16 = 8;             // persistent kernel: 4-warp groups per CTA
+constexpr int kGroupsSplit = 4;
 
 // row -> TMEM lane for an M = 64 accumulator (filled from the self-test probe)
 __constant__ signed char c_row_of_lane[128];
@@ -60,8 +63,8 @@ __device__ __forceinline__ void split_bf16(float x, float& hi, float& lo) {
 }
 
 struct TcSmem {
-  // offsets in bytes from the dynamic shared memory base
-  uint32_t img, reg, msg, outs, part, bars, taddr, total;
+  // offsets in bytes from a group's shared-memory slice; stride = slice size
+  uint32_t img, reg, msg, outs, part, bars, taddr, total, stride;
 };
 
 // Work item = half of a vertex.  Half 0 builds P01 = m0 (x) m1, computes
@@ -87,6 +90,7 @@ __host__ __device__ constexpr TcSmem tc_smem() {
   L.bars = o; o += 16;
   L.taddr = o; o += 16;
   L.total = o;
+  L.stride = (o + 1023u) & ~1023u;
   return L;
 }
 
@@ -100,6 +104,10 @@ struct TcArgs {
   double* slot_diff;
   ConvState* conv;             // diffs + outer-loop step (may be null)
   int* err;
+  int nsweeps;                 // persistent kernel: sweeps to run (at most 4095)
+  unsigned long long* tagged;  // persistent kernel: 4 buffers of tagged entries
+  size_t tagged_stride;        // entries per tagged buffer (64 per slot)
+  unsigned* epoch;             // persistent kernel: [0] epoch of the tags, [1] CTA ticket
 };
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -163,22 +171,106 @@ __device__ __forceinline__ void issue_image(unsigned char* sm_img, const unsigne
 }
 
 // ---- the sweep kernel --------------------------------------------------------------------
-template <bool SPLIT>
-__global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a) {
-  extern __shared__ __align__(1024) unsigned char sm[];
+// GROUPS independent 4-warp groups per CTA, each with its own shared-memory slice, pair
+// of mbarriers, named barrier (1 + group) and 64 TMEM columns.
+//
+// PERSIST: one cooperative launch runs `nsweeps` parallel sweeps without kernel
+// boundaries.  Sweep 0 reads the plain FP32 input buffer and the last sweep writes the
+// plain output buffer; in between, messages travel through four rotating buffers of
+// tagged entries (FP32 value in the low word, tag = (epoch << 12) | sweep in the high
+// word, written and read as single 64-bit accesses), so each thread waits only for the
+// two entries it reads and no flag or memory fence is needed.  Four buffers suffice:
+// the item writing buffer (t + 1) % 4 at sweep t needed, three sweeps earlier, inputs
+// whose producers had read that buffer's previous contents (every vertex has two legs
+// per half), so nothing still unread is overwritten.
+__device__ __forceinline__ void group_sync(uint32_t id) {
+  asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+__device__ __forceinline__ bool group_and(uint32_t id, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred pi, po;\n\t"
+      "setp.ne.u32 pi, %1, 0;\n\t"
+      "bar.red.and.pred po, %2, 128, pi;\n\t"
+      "selp.u32 %0, 1, 0, po;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(id)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ unsigned long long ld_tagged(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_tagged(unsigned long long* p, float v, uint32_t tag) {
+  const unsigned long long w = ((unsigned long long)tag << 32) | __float_as_uint(v);
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(w) : "memory");
+}
+__device__ __forceinline__ uint32_t sweep_tag(uint32_t epoch, int t) { return (epoch << 12) | (uint32_t)t; }
+
+// This thread's two incoming entries of `item` for sweep t (no waiting): from the plain
+// input buffer at t = 0 (tagged as ready), else from the tagged buffer of sweep t.
+__device__ __forceinline__ void fetch_in(const TcArgs& a, uint32_t epoch, int item, int t, int l0, int e0,
+                                         unsigned long long& w0, unsigned long long& w1) {
+  const int u = item >> 1;
+  const int sa = a.rev[4 * u + l0], sb = a.rev[4 * u + l0 + 2];
+  if (t == 0) {
+    const unsigned long long tg = (unsigned long long)sweep_tag(epoch, 0) << 32;
+    w0 = tg | __float_as_uint(__ldcg(a.msg_in + 64 * sa + e0));
+    w1 = tg | __float_as_uint(__ldcg(a.msg_in + 64 * sb + e0));
+  } else {
+    const unsigned long long* tb = a.tagged + (size_t)(t & 3) * a.tagged_stride;
+    w0 = ld_tagged(tb + 64 * sa + e0);
+    w1 = ld_tagged(tb + 64 * sb + e0);
+  }
+}
+
+// Wait (bounded; giving up early once another group has raised the error flag) until
+// both entries carry the tag of sweep t.
+__device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int item, int t, int l0, int e0,
+                                        unsigned long long& w0, unsigned long long& w1) {
+  const uint32_t want = sweep_tag(epoch, t);
+  if ((uint32_t)(w0 >> 32) == want && (uint32_t)(w1 >> 32) == want) return true;
+  const int u = item >> 1;
+  const unsigned long long* tb = a.tagged + (size_t)(t & 3) * a.tagged_stride;
+  const unsigned long long* p0 = tb + 64 * a.rev[4 * u + l0] + e0;
+  const unsigned long long* p1 = tb + 64 * a.rev[4 * u + l0 + 2] + e0;
+  for (uint32_t polls = 0; polls < kMaxDepPolls; ++polls) {
+    if ((uint32_t)(w0 >> 32) != want) w0 = ld_tagged(p0);
+    if ((uint32_t)(w1 >> 32) != want) w1 = ld_tagged(p1);
+    if ((uint32_t)(w0 >> 32) == want && (uint32_t)(w1 >> 32) == want) return true;
+    if (*reinterpret_cast<volatile int*>(a.err)) return false;
+    __nanosleep(32);
+  }
+  atomicExch(a.err, 2);
+  return false;
+}
+
+template <bool SPLIT, int GROUPS, bool PERSIST>
+__global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4 : 8)) bp_tc_kernel(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm_all[];
   constexpr TcSmem L = tc_smem<SPLIT>();
+  const int g = GROUPS > 1 ? (int)(threadIdx.x >> 7) : 0;
+  const uint32_t bar_id = 1 + g;
+  unsigned char* sm = sm_all + g * L.stride;
   uint64_t* bar_load = reinterpret_cast<uint64_t*>(sm + L.bars);
   uint64_t* bar_mma = bar_load + 1;
-  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm + L.taddr);
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm_all + L.taddr);  // group 0 holds the CTA's
   float* msg = reinterpret_cast<float*>(sm + L.msg);    // [4][64] incoming
   float* outs = reinterpret_cast<float*>(sm + L.outs);  // [64] message on the pair's first leg
   float* part = reinterpret_cast<float*>(sm + L.part);  // [4 warps][64] partials, second leg
   unsigned char* reg = sm + L.reg;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x & (kThreads - 1), warp = tid >> 5, lane = tid & 31;
   const int n_items = 2 * a.nv;
+  // groups are numbered across CTAs first, so the groups with one item more than the
+  // others are spread over all SMs
+  const int gid = g * gridDim.x + blockIdx.x, ngroups = gridDim.x * GROUPS;
+  const int nsweeps = PERSIST ? a.nsweeps : 1;
+  const uint32_t epoch = PERSIST ? a.epoch[0] : 0u;
 
-  if (warp == 0) {
-    ptx::tmem_alloc(taddr_s, kTmemCols);
+  if (threadIdx.x < 32) {
+    ptx::tmem_alloc(taddr_s, kTmemCols * GROUPS);
     ptx::tmem_relinquish();
   }
   if (tid == 0) {
@@ -189,13 +281,14 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
-  const uint32_t tmem = *taddr_s;
+  const uint32_t tmem = *taddr_s + (uint32_t)(kTmemCols * g);
   const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
   const uint32_t sbase = ptx::smem_u32(sm);
   const uint32_t Aimg = sbase + L.img, Alo = 2 * kBlk;
   const uint32_t R = sbase + L.reg;
   uint32_t ph_load = 0, ph_mma = 0;
-  bool ok = true;  // false after a bounded wait gave up (block-uniform)
+  bool ok = true;    // group-uniform: false once a bounded wait gave up
+  bool fail = false; // this thread's waits (folded into `ok` once per item)
   constexpr uint32_t idesc128 = ptx::idesc_bf16_f32(128, 64);
   constexpr uint32_t idesc64 = ptx::idesc_bf16_f32(64, 64);
   // M = 64 accumulator row held by this thread (-1: lane unused)
@@ -204,34 +297,33 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
   // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
   // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
   // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next item are
-  // prefetched into registers while the current one is processed.
+  // fetched while the current one is processed.
   const int l0 = tid >> 6, e0 = tid & 63;
-  float pre0 = 0.f, pre1 = 0.f;
+  unsigned long long w0 = 0, w1 = 0;
   // the operand image is static: its copy starts before the done flag is read
-  const bool first = (int)blockIdx.x < n_items;
-  if (first && tid == 0) issue_image<SPLIT>(sm + L.img, a.image, blockIdx.x, bar_load);
+  const bool first = gid < n_items;
+  if (first && tid == 0) issue_image<SPLIT>(sm + L.img, a.image, gid, bar_load);
   const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
-  if (first && !skip) {
-    const int u = blockIdx.x >> 1;
-    pre0 = a.msg_in[64 * a.rev[4 * u + l0] + e0];
-    pre1 = a.msg_in[64 * a.rev[4 * u + l0 + 2] + e0];
-  }
-  for (int item = skip ? n_items : (int)blockIdx.x; item < n_items; item += gridDim.x) {
+  if (first && !skip) fetch_in(a, epoch, gid, 0, l0, e0, w0, w1);
+  int t = (first && !skip) ? 0 : nsweeps, item = gid;
+  while (t < nsweeps) {
+    // the item after this one: the next of this group in the sweep, else the first of
+    // the next sweep
+    int item2 = item + ngroups, t2 = t;
+    if (item2 >= n_items) {
+      item2 = gid;
+      ++t2;
+    }
+    const bool has_next = t2 < nsweeps;
+    const bool last = t == nsweeps - 1;
     const int u = item >> 1, h = item & 1;
     const int s0 = 4 * u;
     // pair (A, B) builds P; pair (H, Lg) receives the outgoing messages
     const int pa = h ? 2 : 0, pb = pa + 1, H = h ? 0 : 2, Lg = H + 1;
-    msg[l0 * 64 + e0] = pre0;
-    msg[(l0 + 2) * 64 + e0] = pre1;
-    {
-      const int nx = item + gridDim.x;
-      if (nx < n_items) {
-        const int un = nx >> 1;
-        pre0 = a.msg_in[64 * a.rev[4 * un + l0] + e0];
-        pre1 = a.msg_in[64 * a.rev[4 * un + l0 + 2] + e0];
-      }
-    }
-    __syncthreads();
+    if (!wait_in(a, epoch, item, t, l0, e0, w0, w1)) fail = true;
+    msg[l0 * 64 + e0] = __uint_as_float((uint32_t)w0);
+    msg[(l0 + 2) * 64 + e0] = __uint_as_float((uint32_t)w1);
+    group_sync(bar_id);
     // 1. P = m_pa (x) m_pb in core layout: thread t writes row bi = t & 7 of the cores
     //    (bo = (t >> 3) & 7, ko = 4 (t >> 6) .. +3); 8 consecutive threads fill one
     //    128-byte core, so the 16-byte stores are free of bank conflicts
@@ -263,23 +355,16 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
       }
     }
     ptx::fence_proxy_async_smem();
+    group_sync(bar_id);
     // 2. first GEMM: rows (s, r) of the image times P^T -> TMEM cols 0..63
-    if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls))) {
-      if (tid == 0) atomicExch(a.err, 1);
-      ok = false;
-      break;
-    }
-    ph_load ^= 1;
     if (tid == 0) {
+      if (!ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls)) fail = true;
       ptx::tc_fence_after();
       mma_k64<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc128, false);
       ptx::mma_commit(bar_mma);
     }
-    if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
-      if (tid == 0) atomicExch(a.err, 1);
-      ok = false;
-      break;
-    }
+    ph_load ^= 1;
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
     ph_mma ^= 1;
     ptx::tc_fence_after();
     // 3. epilogue 1: accumulator row (s, r) -> row r of XT_s (BF16 hi [+ lo]).  Warps 0, 1
@@ -299,35 +384,33 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
     }
     ptx::tc_fence_before();
     ptx::fence_proxy_async_smem();
-    __syncthreads();
+    group_sync(bar_id);
     // 4. second GEMM, Z = image (rows of the other pair, K = (s, this pair)) x XT^T with
     //    M = 64, in two K halves: s = 0 from XT0, then s = 1 from XT1 in the same buffer
-#pragma unroll 1
-    for (int sh = 0; sh < 2; ++sh) {
-      if (sh == 1) {
-        if (warp >= 2) {
-          store_row_packed(reg, xr, hk);
-          if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
-        }
-        ptx::fence_proxy_async_smem();
-        __syncthreads();
-      }
-      if (tid == 0) {
-        ptx::tc_fence_after();
-        mma_k64<SPLIT>(tmem, Aimg + sh * kBlk, Aimg + Alo + sh * kBlk, R, R + kBlk, idesc64, sh == 1);
-        ptx::mma_commit(bar_mma);
-      }
-      if (!__syncthreads_and(ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls))) {
-        if (tid == 0) atomicExch(a.err, 1);
-        ok = false;
-        break;
-      }
-      ph_mma ^= 1;
+    if (tid == 0) {
       ptx::tc_fence_after();
+      mma_k64<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc64, false);
+      ptx::mma_commit(bar_mma);
     }
-    if (!ok) break;
-    // the image's only readers are done: fetch the next item's image now
-    if (tid == 0 && item + (int)gridDim.x < n_items) issue_image<SPLIT>(sm + L.img, a.image, item + gridDim.x, bar_load);
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
+    ph_mma ^= 1;
+    if (warp >= 2) {
+      store_row_packed(reg, xr, hk);
+      if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
+    }
+    ptx::fence_proxy_async_smem();
+    group_sync(bar_id);
+    if (tid == 0) {
+      ptx::tc_fence_after();
+      mma_k64<SPLIT>(tmem, Aimg + kBlk, Aimg + Alo + kBlk, R, R + kBlk, idesc64, true);
+      ptx::mma_commit(bar_mma);
+    }
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
+    ph_mma ^= 1;
+    ptx::tc_fence_after();
+    // the image's only readers are done: fetch the next item's image and incoming entries
+    if (tid == 0 && has_next) issue_image<SPLIT>(sm + L.img, a.image, item2, bar_load);
+    if (has_next) fetch_in(a, epoch, item2, t2, l0, e0, w0, w1);
     // 5. epilogue 2 from registers.  Row zrow = (bh, bl) of Z (bra indices of legs H, Lg),
     //    columns (kh, kl):
     //      outH[bh][kh] = sum_{bl,kl} Z[(bh,bl)][(kh,kl)] m_Lg[bl][kl]   (sum over 8 rows)
@@ -377,7 +460,13 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
       }
     }
     ptx::tc_fence_before();
-    __syncthreads();
+    // one consensus per item on the bounded waits, folded into the barrier the final
+    // stage needs anyway
+    if (!group_and(bar_id, !fail)) {
+      if (tid == 0) atomicExch(a.err, 1);
+      ok = false;
+      break;
+    }
     // 6. finalise: warps 0, 1 the message on leg H, warps 2, 3 the one on leg Lg; every
     //    warp sums all 64 entries of its message and stores the half (32 entries) it owns
     {
@@ -394,12 +483,16 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
       const bool scale = a.normalize && sum != 0.f;
       const int slot = s0 + (!lo_leg ? H : Lg);
       const int own = warp & 1;  // which half of the 64 entries this warp stores
-      float* dst = a.msg_out + 64 * slot;
-      const float* old = a.msg_in + 64 * slot;
       const float v = scale ? o[own] / sum : o[own];
-      dst[lane + 32 * own] = v;
+      const int e = 64 * slot + lane + 32 * own;
+      if (!PERSIST || last) {
+        a.msg_out[e] = v;
+      } else {
+        st_tagged(a.tagged + (size_t)((t + 1) & 3) * a.tagged_stride + e, v, sweep_tag(epoch, t + 1));
+      }
       // the convergence diff needs all 64 entries: the even warp of each leg computes it
       if (a.slot_diff && own == 0) {
+        const float* old = a.msg_in + 64 * slot;
         double n1 = 0, n2 = 0, dd = 0;
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
@@ -426,7 +519,10 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
         }
       }
     }
-    __syncthreads();
+    // msg / outs / part are next written after at least two more group barriers, so the
+    // next item starts without one here
+    item = item2;
+    t = t2;
   }
   if (!ok && tid == 0) {
     // a wait gave up: let the copy / MMAs already issued finish (bounded) before the
@@ -437,11 +533,20 @@ __global__ void __launch_bounds__(kThreads, SPLIT ? 4 : 8) bp_tc_kernel(TcArgs a
   if (skip && first && tid == 0) ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);  // unused image copy
   ptx::tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (threadIdx.x < 32) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, kTmemCols);
+    ptx::tmem_dealloc(*taddr_s, kTmemCols * GROUPS);
   }
-  if (a.conv && !skip) conv_finish_cta(a.conv);
+  if (PERSIST && threadIdx.x == 0) {
+    // the last CTA to finish advances the epoch, so the next launch's tags differ
+    __threadfence();
+    if (atomicAdd(&a.epoch[1], 1u) == gridDim.x - 1) {
+      a.epoch[1] = 0;
+      a.epoch[0] = (epoch + 1) & 0xFFFFFu ? (epoch + 1) & 0xFFFFFu : 1u;
+      __threadfence();
+    }
+  }
+  if (a.conv && !skip) conv_finish_cta(a.conv, nsweeps);
 }
 
 // ---- operand image: per vertex [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ the same for lo] ---------
@@ -624,8 +729,12 @@ struct TcEngine {
   unsigned char* image = nullptr;  // per vertex [A_pq hi | A_qp hi | A_pq lo | A_qp lo]
   size_t image_bytes = 0;
   int* d_err = nullptr;
+  unsigned long long* d_tagged = nullptr;  // persistent kernel: 4 buffers of tagged entries
+  size_t tagged_stride = 0;
+  unsigned* d_epoch = nullptr;
   int sm_count = 0;
   int occ[2] = {0, 0};
+  bool persist_ok[2] = {false, false};  // cooperative grid of sm_count CTAs fits
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -634,6 +743,8 @@ void tc_destroy(TcEngine* e) {
   if (!e) return;
   if (e->image) cudaFree(e->image);
   if (e->d_err) cudaFree(e->d_err);
+  if (e->d_tagged) cudaFree(e->d_tagged);
+  if (e->d_epoch) cudaFree(e->d_epoch);
   delete e;
 }
 
@@ -696,30 +807,57 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   if (err != cudaSuccess) return err;
   constexpr TcSmem L0 = tc_smem<false>();
   constexpr TcSmem L1 = tc_smem<true>();
-  cudaFuncSetAttribute(bp_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L0.total);
-  cudaFuncSetAttribute(bp_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L1.total);
-  cudaFuncSetAttribute(bp_tc_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  cudaFuncSetAttribute(bp_tc_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  const void* k1[2] = {(const void*)bp_tc_kernel<false, 1, false>, (const void*)bp_tc_kernel<true, 1, false>};
+  const void* kp[2] = {(const void*)bp_tc_kernel<false, kGroupsBf16, true>,
+                       (const void*)bp_tc_kernel<true, kGroupsSplit, true>};
+  const uint32_t tot[2] = {L0.total, L1.total};
+  const uint32_t ptot[2] = {kGroupsBf16 * L0.stride, kGroupsSplit * L1.stride};
+  for (int k = 0; k < 2; ++k) {
+    cudaFuncSetAttribute(k1[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tot[k]);
+    cudaFuncSetAttribute(k1[k], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(kp[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ptot[k]);
+    cudaFuncSetAttribute(kp[k], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  }
   // Resident CTAs per SM from the kernel's own resources: shared memory (plus the
   // 1 KB the runtime reserves per CTA), registers and TMEM columns (512 per SM).
   int smem_sm = 0, regs_sm = 0;
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-  int api_occ[2] = {0, 0};
-  cudaError_t oe0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&api_occ[0], bp_tc_kernel<false>, kThreads, L0.total);
-  cudaError_t oe1 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&api_occ[1], bp_tc_kernel<true>, kThreads, L1.total);
-  cudaGetLastError();
-  const uint32_t tot[2] = {L0.total, L1.total};
   for (int k = 0; k < 2; ++k) {
     cudaFuncAttributes fa;
-    cudaFuncGetAttributes(&fa, k ? (const void*)bp_tc_kernel<true> : (const void*)bp_tc_kernel<false>);
+    cudaFuncGetAttributes(&fa, k1[k]);
     const int by_smem = smem_sm / (int)(tot[k] + 1024);
     const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 4;
     e->occ[k] = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTmemCols));
+    // the cooperative launch needs one resident CTA per SM
+    int per_sm = 0;
+    const int groups = k ? kGroupsSplit : kGroupsBf16;
+    cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp[k], kThreads * groups, ptot[k]);
+    e->persist_ok[k] = oe == cudaSuccess && per_sm >= 1;
   }
+  cudaGetLastError();
   if (getenv("ITN_DEBUG"))
-    fprintf(stderr, "[itn] tc residency: bf16 %d (smem %u B, api %d/%d), split %d (smem %u B, api %d/%d), sms %d\n",
-            e->occ[0], L0.total, api_occ[0], (int)oe0, e->occ[1], L1.total, api_occ[1], (int)oe1, e->sm_count);
+    fprintf(stderr, "[itn] tc residency: bf16 %d (smem %u B), split %d (smem %u B), persistent %d/%d, sms %d\n",
+            e->occ[0], L0.total, e->occ[1], L1.total, (int)e->persist_ok[0], (int)e->persist_ok[1], e->sm_count);
+  // tagged message buffers of the persistent kernel, zeroed once (epochs start at 1)
+  const size_t stride = (size_t)std::max<int64_t>(nv, 1) * 4 * 64;
+  if (e->tagged_stride < stride) {
+    if (e->d_tagged) cudaFree(e->d_tagged);
+    e->d_tagged = nullptr;
+    e->tagged_stride = 0;
+    err = cudaMalloc(&e->d_tagged, 4 * stride * sizeof(unsigned long long));
+    if (err != cudaSuccess) return err;
+    err = cudaMemsetAsync(e->d_tagged, 0, 4 * stride * sizeof(unsigned long long), st);
+    if (err != cudaSuccess) return err;
+    e->tagged_stride = stride;
+  }
+  if (!e->d_epoch) {
+    err = cudaMalloc(&e->d_epoch, 2 * sizeof(unsigned));
+    if (err != cudaSuccess) return err;
+    const unsigned init[2] = {1u, 0u};
+    err = cudaMemcpyAsync(e->d_epoch, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    if (err != cudaSuccess) return err;
+  }
   e->nv = (int)nv;
   e->d_off = d_off;
   e->d_rev = d_rev;
@@ -729,8 +867,7 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   return cudaStreamSynchronize(st);
 }
 
-cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
-  if (!e || !e->valid) return cudaErrorInvalidValue;
+static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   TcArgs a;
   a.rev = e->d_rev;
   a.image = e->image;
@@ -741,16 +878,57 @@ cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
   a.slot_diff = r.slot_diff;
   a.conv = r.conv;
   a.err = e->d_err;
+  a.nsweeps = 1;
+  a.tagged = e->d_tagged;
+  a.tagged_stride = e->tagged_stride;
+  a.epoch = e->d_epoch;
+  return a;
+}
+
+cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
+  if (!e || !e->valid) return cudaErrorInvalidValue;
+  TcArgs a = tc_args(e, r);
   const int k = r.split ? 1 : 0;
   const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[k]));
   if (r.split) {
-    constexpr TcSmem L = tc_smem<true>();
-    bp_tc_kernel<true><<<grid, kThreads, L.total, st>>>(a);
+    bp_tc_kernel<true, 1, false><<<grid, kThreads, tc_smem<true>().total, st>>>(a);
   } else {
-    constexpr TcSmem L = tc_smem<false>();
-    bp_tc_kernel<false><<<grid, kThreads, L.total, st>>>(a);
+    bp_tc_kernel<false, 1, false><<<grid, kThreads, tc_smem<false>().total, st>>>(a);
   }
   return cudaGetLastError();
+}
+
+cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used) {
+  *used = false;
+  if (!e || !e->valid || r.slot_diff) return cudaErrorInvalidValue;
+  const int k = r.split ? 1 : 0;
+  // two sweeps would write the plain output buffer while the first sweep's readers of
+  // the same buffer may still be running; tags hold 12 bits of sweep index
+  if (!e->persist_ok[k] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
+  TcArgs a = tc_args(e, r);
+  a.nsweeps = nsweeps;
+  cudaError_t err = cudaSuccess;
+  const int groups = r.split ? kGroupsSplit : kGroupsBf16;
+  // never more groups than items, so every group has work in every sweep
+  const int grid = std::max(1, std::min(e->sm_count, (2 * e->nv + groups - 1) / groups));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kThreads * groups);
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (r.split) {
+    cfg.dynamicSmemBytes = kGroupsSplit * tc_smem<true>().stride;
+    err = cudaLaunchKernelEx(&cfg, bp_tc_kernel<true, kGroupsSplit, true>, a);
+  } else {
+    cfg.dynamicSmemBytes = kGroupsBf16 * tc_smem<false>().stride;
+    err = cudaLaunchKernelEx(&cfg, bp_tc_kernel<false, kGroupsBf16, true>, a);
+  }
+  if (err == cudaSuccess) *used = true;
+  return err;
 }
 
 int tc_error_flag(TcEngine* e, cudaStream_t st) {

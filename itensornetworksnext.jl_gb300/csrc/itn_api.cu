@@ -178,8 +178,9 @@ struct itn_ctx {
   // convergence state (device): dmax, nan, done, at, iters, delta, counter
   DevBuf d_slot_diff, d_state;
 
-  // cached solve graphs
+  // cached solve graphs and the number of kernel launches each holds
   std::map<std::string, cudaGraphExec_t> graphs;
+  std::map<std::string, int> graph_launches;
   // CTA size chosen by the autotuner for the parallel sweep, per dtype (0: not tuned)
   std::vector<int> tuned_block = std::vector<int>(4, 0);
 
@@ -857,6 +858,41 @@ int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
 int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const itn_bp_opts* o,
                     int* launches) {
   const bool use_tol = o->tol >= 0;
+  if (o->precision != ITN_PREC_NATIVE && !use_tol) {
+    // Without a convergence test the BF16 sweeps and then the split sweeps each run as
+    // one persistent launch; a device that cannot host the cooperative grid gets one
+    // launch per sweep.
+    const int nsplit = std::min(nsweeps, std::max(0, o->split_sweeps));
+    int t = 0;
+    for (int part = 0; part < 2; ++part) {
+      const int n = part ? nsplit : nsweeps - nsplit;
+      if (n == 0) continue;
+      TcRun tr;
+      tr.msg_in = c->d_msg[(start + t) & 1].p;
+      tr.msg_out = c->d_msg[(start + t + n) & 1].p;
+      tr.precision = o->precision;
+      tr.split = part == 1;
+      tr.normalize = o->normalize;
+      tr.slot_diff = nullptr;
+      tr.conv = conv(c);
+      bool used = false;
+      cudaError_t e = tc_sweeps_persistent(c->tc, tr, n, c->stream, &used);
+      if (e != cudaSuccess) return cuda_fail(c, e, "persistent tensor-core sweeps");
+      if (used) {
+        *launches += 1;
+      } else {
+        for (int k = 0; k < n; ++k) {
+          tr.msg_in = c->d_msg[(start + t + k) & 1].p;
+          tr.msg_out = c->d_msg[((start + t + k) & 1) ^ 1].p;
+          e = tc_sweep(c->tc, tr, c->stream);
+          if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
+          *launches += 1;
+        }
+      }
+      t += n;
+    }
+    return ITN_OK;
+  }
   for (int t = 0; t < nsweeps; ++t) {
     const int in = (start + t) & 1, out = in ^ 1;
     const int prec = o->precision;
@@ -1013,6 +1049,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     int rec_launches = 0;
     if (it != c->graphs.end()) {
       exec = it->second;
+      rec_launches = c->graph_launches[key];
     } else {
       cudaGraph_t graph;
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1027,6 +1064,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
       cudaGraphDestroy(graph);
       if (ce != cudaSuccess) return cuda_fail(c, ce, "graph instantiate");
       c->graphs[key] = exec;
+      c->graph_launches[key] = rec_launches;
     }
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(cudaGraphLaunch(exec, c->stream));
@@ -1036,9 +1074,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     total_ms += ms;
-    // every recorded sweep is 2 launches (parallel) -- count what the graph holds
-    launches += (o->schedule == ITN_SCHED_PARALLEL) ? n
-                : (int)(n * ((plan.level_off.size() - 1) + (use_tol ? 3 : 1)));
+    launches += rec_launches;
     issued += n;
     if (hs.done) break;
   }

@@ -48,16 +48,17 @@ __device__ __forceinline__ void conv_step(ConvState* s) {
 }
 
 // Called by every CTA of a sweep kernel after its last global write (all threads);
-// the last CTA performs conv_step.  Threads that issued diff atomics must have
-// executed __threadfence() before reaching this call.
-__device__ __forceinline__ void conv_finish_cta(ConvState* s) {
+// the last CTA performs conv_step (`steps` times for a kernel that ran several sweeps
+// without a convergence test).  Threads that issued diff atomics must have executed
+// __threadfence() before reaching this call.
+__device__ __forceinline__ void conv_finish_cta(ConvState* s, int steps = 1) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned t = atomicAdd(&s->tickets, 1u);
     if (t == gridDim.x - 1) {
       __threadfence();
-      conv_step(s);
+      for (int k = 0; k < steps; ++k) conv_step(s);
       s->tickets = 0;
       __threadfence();
     }

@@ -30,6 +30,12 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
                        int precision, cudaStream_t st, const char** why);
 // Enqueue one sweep (all directed messages) on the stream.
 cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st);
+// Enqueue `nsweeps` sweeps as one cooperative launch (one CTA per SM, independent 4-warp
+// groups; intermediate messages travel through tagged device buffers): reads r.msg_in,
+// writes r.msg_out (the two may be the same buffer).  Needs r.slot_diff == null (no
+// convergence test inside).  *used = false (and nothing enqueued) when the device cannot
+// host the cooperative grid, or for nsweeps == 2 or > 4095.
+cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used);
 // Non-zero when a bounded wait inside the tensor-core kernel gave up.
 int tc_error_flag(TcEngine* e, cudaStream_t st);
 // One-CTA tcgen05 self-test (cached per process): M=128 product exact, M=64

@@ -115,3 +115,26 @@ def test_tc_rejects_unsupported_network():
         with pytest.raises(ItnError) as ei:
             e.run(maxiter=2, precision="bf16")
         assert ei.value.status == 6
+
+
+@pytest.mark.parametrize("L,n,split", [(32, 7, 0), (32, 6, 2), (4, 5, 1)])
+def test_persistent_matches_per_sweep_launches(L, n, split):
+    """Without a convergence test the sweeps run as one cooperative launch per precision
+    part (per-item completion counters instead of kernel boundaries); with one the engine
+    launches once per sweep.  Both run the same per-item arithmetic, so the messages must
+    agree bit for bit -- a missed dependency would read a stale or half-written message.
+    32x32 has more half-vertex items (2048) than groups, 4x4 fewer."""
+    g, t = _lattice(L, 11)
+    rng = np.random.default_rng(12)
+    m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
+    with BPEngine(g) as e:
+        e.set_tensors(t.astype(np.float32))
+        e.set_messages(m0)
+        r1 = e.run(maxiter=n, precision="bf16", split_sweeps=split)
+        a = e.messages()
+        e.set_messages(m0)
+        r2 = e.run(maxiter=n, tol=1e-300, precision="bf16", split_sweeps=split)
+        b = e.messages()
+    assert r1.iterations == n and r2.iterations == n
+    assert r1.kernel_launches < r2.kernel_launches
+    np.testing.assert_array_equal(a, b)
