@@ -171,6 +171,50 @@ int32_t itn_contract_network(itn_ctx *ctx, int32_t dtype, int32_t n_tensors, con
                              int64_t out_capacity, int32_t *out_rank, int64_t *out_labels,
                              int64_t *out_dims, double *device_ms);
 
+/* BP simple-update gate application, apply_gate_bp! (src/apply/apply_operators.jl:209-283),
+ * for a batch of independent gates (e.g. one Trotter layer of gates on disjoint sites), one
+ * CTA per gate, FP64 (complex128 for complex dtypes) arithmetic on the device.
+ *
+ * A site tensor is a row-major array with axes [other legs..., site index, shared bond];
+ * a one-site gate has no shared-bond axis.  The other legs are gauged with X_e,
+ * X_e^H X_e = env[e] (the D x D environment message M[bra][ket] of the edge pointing into
+ * the site), which the reference obtains from gram_eigh_full(_with_pinv); env_off < 0
+ * means no gauge on that leg.  Two-site gate: gauge, split each site into an isometry
+ * and R (Gram eigendecomposition; the reference uses qr_compact), apply op[s1',s2',s1,s2]
+ * to R1*R2, truncated SVD (the reference's svd_trunc; here from the Hermitian
+ * eigendecomposition of theta theta^H, directions with sigma <= 1e-7 sigma_max dropped),
+ * keep at most max_rank (> 0) values above cutoff (> 0), optionally divide S by its norm,
+ * absorb sqrt(S) on both sides, undo the gauges.  The new sites have axes
+ * [other legs..., site index, new bond]; out_bond[g] receives the new bond dimension chi
+ * and out_s (from s_off) its singular values, which are the new environment diag(S) of
+ * the bond in both directions.  One-site gate: op[s'][s] applied on the site index,
+ * divided by the gauged norm when normalize.
+ *
+ * out_off[i] must leave room for prod(leg_dim) * d * chi_cap entries, chi_cap =
+ * min(d1 * min(P1, d1 * bond), d2 * min(P2, d2 * bond)) with P_i the product of the other
+ * leg dims of site i; s_off room for chi_cap values.  Limits: d <= 16, at most 6 other
+ * legs of dimension <= 64 each, d * bond <= 128 and d * d * bond <= 128.  sites/envs/ops/
+ * out_sites are host arrays of `dtype`; device_ms (may be NULL) receives the kernel time. */
+typedef struct {
+  int32_t nsite;          /* 1 or 2 */
+  int32_t d[2];           /* site index dimension of each site */
+  int32_t nleg[2];        /* number of other (gauged) legs of each site, <= 6 */
+  int32_t bond;           /* dimension of the bond joining the two sites (2-site gates) */
+  int32_t leg_dim[2][6];  /* dimensions of the other legs */
+  int64_t site_off[2];    /* element offsets of the input sites in `sites` */
+  int64_t env_off[2][6];  /* element offsets of each other leg's D x D message in `envs` (< 0: none) */
+  int64_t op_off;         /* element offset of the operator in `ops` */
+  int64_t out_off[2];     /* element offsets of the output sites in `out_sites` */
+  int64_t s_off;          /* offset of the singular values in `out_s` */
+} itn_gate_desc;
+
+int32_t itn_apply_gates(itn_ctx *ctx, int32_t dtype, int64_t n_gates, const itn_gate_desc *gates,
+                        const void *sites, int64_t n_site_elems, const void *envs,
+                        int64_t n_env_elems, const void *ops, int64_t n_op_elems,
+                        int32_t max_rank, double cutoff, int32_t normalize, void *out_sites,
+                        int64_t out_capacity, double *out_s, int64_t s_capacity,
+                        int32_t *out_bond, double *device_ms);
+
 /* Gradient of the Bethe log-norm (bethe_free_energy, messagecache.jl:185-201) with
  * respect to every site tensor, for the converged messages currently held.  No
  * counterpart in the reference (it has no AD); this is the backward rule the Julia

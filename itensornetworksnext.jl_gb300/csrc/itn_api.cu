@@ -25,6 +25,7 @@
 #include "itn_internal.h"
 #include "itn_tc.h"
 #include "itn_contract.h"
+#include "itn_apply.h"
 
 using namespace itn;
 
@@ -1422,6 +1423,153 @@ int read_network(itn_ctx* c, int32_t n, const int32_t* ranks, const int64_t* lab
 }  // namespace
 
 extern "C" {
+
+// ---- gate application (apply_gate_bp!, src/apply/apply_operators.jl:209-283) ---------------
+namespace {
+// host array of `dtype` -> FP64 / complex128 copy (complex data keeps (re, im) pairs)
+std::vector<double> to_f64(const void* src, int64_t n, int32_t dtype) {
+  const bool cx = dtype == ITN_C64 || dtype == ITN_C128;
+  std::vector<double> out((size_t)n * (cx ? 2 : 1));
+  const size_t m = out.size();
+  if (!src) return out;
+  if (dtype == ITN_F32 || dtype == ITN_C64) {
+    const float* f = static_cast<const float*>(src);
+    for (size_t k = 0; k < m; ++k) out[k] = f[k];
+  } else {
+    memcpy(out.data(), src, m * sizeof(double));
+  }
+  return out;
+}
+void from_f64(const std::vector<double>& v, void* dst, int32_t dtype) {
+  if (dtype == ITN_F32 || dtype == ITN_C64) {
+    float* f = static_cast<float*>(dst);
+    for (size_t k = 0; k < v.size(); ++k) f[k] = (float)v[k];
+  } else {
+    memcpy(dst, v.data(), v.size() * sizeof(double));
+  }
+}
+}  // namespace
+
+int32_t itn_apply_gates(itn_ctx* c, int32_t dtype, int64_t n_gates, const itn_gate_desc* gates, const void* sites,
+                        int64_t n_site_elems, const void* envs, int64_t n_env_elems, const void* ops,
+                        int64_t n_op_elems, int32_t max_rank, double cutoff, int32_t normalize, void* out_sites,
+                        int64_t out_capacity, double* out_s, int64_t s_capacity, int32_t* out_bond,
+                        double* device_ms) {
+  if (!c) return ITN_ERR_ARG;
+  if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
+  if (n_gates < 0) return fail(c, ITN_ERR_ARG, "negative gate count");
+  if (n_gates == 0) {
+    if (device_ms) *device_ms = 0;
+    return ITN_OK;
+  }
+  if (!gates || !sites || !ops || !out_sites || !out_bond) return fail(c, ITN_ERR_ARG, "null pointer");
+  if (n_gates > (1 << 20)) return fail(c, ITN_ERR_ARG, "too many gates in one batch");
+  std::vector<GateJob> jobs((size_t)n_gates);
+  int64_t ws_total = 0;
+  for (int64_t g = 0; g < n_gates; ++g) {
+    const itn_gate_desc& G = gates[g];
+    GateJob& J = jobs[(size_t)g];
+    memset(&J, 0, sizeof(J));
+    if (G.nsite != 1 && G.nsite != 2) return fail(c, ITN_ERR_ARG, "gate %lld: nsite must be 1 or 2", (long long)g);
+    J.nsite = G.nsite;
+    J.bond = G.nsite == 2 ? G.bond : 1;
+    if (J.bond < 1 || J.bond > 128) return fail(c, ITN_ERR_ARG, "gate %lld: bond dimension %d", (long long)g, G.bond);
+    int64_t P[2] = {1, 1};
+    for (int i = 0; i < G.nsite; ++i) {
+      if (G.d[i] < 1 || G.d[i] > 16) return fail(c, ITN_ERR_UNSUPPORTED, "gate %lld: site dimension %d (max 16)", (long long)g, G.d[i]);
+      if (G.nleg[i] < 0 || G.nleg[i] > kGateMaxLegs)
+        return fail(c, ITN_ERR_UNSUPPORTED, "gate %lld: %d other legs (max %d)", (long long)g, G.nleg[i], kGateMaxLegs);
+      J.d[i] = G.d[i];
+      J.nleg[i] = G.nleg[i];
+      for (int j = 0; j < G.nleg[i]; ++j) {
+        const int D = G.leg_dim[i][j];
+        if (D < 1 || D > 64) return fail(c, ITN_ERR_UNSUPPORTED, "gate %lld: leg dimension %d (max 64)", (long long)g, D);
+        J.leg_dim[i][j] = D;
+        P[i] *= D;
+        if (P[i] > (1 << 22)) return fail(c, ITN_ERR_UNSUPPORTED, "gate %lld: site tensor too large", (long long)g);
+        J.env_off[i][j] = G.env_off[i][j];
+        if (G.env_off[i][j] >= 0) {
+          if (!envs || G.env_off[i][j] + (int64_t)D * D > n_env_elems)
+            return fail(c, ITN_ERR_ARG, "gate %lld: environment %d of site %d out of range", (long long)g, j, i);
+        }
+      }
+      const int64_t size = P[i] * G.d[i] * J.bond;
+      if (G.site_off[i] < 0 || G.site_off[i] + size > n_site_elems)
+        return fail(c, ITN_ERR_ARG, "gate %lld: site %d out of range", (long long)g, i);
+      J.site_off[i] = G.site_off[i];
+    }
+    int64_t opn = G.nsite == 2 ? (int64_t)G.d[0] * G.d[1] * G.d[0] * G.d[1] : (int64_t)G.d[0] * G.d[0];
+    if (G.op_off < 0 || G.op_off + opn > n_op_elems) return fail(c, ITN_ERR_ARG, "gate %lld: operator out of range", (long long)g);
+    J.op_off = G.op_off;
+    if (G.nsite == 2) {
+      const int64_t n0 = (int64_t)G.d[0] * J.bond, n1 = (int64_t)G.d[1] * J.bond;
+      const int64_t mcap = G.d[0] * std::min(P[0], n0), ncap = G.d[1] * std::min(P[1], n1);
+      if (n0 > 128 || n1 > 128 || mcap > 128 || ncap > 128)
+        return fail(c, ITN_ERR_UNSUPPORTED, "gate %lld: d * bond and d * d * bond must be <= 128", (long long)g);
+      J.chi_cap = (int)std::min(mcap, ncap);
+      if (!out_s || G.s_off < 0 || G.s_off + J.chi_cap > s_capacity)
+        return fail(c, ITN_ERR_ARG, "gate %lld: singular values out of range", (long long)g);
+      J.s_off = G.s_off;
+    } else {
+      J.chi_cap = 1;
+    }
+    for (int i = 0; i < G.nsite; ++i) {
+      const int64_t need = P[i] * G.d[i] * (G.nsite == 2 ? J.chi_cap : 1);
+      if (G.out_off[i] < 0 || G.out_off[i] + need > out_capacity)
+        return fail(c, ITN_ERR_ARG, "gate %lld: output site %d out of range", (long long)g, i);
+      J.out_off[i] = G.out_off[i];
+    }
+    J.ws = ws_total;
+    ws_total += gate_workspace(J);
+  }
+  if (int r = ensure_device(c)) return r;
+  const bool cx = dtype == ITN_C64 || dtype == ITN_C128;
+  const size_t esz = cx ? 16 : 8;
+  std::vector<double> h_sites = to_f64(sites, n_site_elems, dtype);
+  std::vector<double> h_envs = to_f64(envs, envs ? n_env_elems : 0, dtype);
+  std::vector<double> h_ops = to_f64(ops, n_op_elems, dtype);
+  struct Buf {
+    void* p = nullptr;
+    cudaStream_t st;
+    ~Buf() { if (p) cudaFreeAsync(p, st); }
+  } b_jobs, b_sites, b_envs, b_ops, b_out, b_s, b_bond, b_ws;
+  Buf* all[] = {&b_jobs, &b_sites, &b_envs, &b_ops, &b_out, &b_s, &b_bond, &b_ws};
+  const size_t sizes[] = {jobs.size() * sizeof(GateJob), h_sites.size() * 8, std::max<size_t>(h_envs.size() * 8, 16),
+                          h_ops.size() * 8, (size_t)out_capacity * esz, (size_t)std::max<int64_t>(s_capacity, 1) * 8,
+                          jobs.size() * sizeof(int), (size_t)ws_total * esz};
+  for (int k = 0; k < 8; ++k) {
+    all[k]->st = c->stream;
+    cudaError_t e = cudaMallocAsync(&all[k]->p, std::max<size_t>(sizes[k], 16), c->stream);
+    if (e != cudaSuccess) {
+      all[k]->p = nullptr;
+      return e == cudaErrorMemoryAllocation ? fail(c, ITN_ERR_OOM, "apply_gates: %zu bytes", sizes[k])
+                                            : cuda_fail(c, e, "apply_gates allocation");
+    }
+  }
+  CK(cudaMemcpyAsync(b_jobs.p, jobs.data(), sizes[0], cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(b_sites.p, h_sites.data(), sizes[1], cudaMemcpyHostToDevice, c->stream));
+  if (!h_envs.empty()) CK(cudaMemcpyAsync(b_envs.p, h_envs.data(), h_envs.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(b_ops.p, h_ops.data(), sizes[3], cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(b_out.p, 0, sizes[4], c->stream));
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(launch_gates(cx, (int)n_gates, static_cast<const GateJob*>(b_jobs.p), b_sites.p, b_envs.p, b_ops.p, b_out.p,
+                  static_cast<double*>(b_s.p), static_cast<int*>(b_bond.p), b_ws.p, max_rank, cutoff, normalize,
+                  c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  std::vector<double> h_out((size_t)out_capacity * (cx ? 2 : 1));
+  std::vector<int> h_bond(jobs.size());
+  CK(cudaMemcpyAsync(h_out.data(), b_out.p, sizes[4], cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(h_bond.data(), b_bond.p, sizes[6], cudaMemcpyDeviceToHost, c->stream));
+  if (out_s && s_capacity > 0)
+    CK(cudaMemcpyAsync(out_s, b_s.p, (size_t)s_capacity * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (device_ms) *device_ms = ms;
+  from_f64(h_out, out_sites, dtype);
+  for (size_t g = 0; g < jobs.size(); ++g) out_bond[g] = h_bond[g];
+  return ITN_OK;
+}
 
 int32_t itn_contraction_order(int32_t n, const int32_t* ranks, const int64_t* labels, const int64_t* dims,
                               int32_t alg, int32_t* steps_out) {

@@ -33,7 +33,16 @@ EXPORTED = [
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
     "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest", "itn_bp_grad",
     "itn_sweep_vjp", "itn_logz_static_scratch", "itn_contraction_order", "itn_contract_network",
+    "itn_apply_gates",
 ]
+
+
+class GateDesc(ctypes.Structure):
+    """itn_gate_desc (include/itn_gpu.h)."""
+    _fields_ = [("nsite", ctypes.c_int32), ("d", ctypes.c_int32 * 2), ("nleg", ctypes.c_int32 * 2),
+                ("bond", ctypes.c_int32), ("leg_dim", (ctypes.c_int32 * 6) * 2),
+                ("site_off", ctypes.c_int64 * 2), ("env_off", (ctypes.c_int64 * 6) * 2),
+                ("op_off", ctypes.c_int64), ("out_off", ctypes.c_int64 * 2), ("s_off", ctypes.c_int64)]
 
 
 class ItnError(RuntimeError):
@@ -106,6 +115,9 @@ def _declare(lib):
                                         ctypes.POINTER(_I32), _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logz_static_scratch": (_I32, [_I32, _VP, _I32, _I32, _I64, _I64, _I64, _VP, _VP, _VP, _VP,
                                            _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_char_p, _I32]),
+        "itn_apply_gates": (_I32, [_VP, _I32, _I64, _VP, _VP, _I64, _VP, _I64, _VP, _I64, _I32,
+                                   ctypes.c_double, _I32, _VP, _I64, _VP, _I64, _VP,
+                                   ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

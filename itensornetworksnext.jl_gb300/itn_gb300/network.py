@@ -558,3 +558,184 @@ def contract_network(tn, alg=None):
         for i in t.inds:
             dims[i.name] = i.dim
     return ITensor(data, [Index(dims[n], n) for n in labels])
+
+
+# ---- gate application (src/apply/apply_operators.jl) -------------------------------------------
+class Operator(ITensor):
+    """A named operator (ITensorBase ``operator(data, codomain, domain)``): data with axes
+    (codomain..., domain...); applying it contracts the domain names with a tensor and
+    renames the codomain back to the domain names."""
+
+    def __init__(self, data, codomain_inds, domain_inds):
+        super().__init__(data, list(codomain_inds) + list(domain_inds))
+        self.codomain = tuple(i.name for i in codomain_inds)
+        self.domain = tuple(i.name for i in domain_inds)
+
+
+def operator(data, codomain_inds, domain_inds):
+    return Operator(data, codomain_inds, domain_inds)
+
+
+@dataclass
+class BPApplyGate:
+    """Default single-operator strategy (apply_operators.jl:190-224): BP simple update.
+    ``trunc`` = max rank (int), (max_rank, cutoff) or None; ``normalize`` rescales
+    (the singular values of a two-site gate to unit norm, a one-site result to unit
+    gauged norm)."""
+    trunc: object = None
+    normalize: bool = False
+
+
+def _trunc_args(trunc):
+    if trunc is None:
+        return None, None
+    if isinstance(trunc, (tuple, list)):
+        return trunc[0], trunc[1]
+    return int(trunc), None
+
+
+def _env_matrix(env: MessageCache, edge, ket_names):
+    """The D x D matrix M[bra, ket] of env[edge], ket axes in the order of ket_names."""
+    t = env[edge]
+    k = len(t.inds) // 2
+    bra, ket = list(t.dimnames[:k]), list(t.dimnames[k:])
+    if set(ket) != set(ket_names):
+        # the bra names may come first or second: find the half that holds the link names
+        bra, ket = ket, bra
+        if set(ket) != set(ket_names):
+            raise ItnArgumentError(1, f"environment of {edge} does not carry the link names")
+    pair = {kn: bn for kn, bn in zip(ket, bra)}
+    order = [pair[n] for n in ket_names] + list(ket_names)
+    arr = t.permute(order)
+    D = int(np.prod([_dim_of(t, n) for n in ket_names]))
+    return arr.reshape(D, D)
+
+
+def _gate_site(state: ITensorNetwork, v, domain, partner, env):
+    """Site array [other legs..., s(, b)] of vertex v for a gate with the given domain names,
+    the names of each axis group and the environments of the gauged legs."""
+    t = state[v]
+    groups, envs = [], []
+    for w in state.neighbors(v):
+        if w == partner:
+            continue
+        names = state.linknames(v, w)
+        groups.append(names)
+        envs.append(_env_matrix(env, (w, v), names) if env is not None and (w, v) in env.keys() else None)
+    extra = [n for n in state.sitenames(v) if n not in domain]
+    for n in extra:
+        groups.append([n])
+        envs.append(None)
+    mine = [n for n in domain if n in t.dimnames]
+    bond = state.linknames(v, partner) if partner is not None else []
+    order = [n for g in groups for n in g] + mine + bond
+    shape = [int(np.prod([_dim_of(t, n) for n in g])) for g in groups]
+    shape += [int(np.prod([_dim_of(t, n) for n in mine]))]
+    if partner is not None:
+        shape += [int(np.prod([_dim_of(t, n) for n in bond]))]
+    return t.permute(order).reshape(shape), groups, mine, envs
+
+
+def _op_matrix(op: Operator, domains):
+    """op as [s1', (s2',) s1, (s2)] with each s the fused names of one site's domain part."""
+    cod_of = dict(zip(op.domain, op.codomain))
+    order = [cod_of[n] for d in domains for n in d] + [n for d in domains for n in d]
+    arr = op.permute(order)
+    dims = [int(np.prod([_dim_of(op, n) for n in d])) for d in domains]
+    return arr.reshape(dims + dims)
+
+
+def _gate_vertices(op: Operator, state: ITensorNetwork):
+    vs = [v for v in state.vertices() if set(op.domain) & set(state.sitenames(v))]
+    if not vs:
+        raise ItnArgumentError(1, "operator shares no indices with the tensor network")
+    if len(vs) > 2:
+        raise ItnArgumentError(1, f"{len(vs)}-site gate decomposition not implemented")
+    return vs
+
+
+def _gate_of(op: Operator, state: ITensorNetwork, env: MessageCache):
+    from .apply import Gate
+    vs = _gate_vertices(op, state)
+    if len(vs) == 1:
+        v = vs[0]
+        psi, groups, mine, envs = _gate_site(state, v, op.domain, None, env)
+        return Gate([psi], [envs], _op_matrix(op, [mine]), extra=dict(vs=vs, groups=[groups], mine=[mine]))
+    v1, v2 = vs
+    if not state.linknames(v1, v2):
+        raise ItnArgumentError(1, "a two-site gate needs neighbouring vertices")
+    p1, g1, m1, e1 = _gate_site(state, v1, op.domain, v2, env)
+    p2, g2, m2, e2 = _gate_site(state, v2, op.domain, v1, env)
+    return Gate([p1, p2], [e1, e2], _op_matrix(op, [m1, m2]), extra=dict(vs=vs, groups=[g1, g2], mine=[m1, m2]))
+
+
+def _finish(state: ITensorNetwork, env: MessageCache, gate, result):
+    dest = dict(state.tensors)
+    env2 = env.copy() if env is not None else MessageCache({})
+    vs = gate.extra["vs"]
+    if len(vs) == 1:
+        v = vs[0]
+        t = state[v]
+        groups, mine = gate.extra["groups"][0], gate.extra["mine"][0]
+        names = [n for g in groups for n in g] + mine
+        arr = result.reshape([_dim_of(t, n) for n in names])
+        dest[v] = ITensor(arr, [Index(_dim_of(t, n), n) for n in names])
+        return ITensorNetwork(dest), env2
+    n1, n2, S = result
+    chi = len(S)
+    bond = Index(chi, uniquename())
+    for i, (v, arr) in enumerate(zip(vs, (n1, n2))):
+        t = state[v]
+        groups, mine = gate.extra["groups"][i], gate.extra["mine"][i]
+        names = [n for g in groups for n in g] + mine
+        a = arr.reshape([_dim_of(t, n) for n in names] + [chi])
+        dest[v] = ITensor(a, [Index(_dim_of(t, n), n) for n in names] + [bond])
+    v1, v2 = vs
+    dt = np.result_type(n1.dtype, np.float64) if n1.dtype.kind != "c" else n1.dtype
+    diag = np.diag(S).astype(dt)
+    env2[(v1, v2)] = ITensor(diag, [Index(chi, uniquename()), bond])
+    env2[(v2, v1)] = ITensor(diag.copy(), [Index(chi, uniquename()), bond])
+    return ITensorNetwork(dest), env2
+
+
+def apply_operator(op: Operator, state: ITensorNetwork, env: MessageCache, *, alg=None, trunc=None,
+                   normalize=None, context=None):
+    """apply_operator(operator, state, env; alg, kwargs...) -> (state, env)
+    (apply_operators.jl:147-188, BP simple update :226-283), on the GPU."""
+    return apply_operators([op], state, env, alg=alg, trunc=trunc, normalize=normalize, context=context)
+
+
+def apply_operators(ops, state: ITensorNetwork, env: MessageCache, *, alg=None, trunc=None, normalize=None,
+                    context=None):
+    """apply_operators(operators, state, env; alg, kwargs...) -> (state, env)
+    (apply_operators.jl:14-120): the operators in turn, each updating the state and the
+    environment of its bond.  Consecutive operators on disjoint vertices are applied in
+    one GPU batch (the result is the same as one by one: each gate reads only its own
+    sites and the environments of edges into them; another gate changes only its own
+    sites and the environments of its own bond)."""
+    from .apply import apply_gates
+    alg = alg if alg is not None else BPApplyGate()
+    if trunc is not None:
+        alg = BPApplyGate(trunc=trunc, normalize=alg.normalize)
+    if normalize is not None:
+        alg = BPApplyGate(trunc=alg.trunc, normalize=bool(normalize))
+    max_rank, cutoff = _trunc_args(alg.trunc)
+    ops = list(ops)
+    if not ops:
+        return ITensorNetwork(dict(state.tensors)), (env.copy() if env is not None else None)
+    k = 0
+    while k < len(ops):
+        # the longest run of operators on pairwise disjoint vertices
+        batch, used = [], set()
+        while k < len(ops):
+            vs = _gate_vertices(ops[k], state)
+            touch = set(vs)
+            if batch and touch & used:
+                break
+            batch.append(_gate_of(ops[k], state, env))
+            used |= touch
+            k += 1
+        results = apply_gates(batch, max_rank=max_rank, cutoff=cutoff, normalize=alg.normalize, context=context)
+        for gate, res in zip(batch, results):
+            state, env = _finish(state, env, gate, res)
+    return state, env

@@ -78,3 +78,21 @@ def test_incoming_messages_exclude_reverse():
     assert N.incoming_messages(cache, (2, 3)) == [(1, 2)]
     assert N.incoming_messages(cache, (1, 2)) == []
     assert N.incoming_messages(cache, (2, 1)) == [(3, 2)]
+
+
+def test_apply_operator_argument_errors():
+    """apply_gate_bp! errors (src/apply/apply_operators.jl:214-227): an operator that shares
+    no index with the network, and one acting on more than two sites."""
+    from itn_gb300 import network as N
+    s = [N.Index(2) for _ in range(3)]
+    l01, l12 = N.Index(2), N.Index(2)
+    tn = N.ITensorNetwork({0: N.ITensor(np.ones((2, 2)), [s[0], l01]),
+                           1: N.ITensor(np.ones((2, 2, 2)), [l01, s[1], l12]),
+                           2: N.ITensor(np.ones((2, 2)), [l12, s[2]])})
+    other = N.Index(2)
+    op = N.operator(np.eye(2), [N.Index(2)], [other])
+    with pytest.raises(N.ItnArgumentError, match="shares no indices"):
+        N.apply_operator(op, tn, None)
+    op3 = N.operator(np.ones((2,) * 6), [N.Index(2) for _ in range(3)], s)
+    with pytest.raises(N.ItnArgumentError, match="3-site gate decomposition not implemented"):
+        N.apply_operator(op3, tn, None)
