@@ -370,6 +370,7 @@ def run_gpu(args):
         line["grad"] = bench_grad(device)
         line["batched"] = bench_batched(device)
         line["bp_16x16_D4"] = bench_16x16(device)
+        line["apply_layer_16x16_D4"] = bench_apply_layer(device)
     print(json.dumps(line))
     eng.close()
     return 0
@@ -485,6 +486,67 @@ def bench_16x16(device):
     z, _, ms = contract_network(ts, ls, return_time=True)
     out["exact_6x6_D3"] = {"logz_exact": float(np.log(z[()])), "logz_bp": lz_bp,
                            "bp_abs_err": abs(lz_bp - float(np.log(z[()]))), "contract_ms": ms}
+    return out
+
+
+def bench_apply_layer(device):
+    """BP simple-update gate application (apply_operators.jl): one layer of 128 random
+    two-site gates on the horizontal bonds (even columns) of a 16x16 open PEPS, d=2, D=4,
+    environments from a converged FP64 BP solve, truncation to rank 4.  The whole layer is
+    one itn_apply_gates batch (one CTA per gate); the CPU leg applies the same gates with the
+    numpy restatement of the algorithm, one by one, on the host."""
+    from itn_gb300 import network as N
+    from itn_gb300.apply import apply_gates
+    L, D, d = 16, 4, 2
+    rng = np.random.default_rng(1616)
+    s = {(x, y): N.Index(d) for x in range(L) for y in range(L)}
+    h = {(x, y): N.Index(D) for x in range(L - 1) for y in range(L)}
+    v = {(x, y): N.Index(D) for x in range(L) for y in range(L - 1)}
+    tensors = {}
+    for x in range(L):
+        for y in range(L):
+            inds = [s[(x, y)]]
+            if x > 0:
+                inds.append(h[(x - 1, y)])
+            if x < L - 1:
+                inds.append(h[(x, y)])
+            if y > 0:
+                inds.append(v[(x, y - 1)])
+            if y < L - 1:
+                inds.append(v[(x, y)])
+            shape = [i.dim for i in inds]
+            tensors[(x, y)] = N.ITensor(rng.standard_normal(shape) / np.sqrt(d * D ** 4), inds)
+    tn = N.ITensorNetwork(tensors)
+    nn = N.NormNetwork(tn)
+    env = N.beliefpropagation(nn, N.message_environment("one", nn), stopping_criterion=dict(maxiter=200, tol=1e-10))
+    ops = []
+    for x in range(0, L - 1, 2):
+        for y in range(L):
+            cod = [N.Index(d), N.Index(d)]
+            ops.append(N.operator(rng.standard_normal((d, d, d, d)), cod, [s[(x, y)], s[(x + 1, y)]]))
+    gates = [N._gate_of(op, tn, env) for op in ops]
+    times = []
+    for _ in range(4):
+        t0 = time.perf_counter()
+        res, ms = apply_gates(gates, max_rank=D, return_time=True)
+        times.append((ms, time.perf_counter() - t0))
+    ms = min(t[0] for t in times[1:])
+    wall = min(t[1] for t in times[1:])
+    out = {"workload": "16x16 open PEPS d=2 D=4, 128 two-site gates (one layer), BP environments, trunc rank 4, FP64",
+           "gates": len(gates), "device_ms": ms, "gates_per_s_device": len(gates) / (ms * 1e-3),
+           "e2e_ms": wall * 1e3, "gates_per_s_e2e": len(gates) / wall,
+           "bond_dims": sorted(set(int(len(r[2])) for r in res))}
+    try:
+        sys.path.insert(0, ROOT)
+        from oracle import apply_oracle as AO
+        t0 = time.perf_counter()
+        for g in gates:
+            AO.apply_gate_2site(g.sites[0], g.sites[1], g.envs[0], g.envs[1], g.op, maxrank=D)
+        cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(gates) / cpu, "unit": "gates/s", "cores": 1, "kind": "port",
+                               "sample": "the same 128 gates, numpy restatement, one by one"}
+    except Exception as exc:  # the oracle is a checker; its absence does not void the GPU number
+        out["cpu_baseline"] = {"unavailable": str(exc)}
     return out
 
 

@@ -3,6 +3,7 @@
  * entry points fail with a status instead of aborting; with a GPU it runs a 2-vertex BP
  * solve and checks the log-norm against the closed form.  Prints "ok" on success. */
 #include <math.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -33,6 +34,13 @@ int main(int argc, char **argv) {
   int64_t clash_dims[6] = {2, 3, 5, 4, 4, 2}; /* index 1 with dims 3 and 5 */
   CHECK(itn_contraction_order(3, ranks, labels, clash_dims, 0, steps) == ITN_ERR_ARG,
         "dimension clash rejected");
+  /* the gate descriptor layout a ctypes / ccall binding mirrors */
+  CHECK(sizeof(itn_gate_desc) == 216 && offsetof(itn_gate_desc, site_off) == 72 &&
+            offsetof(itn_gate_desc, s_off) == 208,
+        "itn_gate_desc layout");
+  CHECK(itn_apply_gates(NULL, ITN_F64, 0, NULL, NULL, 0, NULL, 0, NULL, 0, 0, 0.0, 0, NULL, 0, NULL, 0, NULL,
+                        NULL) == ITN_ERR_ARG,
+        "apply_gates without a context");
   CHECK(itn_create(NULL, 0, 0) == ITN_ERR_ARG, "null out pointer");
   itn_ctx *ctx = NULL;
   const int32_t st = itn_create(&ctx, 0, 0);
@@ -59,6 +67,36 @@ int main(int argc, char **argv) {
   CHECK(itn_logscalars(ctx, NULL, NULL, NULL, NULL, tot, flags) == ITN_OK, itn_last_error(ctx));
   /* <psi|psi> = sum_{s,s'} (sum_k d(s,k) d(s',k))^2 = 2: BP is exact on a tree */
   CHECK(fabs(tot[0] - log(2.0)) < 1e-12, "log-norm of the two-site network");
+  /* an identity two-site gate on two sites without other legs (s = 2, bond 2) leaves the
+   * contracted pair unchanged */
+  {
+    double sites[8] = {0.3, -1.2, 0.7, 2.0, 1.1, 0.4, -0.5, 0.9}; /* psi1[s][b], psi2[s][b] */
+    double op[16] = {0};
+    for (int k = 0; k < 4; ++k) op[k * 5] = 1.0;
+    itn_gate_desc g = {0};
+    g.nsite = 2;
+    g.d[0] = g.d[1] = 2;
+    g.bond = 2;
+    g.site_off[0] = 0;
+    g.site_off[1] = 4;
+    g.op_off = 0;
+    g.out_off[0] = 0;
+    g.out_off[1] = 4; /* chi_cap = 2 * min(1, 4) = 2 */
+    g.s_off = 0;
+    double out[8], s[2];
+    int32_t chi = 0;
+    CHECK(itn_apply_gates(ctx, ITN_F64, 1, &g, sites, 8, NULL, 0, op, 16, 0, 0.0, 0, out, 8, s, 2, &chi, NULL) ==
+              ITN_OK,
+          itn_last_error(ctx));
+    CHECK(chi >= 1 && chi <= 2, "new bond dimension");
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 2; ++b) {
+        double want = 0, got = 0;
+        for (int k = 0; k < 2; ++k) want += sites[a * 2 + k] * sites[4 + b * 2 + k];
+        for (int k = 0; k < chi; ++k) got += out[a * chi + k] * out[4 + b * chi + k];
+        CHECK(fabs(got - want) < 1e-12, "identity gate keeps the pair");
+      }
+  }
   itn_destroy(ctx);
   printf("ok\n");
   return 0;

@@ -72,3 +72,14 @@ def test_missing_library_fails_loudly(tmp_path):
             L.load(str(tmp_path / "libitn_gpu.so"))
     finally:
         L._lib = saved
+
+
+def test_gate_descriptor_layout(lib_built):
+    """ctypes mirror of itn_gate_desc matches the C layout (216 bytes; the C client checks
+    the same numbers with sizeof / offsetof)."""
+    from itn_gb300 import _lib as L
+    assert ctypes.sizeof(L.GateDesc) == 216
+    assert L.GateDesc.site_off.offset == 72 and L.GateDesc.s_off.offset == 208
+    lib = L.load(lib_built)
+    assert lib.itn_apply_gates(None, 1, 0, None, None, 0, None, 0, None, 0, 0, 0.0, 0, None, 0, None, 0,
+                               None, None) == L.ITN_ERR_ARG

@@ -163,3 +163,30 @@ def test_apply_operators_applies_a_sequence(dtype):
     want = np.einsum("xyst,astb->axyb", g1.data, psi)
     want = np.einsum("xyst,abst->abxy", g2.data, want)
     assert _rel(_dense(gated, s), want) < _rtol(dtype)
+
+
+def test_rejects_bad_descriptors():
+    """Host-side validation of itn_apply_gates: arrays out of range -> ITN_ERR_ARG, shapes
+    beyond the kernel's limits -> ITN_ERR_UNSUPPORTED; nothing reaches the device."""
+    import ctypes
+    from itn_gb300 import _lib as L, ItnArgumentError, ItnError
+    from itn_gb300.contract import Context
+    rng = np.random.default_rng(13)
+    big = Gate([_randn(rng, (2, 70), np.float64), _randn(rng, (2, 70), np.float64)], [[], []],
+               _randn(rng, (2, 2, 2, 2), np.float64))
+    with pytest.raises(ItnError) as ei:
+        apply_gates([big])
+    assert ei.value.status == L.ITN_ERR_UNSUPPORTED
+    with Context() as ctx:
+        g = (L.GateDesc * 1)()
+        g[0].nsite, g[0].bond = 2, 2
+        g[0].d[0] = g[0].d[1] = 2
+        g[0].site_off[1] = 100                    # past the 8 site entries
+        g[0].out_off[1] = 4
+        sites, op = np.zeros(8), np.eye(4)
+        out, s, chi = np.zeros(8), np.zeros(2), np.zeros(1, dtype=np.int32)
+        st = ctx.lib.itn_apply_gates(ctx.ctx, L.F64, 1, g, L.ptr(sites), 8, None, 0, L.ptr(op), 16, 0, 0.0, 0,
+                                     L.ptr(out), 8, L.ptr(s), 2, L.ptr(chi), None)
+        assert st == L.ITN_ERR_ARG
+        with pytest.raises(ItnArgumentError, match="out of range"):
+            L.check(ctx.ctx, st)
