@@ -258,4 +258,46 @@ function ChainRulesCore.rrule(::typeof(bp_logz), nn::NormNetwork, messages; alg 
     return y, bp_logz_pullback
 end
 
+# ---- gate application (src/apply/apply_operators.jl:209-283) -------------------------------
+# Mirrors itn_gate_desc (216 bytes).  A BPApplyGate-compatible strategy permutes each site to
+# [other legs..., site index, shared bond] (column-major Julia arrays are passed reversed:
+# the C side reads row-major), packs env[e] as M[bra, ket] per other leg and the operator
+# as op[s1', s2', s1, s2], fills one descriptor per gate of a layer and calls
+# gpu_apply_gates! once for the whole layer.
+struct ItnGateDesc
+    nsite::Int32
+    d::NTuple{2,Int32}
+    nleg::NTuple{2,Int32}
+    bond::Int32
+    leg_dim::NTuple{2,NTuple{6,Int32}}
+    site_off::NTuple{2,Int64}
+    env_off::NTuple{2,NTuple{6,Int64}}
+    op_off::Int64
+    out_off::NTuple{2,Int64}
+    s_off::Int64
+end
+
+function gpu_apply_gates!(out::Vector{T}, svals::Vector{Float64}, chis::Vector{Int32},
+                          descs::Vector{ItnGateDesc}, sites::Vector{T}, envs::Vector{T},
+                          ops::Vector{T}; maxrank::Integer = 0, cutoff::Real = 0.0,
+                          normalize::Bool = false, device::Integer = 0) where {T}
+    ctx = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:itn_create, libitn), Int32, (Ptr{Ptr{Cvoid}}, Int32, Int32), ctx, device, 0)
+    st == ITN_OK || error("itn_create failed with status $st")
+    try
+        GC.@preserve out svals chis descs sites envs ops begin
+            check(ctx[], ccall((:itn_apply_gates, libitn), Int32,
+                (Ptr{Cvoid}, Int32, Int64, Ptr{ItnGateDesc}, Ptr{Cvoid}, Int64, Ptr{Cvoid}, Int64,
+                 Ptr{Cvoid}, Int64, Int32, Float64, Int32, Ptr{Cvoid}, Int64, Ptr{Float64}, Int64,
+                 Ptr{Int32}, Ptr{Float64}),
+                ctx[], eltype_code(T), length(descs), descs, sites, length(sites), envs, length(envs),
+                ops, length(ops), maxrank, cutoff, normalize, out, length(out), svals, length(svals),
+                chis, C_NULL))
+        end
+    finally
+        ccall((:itn_destroy, libitn), Int32, (Ptr{Cvoid},), ctx[])
+    end
+    return out, svals, chis
+end
+
 end # module
