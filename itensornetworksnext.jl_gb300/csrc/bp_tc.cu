@@ -45,8 +45,6 @@ constexpr int kTmemCols = 64;
 constexpr int kGroupsBf16 = 8;             // persistent kernel: 4-warp groups per CTA
 constexpr int kGroupsSplit = 4;
 
-// row -> TMEM lane for an M = 64 accumulator (filled from the self-test probe)
-__constant__ signed char c_row_of_lane[128];
 
 // byte offset of element (r, k) inside a 64 x 64 BF16 block (core-matrix layout)
 __host__ __device__ __forceinline__ uint32_t blk_off(int r, int k) {
@@ -291,9 +289,6 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
   bool fail = false; // this thread's waits (folded into `ok` once per item)
   constexpr uint32_t idesc128 = ptx::idesc_bf16_f32(128, 64);
   constexpr uint32_t idesc64 = ptx::idesc_bf16_f32(64, 64);
-  // M = 64 accumulator row held by this thread (-1: lane unused)
-  const int zrow = c_row_of_lane[warp * 32 + lane];
-
   // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
   // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
   // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next item are
@@ -411,52 +406,57 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
     // the image's only readers are done: fetch the next item's image and incoming entries
     if (tid == 0 && has_next) issue_image<SPLIT>(sm + L.img, a.image, item2, bar_load);
     if (has_next) fetch_in(a, epoch, item2, t2, l0, e0, w0, w1);
-    // 5. epilogue 2 from registers.  Row zrow = (bh, bl) of Z (bra indices of legs H, Lg),
-    //    columns (kh, kl):
-    //      outH[bh][kh] = sum_{bl,kl} Z[(bh,bl)][(kh,kl)] m_Lg[bl][kl]   (sum over 8 rows)
-    //      outL[bl][kl] = sum_{bh,kh} Z[(bh,bl)][(kh,kl)] m_H[bh][kh]    (sum over 8 rows)
+    // 5. epilogue 2 from registers.  Z = Z[(bh,bl)][(kh,kl)] (bra indices of legs H, Lg
+    //    on rows, kets on columns) is read with the 16x32bx2 shape: thread (w, l) holds row
+    //    16w + (l & 15), i.e. bh = 2w + ((l >> 3) & 1), bl = l & 7, and the columns of its
+    //    half hf = l >> 4: kh = 4 hf .. 4 hf + 3, all kl.
+    //      outH[bh][kh] = sum_{bl,kl} Z m_Lg[bl][kl]   (reduced over bl: lanes ^1 ^2 ^4)
+    //      outL[bl][kl] = sum_{bh,kh} Z m_H[bh][kh]    (over the halves ^16, bh ^8, warps)
     {
-      const int bh = zrow >> 3, bl = zrow & 7;
-      float th[8], tl[8], ml[8], mh[8];
+      const int hf = lane >> 4, bh = 2 * warp + ((lane >> 3) & 1), bl = lane & 7;
+      float th[4], tl[8], ml[8], mh[4];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        th[k] = tl[k] = 0.f;
-        ml[k] = msg[Lg * 64 + (bl & 7) * 8 + k];
-        mh[k] = msg[H * 64 + (bh & 7) * 8 + k];
+        tl[k] = 0.f;
+        ml[k] = msg[Lg * 64 + bl * 8 + k];
       }
 #pragma unroll
-      for (int qc = 0; qc < 4; ++qc) {  // columns kh = 2 qc, 2 qc + 1
+      for (int q = 0; q < 4; ++q) {
+        th[q] = 0.f;
+        mh[q] = msg[H * 64 + bh * 8 + 4 * hf + q];
+      }
+#pragma unroll
+      for (int qc = 0; qc < 2; ++qc) {  // columns 16 qc + j (+ 32 hf): kh = 4 hf + 2 qc + (j >> 3)
         float z[16];
-        ptx::tmem_ld16(tq + 16 * qc, z);
+        ptx::tmem_ld16x2(tq + 16 * qc, z);
         ptx::tmem_wait_ld();
-        if (zrow >= 0) {
 #pragma unroll
-          for (int j = 0; j < 2; ++j)
+        for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
-            for (int kl = 0; kl < 8; ++kl) {
-              const int kh = 2 * qc + j;
-              th[kh] = fmaf(z[j * 8 + kl], ml[kl], th[kh]);
-              tl[kl] = fmaf(z[j * 8 + kl], mh[kh], tl[kl]);
-            }
-        }
+          for (int kl = 0; kl < 8; ++kl) {
+            const int q = 2 * qc + jj;
+            th[q] = fmaf(z[jj * 8 + kl], ml[kl], th[q]);
+            tl[kl] = fmaf(z[jj * 8 + kl], mh[q], tl[kl]);
+          }
       }
-      // rows 16w + lane (lane < 16): bl = lane & 7, bh = 2w + (lane >> 3)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        th[q] += __shfl_xor_sync(0xffffffffu, th[q], 1);
+        th[q] += __shfl_xor_sync(0xffffffffu, th[q], 2);
+        th[q] += __shfl_xor_sync(0xffffffffu, th[q], 4);
+      }
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        th[k] += __shfl_xor_sync(0xffffffffu, th[k], 1);
-        th[k] += __shfl_xor_sync(0xffffffffu, th[k], 2);
-        th[k] += __shfl_xor_sync(0xffffffffu, th[k], 4);
+        tl[k] += __shfl_xor_sync(0xffffffffu, tl[k], 16);
         tl[k] += __shfl_xor_sync(0xffffffffu, tl[k], 8);
       }
-      if (zrow >= 0) {
-        if ((lane & 7) == 0) {
+      if (bl == 0) {
 #pragma unroll
-          for (int k = 0; k < 8; ++k) outs[bh * 8 + k] = th[k];
-        }
-        if (lane < 8) {
+        for (int q = 0; q < 4; ++q) outs[bh * 8 + 4 * hf + q] = th[q];
+      }
+      if (lane < 8) {
 #pragma unroll
-          for (int k = 0; k < 8; ++k) part[warp * 64 + bl * 8 + k] = tl[k];
-        }
+        for (int k = 0; k < 8; ++k) part[warp * 64 + bl * 8 + k] = tl[k];
       }
     }
     ptx::tc_fence_before();
@@ -633,6 +633,69 @@ __global__ void __launch_bounds__(kThreads) tc_probe_kernel(float* out, int* err
   }
 }
 
+// Second probe: D_row[r][n] = r and D_col[r][n] = n (M = 64, exact BF16 products with an
+// identity A) read back with the 16x32bx2 shape the sweep's second epilogue uses; out[t][j]
+// = (row, col) received by thread t in register j.
+__global__ void __launch_bounds__(kThreads) tc_probe16_kernel(float* out, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* A = sm;
+  unsigned char* Br = sm + kBlk;
+  unsigned char* Bc = sm + 2 * kBlk;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 3 * kBlk);
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm + 3 * kBlk + 16);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int j = tid; j < 64 * 64; j += kThreads) {
+    const int r = j >> 6, k = j & 63;
+    *reinterpret_cast<__nv_bfloat16*>(A + blk_off(r, k)) = __float2bfloat16_rn(r == k ? 1.f : 0.f);
+    *reinterpret_cast<__nv_bfloat16*>(Br + blk_off(r, k)) = __float2bfloat16_rn((float)k);
+    *reinterpret_cast<__nv_bfloat16*>(Bc + blk_off(r, k)) = __float2bfloat16_rn((float)r);
+  }
+  if (warp == 0) {
+    ptx::tmem_alloc(taddr_s, 128);
+    ptx::tmem_relinquish();
+  }
+  if (tid == 0) {
+    ptx::mbar_init(bar, 1);
+    ptx::fence_mbar_init();
+  }
+  ptx::fence_proxy_async_smem();
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *taddr_s;
+  if (tid == 0) {
+    const uint32_t a0 = ptx::smem_u32(A), br = ptx::smem_u32(Br), bc = ptx::smem_u32(Bc);
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t ko = 2 * j * 128;
+      ptx::mma_bf16(tmem, ptx::smem_desc(a0 + ko, 128, 1024), ptx::smem_desc(br + ko, 128, 1024),
+                    ptx::idesc_bf16_f32(64, 64), j > 0);
+      ptx::mma_bf16(tmem + 64, ptx::smem_desc(a0 + ko, 128, 1024), ptx::smem_desc(bc + ko, 128, 1024),
+                    ptx::idesc_bf16_f32(64, 64), j > 0);
+    }
+    ptx::mma_commit(bar);
+  }
+  const bool ok = __syncthreads_and(ptx::mbar_wait_bounded(bar, 0, kMaxPolls));
+  if (!ok && tid == 0) atomicExch(err, 1);
+  ptx::tc_fence_after();
+  if (ok) {
+    const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);
+    float vr[16], vc[16];
+    ptx::tmem_ld16x2(tq, vr);
+    ptx::tmem_ld16x2(tq + 64, vc);
+    ptx::tmem_wait_ld();
+    for (int j = 0; j < 16; ++j) {
+      out[(tid * 16 + j) * 2 + 0] = vr[j];
+      out[(tid * 16 + j) * 2 + 1] = vc[j];
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 128);
+  }
+}
+
 struct ProbeResult {
   bool ran = false;
   bool m128_ok = false;
@@ -702,9 +765,35 @@ cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max
     for (int r = 0; r < 64 && expected; ++r)
       expected = g_probe.row_of_lane[(r / 16) * 32 + (r % 16)] == r;
     g_probe.m64_ok = herr == 0 && expected;
-    if (g_probe.m64_ok) {
-      e = cudaMemcpyToSymbol(c_row_of_lane, g_probe.row_of_lane, 128);
+    // the second epilogue's 16x32bx2 loads: thread t, register j <- row 16 (t / 32) +
+    // (t & 15), column j + 32 ((t >> 4) & 1)
+    {
+      float* d16 = nullptr;
+      int* d_err16 = nullptr;
+      e = cudaMalloc(&d16, 128 * 16 * 2 * sizeof(float));
       if (e != cudaSuccess) return e;
+      e = cudaMalloc(&d_err16, sizeof(int));
+      if (e != cudaSuccess) { cudaFree(d16); return e; }
+      cudaMemsetAsync(d_err16, 0, sizeof(int), st);
+      cudaMemsetAsync(d16, 0xff, 128 * 16 * 2 * sizeof(float), st);
+      const size_t smem16 = 3 * kBlk + 64;
+      cudaFuncSetAttribute(tc_probe16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem16);
+      tc_probe16_kernel<<<1, kThreads, smem16, st>>>(d16, d_err16);
+      e = cudaGetLastError();
+      std::vector<float> h16(128 * 16 * 2);
+      int herr16 = 0;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h16.data(), d16, h16.size() * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&herr16, d_err16, 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      cudaFree(d16);
+      cudaFree(d_err16);
+      if (e != cudaSuccess) return e;
+      bool ok16 = herr16 == 0;
+      for (int t = 0; t < 128 && ok16; ++t)
+        for (int j = 0; j < 16 && ok16; ++j)
+          ok16 = h16[(t * 16 + j) * 2] == (float)(16 * (t / 32) + (t & 15)) &&
+                 h16[(t * 16 + j) * 2 + 1] == (float)(j + 32 * ((t >> 4) & 1));
+      g_probe.m64_ok = g_probe.m64_ok && ok16;
     }
     g_probe.ran = true;
   }
