@@ -539,6 +539,7 @@ __global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
   const T* tin = reinterpret_cast<const T*>(d.tan_in);
   const int half = a.msg_cap / 2;
+  if (d.done && *reinterpret_cast<const volatile int*>(d.done)) return;
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
@@ -646,9 +647,10 @@ __global__ void grad_g_kernel(const long long* moff, const int* rev, const int* 
 // mu_s = (lambda_s - <lambda_s, F_s>) / S_s  (normalised updates) or lambda_s
 template <typename T>
 __global__ void grad_mu_kernel(const long long* moff, int nslots, const T* lam, const T* F, const T* S, T* mu,
-                               int normalize) {
+                               int normalize, const int* done) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nslots) return;
+  if (done && *reinterpret_cast<const volatile int*>(done)) return;
   T dot = 0;
   if (normalize)
     for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) dot += lam[j] * F[j];
@@ -659,7 +661,8 @@ __global__ void grad_mu_kernel(const long long* moff, int nslots, const T* lam, 
 
 // lambda <- g + cot; stats[0] = max |change|, stats[1] = max |lambda| (order-encoded)
 template <typename T>
-__global__ void grad_update_kernel(long long n, const T* g, const T* cot, T* lam, unsigned long long* stats) {
+__global__ void grad_update_kernel(long long n, const T* g, const T* cot, T* lam, AdjState* adj) {
+  if (*reinterpret_cast<const volatile int*>(&adj->done)) return;
   double dmax = 0, lmax = 0;
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
     const T v = g[j] + cot[j];
@@ -671,9 +674,35 @@ __global__ void grad_update_kernel(long long n, const T* g, const T* cot, T* lam
   for (int o = 8; o >= 1; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
   for (int o = 16; o >= 1; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(&stats[0], enc_double(dmax));
-    atomicMax(&stats[1], enc_double(lmax));
+    atomicMax(&adj->dmax, enc_double(dmax));
+    atomicMax(&adj->lmax, enc_double(lmax));
   }
+}
+
+__global__ void adj_reset_kernel(AdjState* s, double tol, int maxiter) {
+  s->dmax = s->lmax = enc_double(0.0);
+  s->done = maxiter <= 0;
+  s->iters = 0;
+  s->nan = 0;
+  s->maxiter = maxiter;
+  s->tol = tol;
+  s->resid = 0.0;
+}
+
+// One step of the adjoint loop's stopping rule (single thread, after the update).
+__global__ void adj_step_kernel(AdjState* s) {
+  if (s->done) return;
+  const int it = ++s->iters;
+  const double dmax = dec_double(s->dmax), lmax = dec_double(s->lmax);
+  const double r = lmax > 0 ? dmax / lmax : 0.0;
+  s->resid = r;
+  if (r != r) {
+    s->nan = 1;
+    s->done = 1;
+  } else if (r < s->tol || it >= s->maxiter) {
+    s->done = 1;
+  }
+  s->dmax = s->lmax = enc_double(0.0);
 }
 
 // ---- the one-layer kernel ----------------------------------------------------------------
@@ -1108,21 +1137,31 @@ cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, cons
 }
 
 cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const void* lam, const void* F,
-                           const void* S, void* mu, int normalize, cudaStream_t st) {
+                           const void* S, void* mu, int normalize, const int* done, cudaStream_t st) {
   if (nslots <= 0) return cudaSuccess;
   const int grid = (nslots * 32 + 255) / 256;
   ITN_REAL_DISPATCH(dtype, grad_mu_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)lam, (const T*)F,
-                                                                  (const T*)S, (T*)mu, normalize);
+                                                                  (const T*)S, (T*)mu, normalize, done);
                     return cudaGetLastError());
 }
 
 cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
-                               unsigned long long* stats, cudaStream_t st) {
+                               AdjState* adj, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int grid = (int)std::min<long long>((n + 255) / 256, 1024);
   ITN_REAL_DISPATCH(dtype, grad_update_kernel<T><<<grid, 256, 0, st>>>(n, (const T*)g, (const T*)cot, (T*)lam,
-                                                                      stats);
+                                                                      adj);
                     return cudaGetLastError());
+}
+
+cudaError_t launch_adj_reset(AdjState* adj, double tol, int maxiter, cudaStream_t st) {
+  adj_reset_kernel<<<1, 1, 0, st>>>(adj, tol, maxiter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_step(AdjState* adj, cudaStream_t st) {
+  adj_step_kernel<<<1, 1, 0, st>>>(adj);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st) {

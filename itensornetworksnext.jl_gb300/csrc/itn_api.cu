@@ -1029,14 +1029,20 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   }
   CK(launch_reset_state(conv(c), use_tol ? o->tol : -1.0, use_tol ? 1 : 0, c->stream));
   int launches = 1;
-  const int chunk = o->maxiter >= 0 ? o->maxiter : 64;
+  // Without a tolerance the whole run is one graph.  With one, sweeps after convergence
+  // are no-op launches (~2 us each), so a CUDA-core run goes in growing chunks (16, 32,
+  // 64, 64, ...) with one host check of the done flag per chunk.  Tensor-core runs keep one
+  // graph per maxiter: their split sweeps are the last ones of the graph.
   const int64_t cap = o->maxiter >= 0 ? o->maxiter : 1000000;
+  const bool grow = use_tol && (o->precision == ITN_PREC_NATIVE || o->maxiter < 0);
+  int chunk = grow ? 16 : (o->maxiter >= 0 ? (int)std::min<int64_t>(cap, 1 << 30) : 64);
   int64_t issued = 0;
   float total_ms = 0.f;
   ConvState hs;
   memset(&hs, 0, sizeof(hs));
   while (issued < cap) {
     const int n = (int)std::min<int64_t>(chunk, cap - issued);
+    if (grow) chunk = std::min(2 * chunk, 64);
     if (n <= 0) break;
     // one cached graph per (schedule, start buffer, sweep count, options)
     char keyb[256];
@@ -1221,10 +1227,10 @@ int adjoint_prepare(itn_ctx* c, const void* m, int normalized) {
 // cot = J^T lam for the sweep m -> F(m) (needs adjoint_prepare): lam is projected through
 // the normalisation (mu = (lam - <lam, F>) / S) and pushed back through the products by
 // the dual interpreter (tangent of the leave-one-out contraction on every leg).
-int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normalized) {
+int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normalized, const int* done = nullptr) {
   const int ns = (int)c->nslots, np = (int)c->items_par.size() / 2;
   CK(launch_grad_mu(c->dtype, c->d_moff.as<long long>(), ns, lam, c->d_F.p, c->d_S.p, c->d_mu.p, normalized,
-                    c->stream));
+                    done, c->stream));
   GenericArgs da;
   LaunchCfg dcfg;
   if (int r = plan_dual(c, da, dcfg, c->d_items_par.as<int>(), np, m)) return r;
@@ -1232,6 +1238,7 @@ int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normaliz
   memset(&dd, 0, sizeof(dd));
   dd.tan_in = c->d_mu.p;
   dd.tan_out = cot;
+  dd.done = done;
   CK(launch_dual(c->dtype, da, dd, dcfg, c->stream));
   return ITN_OK;
 }
@@ -1295,31 +1302,38 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
   if (o->adjoint) {
     CK(c->d_g.ensure(std::max<size_t>(mb, 16)));
     CK(c->d_lam.ensure(std::max<size_t>(mb, 16)));
-    CK(c->d_stats.ensure(2 * sizeof(unsigned long long)));
+    CK(c->d_stats.ensure(sizeof(AdjState)));
     if (int r = adjoint_prepare(c, m, o->normalized)) return r;
     // g = dL/dm, lambda_0 = g
     CK(launch_grad_g(dt, c->d_moff.as<long long>(), c->d_rev.as<int>(), c->d_slot_dst.as<int>(),
                      c->d_slot_eidx.as<int>(), ns, c->d_U.p, m, c->d_zv.p, c->d_ze.p, c->d_g.p, c->stream));
     CK(cudaMemcpyAsync(c->d_lam.p, c->d_g.p, mb, cudaMemcpyDeviceToDevice, c->stream));
-    const unsigned long long init[2] = {0x8000000000000000ull, 0x8000000000000000ull};  // enc(+0.0)
-    // adjoint BP: lambda <- g + J^T lambda  until the relative change is below tol
-    for (iters = 0; iters < std::max(o->maxiter, 0);) {
-      if (int r = apply_jt(c, m, c->d_lam.p, c->d_cot.p, o->normalized)) return r;
-      CK(cudaMemcpyAsync(c->d_stats.p, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
-      CK(launch_grad_update(dt, (long long)c->moff[c->nslots], c->d_g.p, c->d_cot.p, c->d_lam.p,
-                            c->d_stats.as<unsigned long long>(), c->stream));
-      unsigned long long hs[2];
-      CK(cudaMemcpyAsync(hs, c->d_stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+    // adjoint BP: lambda <- g + J^T lambda until the relative change is below tol.  The
+    // stopping rule runs on the device (AdjState); iterations are enqueued in chunks and
+    // the host reads the state once per chunk (launches after the stop return at once).
+    AdjState* adj = c->d_stats.as<AdjState>();
+    const int maxit = std::max(o->maxiter, 0);
+    CK(launch_adj_reset(adj, o->tol, maxit, c->stream));
+    AdjState hs;
+    memset(&hs, 0, sizeof(hs));
+    for (int issued = 0; issued < maxit;) {
+      const int chunk = std::min(maxit - issued, 8);
+      for (int k = 0; k < chunk; ++k) {
+        if (int r = apply_jt(c, m, c->d_lam.p, c->d_cot.p, o->normalized, &adj->done)) return r;
+        CK(launch_grad_update(dt, (long long)c->moff[c->nslots], c->d_g.p, c->d_cot.p, c->d_lam.p, adj, c->stream));
+        CK(launch_adj_step(adj, c->stream));
+      }
+      issued += chunk;
+      CK(cudaMemcpyAsync(&hs, adj, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
       CK(cudaStreamSynchronize(c->stream));
-      ++iters;
-      const double dmax = dec_double(hs[0]), lmax = dec_double(hs[1]);
-      resid = lmax > 0 ? dmax / lmax : 0.0;
-      if (!(resid == resid)) return fail(c, ITN_ERR_NAN, "adjoint iteration produced NaN");
-      if (resid < o->tol) break;
+      if (hs.done) break;
     }
+    iters = hs.iters;
+    resid = hs.resid;
+    if (hs.nan) return fail(c, ITN_ERR_NAN, "adjoint iteration produced NaN");
     // correction lambda^T dF/dA: tangent part of the all-legs contraction with mu
     CK(launch_grad_mu(dt, c->d_moff.as<long long>(), ns, c->d_lam.p, c->d_F.p, c->d_S.p, c->d_mu.p,
-                      o->normalized, c->stream));
+                      o->normalized, nullptr, c->stream));
     d.tan_in = c->d_mu.p;
     d.dump_tangent = 1;
     for (int tr = 0; tr < 2; ++tr) {

@@ -65,6 +65,21 @@ struct DualArgs {
   void* grad_out;      // DUMP target (packed canonical tensors)
   const void* zv;      // per-vertex Z_u (DUMP of the value plane scales by 1/Z_u)
   int dump_tangent;    // DUMP the tangent plane (unscaled) instead of the value plane
+  const int* done;     // adjoint loop: skip the launch once the iteration has stopped (may be null)
+};
+
+// Device-side state of the adjoint fixed-point iteration lambda <- g + J^T lambda: the
+// update kernel folds max|lambda_new - lambda| and max|lambda_new| into dmax / lmax
+// (order-encoded), a one-thread step kernel turns them into the relative change and
+// stops the loop; launches after the stop return at once.
+struct AdjState {
+  unsigned long long dmax, lmax;
+  int done;       // stopped (converged, NaN or maxiter)
+  int iters;      // iterations executed
+  int nan;        // the relative change was NaN
+  int maxiter;
+  double tol;
+  double resid;   // last relative change
 };
 
 struct LaunchCfg {
@@ -101,9 +116,11 @@ cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, cons
                           const int* eidx, int nslots, const void* U, const void* m, const void* zv,
                           const void* ze, void* g, cudaStream_t st);
 cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const void* lam, const void* F,
-                           const void* S, void* mu, int normalize, cudaStream_t st);
+                           const void* S, void* mu, int normalize, const int* done, cudaStream_t st);
 cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
-                               unsigned long long* stats, cudaStream_t st);
+                               AdjState* adj, cudaStream_t st);
+cudaError_t launch_adj_reset(AdjState* adj, double tol, int maxiter, cudaStream_t st);
+cudaError_t launch_adj_step(AdjState* adj, cudaStream_t st);
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st);
 cudaError_t launch_step_check(ConvState* s, cudaStream_t st);
 
