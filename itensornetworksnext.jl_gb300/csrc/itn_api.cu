@@ -519,11 +519,23 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
   c->seq_plans.clear();
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
+  // Small networks (fewer vertices than 4 per SM) get two items per vertex: the two
+  // branches of the top-level leave-one-out split (legs [0, h) and [h, z)) do the same
+  // absorptions as one item but give the SMs twice the CTAs; large networks keep one item
+  // per vertex (one read of the site tensor).
+  const bool halves = nv <= 4 * std::max(c->sm_count, 1);
   for (int64_t u = 0; u < nv; ++u) {
     const int z = (int)(c->off[u + 1] - c->off[u]);
     const uint32_t full = z >= 32 ? 0xffffffffu : ((1u << z) - 1u);
     if (layers == 2) {
-      if (z > 0) {
+      if (z >= 2 && halves) {
+        const int h = (z + 1) / 2;
+        const uint32_t lo = (1u << h) - 1u;
+        c->items_par.push_back((int)u);
+        c->items_par.push_back(program_offset(c, z, lo, 0));
+        c->items_par.push_back((int)u);
+        c->items_par.push_back(program_offset(c, z, full & ~lo, 0));
+      } else if (z > 0) {
         c->items_par.push_back((int)u);
         c->items_par.push_back(program_offset(c, z, full, 0));
       }
