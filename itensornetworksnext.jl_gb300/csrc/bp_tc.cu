@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(kThreads) tc_probe16_kernel(float* out, int* e
   unsigned char* Bc = sm + 2 * kBlk;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 3 * kBlk);
   uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm + 3 * kBlk + 16);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
   for (int j = tid; j < 64 * 64; j += kThreads) {
     const int r = j >> 6, k = j & 63;
     *reinterpret_cast<__nv_bfloat16*>(A + blk_off(r, k)) = __float2bfloat16_rn(r == k ? 1.f : 0.f);
