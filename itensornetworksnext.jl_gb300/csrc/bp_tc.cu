@@ -42,13 +42,37 @@ constexpr int kBlk = 8192;                 // bytes of one 64 x 64 BF16 operand 
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
 constexpr uint32_t kMaxDepPolls = 1u << 22; // bounded waits on another item (64 ns apart)
 constexpr int kTmemCols = 64;
-constexpr int kGroupsBf16 = 8;             // persistent kernel: 4-warp groups per CTA
-constexpr int kGroupsSplit = 4;
+// operand modes of the sweep kernel
+constexpr int kOpBf16 = 0;   // BF16 operands
+constexpr int kOpSplit = 1;  // BF16 hi/lo split operands (3 MMAs per product)
+constexpr int kOpTf32 = 2;   // TF32 operands (kind::tf32, K = 8 per MMA)
+constexpr int kNumOps = 3;
+template <int OP> struct OpT {
+  static constexpr bool split = OP == kOpSplit;
+  static constexpr bool tf32 = OP == kOpTf32;
+  static constexpr uint32_t blk = tf32 ? 16384u : 8192u;  // bytes of one 64 x 64 operand block
+  static constexpr uint32_t sbo = tf32 ? 2048u : 1024u;   // bytes between 8-row core groups
+  static constexpr int ksteps = tf32 ? 8 : 4;             // MMAs per K = 64 (32 bytes of a row each)
+  static constexpr int planes = split ? 2 : 1;            // hi [+ lo]
+  // operand image bytes per vertex: BF16 [A_pq hi | A_qp hi | A_pq lo | A_qp lo], TF32 [A_pq | A_qp]
+  static constexpr uint32_t img_vertex = tf32 ? 4u * 16384u : 8u * 8192u;
+  static constexpr int groups = OP == kOpBf16 ? 8 : 4;    // persistent kernel: 4-warp groups per CTA
+  static constexpr int per_sm = OP == kOpBf16 ? 8 : 4;    // per-sweep kernel: CTAs per SM
+};
 
 
 // byte offset of element (r, k) inside a 64 x 64 BF16 block (core-matrix layout)
 __host__ __device__ __forceinline__ uint32_t blk_off(int r, int k) {
   return (uint32_t)((((r >> 3) << 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// byte offset of element (r, k) inside a 64 x 64 block of the mode's element type
+template <int OP>
+__host__ __device__ __forceinline__ uint32_t op_off(int r, int k) {
+  if constexpr (OP == kOpTf32)
+    return (uint32_t)((((r >> 3) << 4) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+  else
+    return blk_off(r, k);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -73,15 +97,15 @@ struct TcSmem {
 // G2 runs as two K = 64 halves (s = 0, then s = 1) so that one 64 x 64 operand buffer
 // holds P, then XT0, then XT1: 8 CTAs fit on an SM (4 for the split variant), which
 // covers the 2 V half-vertex items of the 32 x 32 lattice in two waves instead of three.
-// img : A_qp (half 0) or A_pq (half 1): hi [+ lo]          16 KB [32 KB]
-// reg : P, then XT0, then XT1 (hi [+ lo])                   8 KB [16 KB]
+// img : A_qp (half 0) or A_pq (half 1): hi [+ lo]          16 KB [32 KB split / TF32]
+// reg : P, then XT0, then XT1 (hi [+ lo])                   8 KB [16 KB split / TF32]
 // msg : incoming messages m0..m3 (FP32)                     1 KB
-template <bool SPLIT>
+template <int OP>
 __host__ __device__ constexpr TcSmem tc_smem() {
   TcSmem L{};
   uint32_t o = 0;
-  L.img = o;  o += (SPLIT ? 4 : 2) * kBlk;
-  L.reg = o;  o += (SPLIT ? 2 : 1) * kBlk;
+  L.img = o;  o += 2 * OpT<OP>::planes * OpT<OP>::blk;
+  L.reg = o;  o += OpT<OP>::planes * OpT<OP>::blk;
   L.msg = o;  o += 4 * 64 * 4;
   L.outs = o; o += 64 * 4;
   L.part = o; o += 4 * 64 * 4;
@@ -94,7 +118,7 @@ __host__ __device__ constexpr TcSmem tc_smem() {
 
 struct TcArgs {
   const int* rev;
-  const unsigned char* image;  // per vertex: [A_pq hi | A_qp hi | A_pq lo | A_qp lo], 16 KB each
+  const unsigned char* image;  // operand image of the mode (OpT<OP>::img_vertex bytes per vertex)
   const float* msg_in;
   float* msg_out;
   int nv;
@@ -140,32 +164,48 @@ __device__ __forceinline__ void store_row_packed(unsigned char* blk, int r, cons
         make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
 }
 
-// Issue D (+)= A * B^T over K = 64 (four K-steps of 16), with the split terms when SPLIT.
-template <bool SPLIT>
+// Store a 64-entry row of TF32 patterns into row r of a 64 x 64 TF32 block.
+__device__ __forceinline__ void store_row_tf32(unsigned char* blk, int r, const uint32_t (&w)[64]) {
+#pragma unroll
+  for (int c = 0; c < 16; ++c)
+    *reinterpret_cast<uint4*>(blk + op_off<kOpTf32>(r, c * 4)) =
+        make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+}
+
+// Issue D (+)= A * B^T over K = 64 (K-steps of 32 bytes per row), with the split terms
+// for kOpSplit and kind::tf32 MMAs for kOpTf32.
+template <int OP>
 __device__ __forceinline__ void mma_k64(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t b, uint32_t b_lo,
                                         uint32_t idesc, bool accumulate) {
+  constexpr uint32_t sbo = OpT<OP>::sbo;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < OpT<OP>::ksteps; ++j) {
     const uint32_t ko = (uint32_t)(2 * j) * 128;  // core columns 2j, 2j+1
-    ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc,
-                  accumulate || j > 0);
-    if constexpr (SPLIT) {
-      ptx::mma_bf16(d, ptx::smem_desc(a_lo + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc, 1);
-      ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b_lo + ko, 128, 1024), idesc, 1);
+    if constexpr (OP == kOpTf32) {
+      ptx::mma_tf32(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc,
+                    accumulate || j > 0);
+    } else {
+      ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc,
+                    accumulate || j > 0);
+      if constexpr (OP == kOpSplit) {
+        ptx::mma_bf16(d, ptx::smem_desc(a_lo + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc, 1);
+        ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b_lo + ko, 128, sbo), idesc, 1);
+      }
     }
   }
 }
 
-template <bool SPLIT>
+template <int OP>
 __device__ __forceinline__ void issue_image(unsigned char* sm_img, const unsigned char* image, int item,
                                             uint64_t* bar) {
+  using O = OpT<OP>;
   const int u = item >> 1, h = item & 1;
-  // half 0 uses A_qp (second 16 KB of the hi image), half 1 A_pq (first)
-  const unsigned char* base = image + (size_t)u * 4 * (2 * kBlk);
-  const uint32_t hi_off = (h ? 0u : 2u) * kBlk;
-  ptx::mbar_arrive_expect_tx(bar, (SPLIT ? 4 : 2) * kBlk);
-  ptx::bulk_g2s(sm_img, base + hi_off, 2 * kBlk, bar);
-  if constexpr (SPLIT) ptx::bulk_g2s(sm_img + 2 * kBlk, base + 4 * kBlk + hi_off, 2 * kBlk, bar);
+  // half 0 uses A_qp (blocks 2, 3 of the image), half 1 A_pq (blocks 0, 1)
+  const unsigned char* base = image + (size_t)u * O::img_vertex;
+  const uint32_t hi_off = (h ? 0u : 2u) * O::blk;
+  ptx::mbar_arrive_expect_tx(bar, 2 * O::planes * O::blk);
+  ptx::bulk_g2s(sm_img, base + hi_off, 2 * O::blk, bar);
+  if constexpr (O::split) ptx::bulk_g2s(sm_img + 2 * O::blk, base + 4 * O::blk + hi_off, 2 * O::blk, bar);
 }
 
 // ---- the sweep kernel --------------------------------------------------------------------
@@ -245,10 +285,12 @@ __device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int ite
   return false;
 }
 
-template <bool SPLIT, int GROUPS, bool PERSIST>
-__global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4 : 8)) bp_tc_kernel(TcArgs a) {
+template <int OP, int GROUPS, bool PERSIST>
+__global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::per_sm) bp_tc_kernel(TcArgs a) {
+  using O = OpT<OP>;
+  constexpr bool SPLIT = O::split;
   extern __shared__ __align__(1024) unsigned char sm_all[];
-  constexpr TcSmem L = tc_smem<SPLIT>();
+  constexpr TcSmem L = tc_smem<OP>();
   const int g = GROUPS > 1 ? (int)(threadIdx.x >> 7) : 0;
   const uint32_t bar_id = 1 + g;
   unsigned char* sm = sm_all + g * L.stride;
@@ -282,13 +324,13 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
   const uint32_t tmem = *taddr_s + (uint32_t)(kTmemCols * g);
   const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
   const uint32_t sbase = ptx::smem_u32(sm);
-  const uint32_t Aimg = sbase + L.img, Alo = 2 * kBlk;
+  const uint32_t Aimg = sbase + L.img, Alo = 2 * O::blk;
   const uint32_t R = sbase + L.reg;
   uint32_t ph_load = 0, ph_mma = 0;
   bool ok = true;    // group-uniform: false once a bounded wait gave up
   bool fail = false; // this thread's waits (folded into `ok` once per item)
-  constexpr uint32_t idesc128 = ptx::idesc_bf16_f32(128, 64);
-  constexpr uint32_t idesc64 = ptx::idesc_bf16_f32(64, 64);
+  constexpr uint32_t idesc128 = O::tf32 ? ptx::idesc_tf32_f32(128, 64) : ptx::idesc_bf16_f32(128, 64);
+  constexpr uint32_t idesc64 = O::tf32 ? ptx::idesc_tf32_f32(64, 64) : ptx::idesc_bf16_f32(64, 64);
   // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
   // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
   // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next item are
@@ -297,7 +339,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
   unsigned long long w0 = 0, w1 = 0;
   // the operand image is static: its copy starts before the done flag is read
   const bool first = gid < n_items;
-  if (first && tid == 0) issue_image<SPLIT>(sm + L.img, a.image, gid, bar_load);
+  if (first && tid == 0) issue_image<OP>(sm + L.img, a.image, gid, bar_load);
   const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
   if (first && !skip) fetch_in(a, epoch, gid, 0, l0, e0, w0, w1);
   int t = (first && !skip) ? 0 : nsweeps, item = gid;
@@ -332,14 +374,22 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
       for (int j = 0; j < 4; ++j) {
         const int ko = kq + j;
         const float w = ma[bo * 8 + ko];
-        const uint32_t off = blk_off(bo * 8 + bi, ko * 8);
-        if constexpr (SPLIT) {
+        const uint32_t off = op_off<OP>(bo * 8 + bi, ko * 8);
+        if constexpr (O::tf32) {
+          // 8 K-entries = two 16-byte core rows
+          *reinterpret_cast<uint4*>(reg + off) =
+              make_uint4(ptx::to_tf32(w * mb[0]), ptx::to_tf32(w * mb[1]), ptx::to_tf32(w * mb[2]),
+                         ptx::to_tf32(w * mb[3]));
+          *reinterpret_cast<uint4*>(reg + op_off<OP>(bo * 8 + bi, ko * 8 + 4)) =
+              make_uint4(ptx::to_tf32(w * mb[4]), ptx::to_tf32(w * mb[5]), ptx::to_tf32(w * mb[6]),
+                         ptx::to_tf32(w * mb[7]));
+        } else if constexpr (SPLIT) {
           float hv[8], lv[8];
 #pragma unroll
           for (int k = 0; k < 8; ++k) split_bf16(w * mb[k], hv[k], lv[k]);
           *reinterpret_cast<uint4*>(reg + off) = make_uint4(pack_bf16(hv[0], hv[1]), pack_bf16(hv[2], hv[3]),
                                                             pack_bf16(hv[4], hv[5]), pack_bf16(hv[6], hv[7]));
-          *reinterpret_cast<uint4*>(reg + kBlk + off) =
+          *reinterpret_cast<uint4*>(reg + O::blk + off) =
               make_uint4(pack_bf16(lv[0], lv[1]), pack_bf16(lv[2], lv[3]), pack_bf16(lv[4], lv[5]),
                          pack_bf16(lv[6], lv[7]));
         } else {
@@ -355,7 +405,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
     if (tid == 0) {
       if (!ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls)) fail = true;
       ptx::tc_fence_after();
-      mma_k64<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc128, false);
+      mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc128, false);
       ptx::mma_commit(bar_mma);
     }
     ph_load ^= 1;
@@ -366,17 +416,28 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
     //    hold s = 0 and store XT0 now; warps 2, 3 keep s = 1 packed in registers until the
     //    first half of G2 has consumed XT0 (G2's accumulator overwrites their TMEM lanes).
     const int xr = (warp * 32 + lane) & 63;
-    uint32_t hk[32], lk[SPLIT ? 32 : 1];
+    // BF16: 32 packed pairs (+ 32 lo pairs when split); TF32: 64 TF32 patterns
+    uint32_t hk[O::tf32 ? 64 : 32], lk[SPLIT ? 32 : 1];
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       float v[32];
       tmem_ld32(tq + 32 * half, v);
-      pack_row32<SPLIT>(v, hk + 16 * half, lk + (SPLIT ? 16 * half : 0));
+      if constexpr (O::tf32) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) hk[32 * half + e] = ptx::to_tf32(v[e]);
+      } else {
+        pack_row32<SPLIT>(v, hk + 16 * half, lk + (SPLIT ? 16 * half : 0));
+      }
     }
-    if (warp < 2) {
-      store_row_packed(reg, xr, hk);
-      if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
-    }
+    auto store_xt = [&]() {
+      if constexpr (O::tf32) {
+        store_row_tf32(reg, xr, *reinterpret_cast<uint32_t(*)[64]>(hk));
+      } else {
+        store_row_packed(reg, xr, *reinterpret_cast<uint32_t(*)[32]>(hk));
+        if constexpr (SPLIT) store_row_packed(reg + O::blk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
+      }
+    };
+    if (warp < 2) store_xt();
     ptx::tc_fence_before();
     ptx::fence_proxy_async_smem();
     group_sync(bar_id);
@@ -384,27 +445,24 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : (SPLIT ? 4
     //    M = 64, in two K halves: s = 0 from XT0, then s = 1 from XT1 in the same buffer
     if (tid == 0) {
       ptx::tc_fence_after();
-      mma_k64<SPLIT>(tmem, Aimg, Aimg + Alo, R, R + kBlk, idesc64, false);
+      mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc64, false);
       ptx::mma_commit(bar_mma);
     }
     if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
     ph_mma ^= 1;
-    if (warp >= 2) {
-      store_row_packed(reg, xr, hk);
-      if constexpr (SPLIT) store_row_packed(reg + kBlk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
-    }
+    if (warp >= 2) store_xt();
     ptx::fence_proxy_async_smem();
     group_sync(bar_id);
     if (tid == 0) {
       ptx::tc_fence_after();
-      mma_k64<SPLIT>(tmem, Aimg + kBlk, Aimg + Alo + kBlk, R, R + kBlk, idesc64, true);
+      mma_k64<OP>(tmem, Aimg + O::blk, Aimg + Alo + O::blk, R, R + O::blk, idesc64, true);
       ptx::mma_commit(bar_mma);
     }
     if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
     ph_mma ^= 1;
     ptx::tc_fence_after();
     // the image's only readers are done: fetch the next item's image and incoming entries
-    if (tid == 0 && has_next) issue_image<SPLIT>(sm + L.img, a.image, item2, bar_load);
+    if (tid == 0 && has_next) issue_image<OP>(sm + L.img, a.image, item2, bar_load);
     if (has_next) fetch_in(a, epoch, item2, t2, l0, e0, w0, w1);
     // 5. epilogue 2 from registers.  Z = Z[(bh,bl)][(kh,kl)] (bra indices of legs H, Lg
     //    on rows, kets on columns) is read with the 16x32bx2 shape: thread (w, l) holds row
@@ -571,6 +629,70 @@ __global__ void tc_image_kernel(const float* __restrict__ tens, int nv, unsigned
   }
 }
 
+// ---- TF32 operand image: per vertex [A_pq(s=0,1) | A_qp(s=0,1)], 16 KB per block ----------
+__global__ void tc_image_tf32_kernel(const float* __restrict__ tens, int nv, unsigned char* __restrict__ img) {
+  constexpr uint32_t blk = OpT<kOpTf32>::blk;
+  const long long total = (long long)nv * 8192;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
+       j += (long long)gridDim.x * blockDim.x) {
+    const int u = (int)(j >> 13), e = (int)(j & 8191);
+    const int s = e >> 12, p = (e >> 6) & 63, q = e & 63;
+    const uint32_t v = ptx::to_tf32(tens[j]);
+    unsigned char* base = img + (size_t)u * OpT<kOpTf32>::img_vertex;
+    *reinterpret_cast<uint32_t*>(base + s * blk + op_off<kOpTf32>(p, q)) = v;
+    *reinterpret_cast<uint32_t*>(base + 2 * blk + s * blk + op_off<kOpTf32>(q, p)) = v;
+  }
+}
+
+// ---- TF32 self-test: D = A B^T, A 128 x 64 and B 64 x 64 exact in TF32, kind::tf32 -------
+__global__ void __launch_bounds__(kThreads) tc_probe_tf32_kernel(float* out, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  constexpr uint32_t blk = OpT<kOpTf32>::blk;
+  unsigned char* A = sm;            // 2 blocks
+  unsigned char* B = sm + 2 * blk;  // 1 block
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 3 * blk);
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(sm + 3 * blk + 16);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int j = tid; j < 128 * 64; j += kThreads) {
+    const int r = j >> 6, k = j & 63;
+    *reinterpret_cast<float*>(A + (r >> 6) * blk + op_off<kOpTf32>(r & 63, k)) =
+        (float)(((r * 7 + k * 3) % 17) - 8) * 0.125f;
+    if (r < 64) *reinterpret_cast<float*>(B + op_off<kOpTf32>(r, k)) = (float)(((r * 5 + k * 11) % 13) - 6) * 0.25f;
+  }
+  if (warp == 0) {
+    ptx::tmem_alloc(taddr_s, 64);
+    ptx::tmem_relinquish();
+  }
+  if (tid == 0) {
+    ptx::mbar_init(bar, 1);
+    ptx::fence_mbar_init();
+  }
+  ptx::fence_proxy_async_smem();
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *taddr_s;
+  if (tid == 0) {
+    mma_k64<kOpTf32>(tmem, ptx::smem_u32(A), 0, ptx::smem_u32(B), 0, ptx::idesc_tf32_f32(128, 64), false);
+    ptx::mma_commit(bar);
+  }
+  const bool ok = __syncthreads_and(ptx::mbar_wait_bounded(bar, 0, kMaxPolls));
+  if (!ok && tid == 0) atomicExch(err, 1);
+  ptx::tc_fence_after();
+  if (ok) {
+    float v[64];
+    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), *reinterpret_cast<float(*)[32]>(v));
+    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + 32, *reinterpret_cast<float(*)[32]>(v + 32));
+    for (int e = 0; e < 64; ++e) out[(warp * 32 + lane) * 64 + e] = v[e];
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 64);
+  }
+}
+
 // ---- self-test probe: one CTA, exactly representable BF16 inputs --------------------------
 // A (128 x 64), B (64 x 64); D128 = A B^T with M = 128 in TMEM cols 0..63, D64 = A[0:64] B^T
 // with M = 64 in cols 64..127.  Every TMEM lane of both is written out (out[128][128]).
@@ -700,6 +822,7 @@ struct ProbeResult {
   bool ran = false;
   bool m128_ok = false;
   bool m64_ok = false;
+  bool tf32_ok = false;
   double max_err = 0;
   signed char row_of_lane[128];
 };
@@ -795,6 +918,33 @@ cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max
                  h16[(t * 16 + j) * 2 + 1] == (float)(j + 32 * ((t >> 4) & 1));
       g_probe.m64_ok = g_probe.m64_ok && ok16;
     }
+    // TF32 products (the TF32 precision mode)
+    {
+      float* dt = nullptr;
+      int* d_errt = nullptr;
+      e = cudaMalloc(&dt, 128 * 64 * sizeof(float));
+      if (e != cudaSuccess) return e;
+      e = cudaMalloc(&d_errt, sizeof(int));
+      if (e != cudaSuccess) { cudaFree(dt); return e; }
+      cudaMemsetAsync(d_errt, 0, sizeof(int), st);
+      cudaMemsetAsync(dt, 0, 128 * 64 * sizeof(float), st);
+      const size_t smemt = 3 * OpT<kOpTf32>::blk + 64;
+      cudaFuncSetAttribute(tc_probe_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemt);
+      tc_probe_tf32_kernel<<<1, kThreads, smemt, st>>>(dt, d_errt);
+      e = cudaGetLastError();
+      std::vector<float> ht(128 * 64);
+      int herrt = 0;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(ht.data(), dt, ht.size() * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&herrt, d_errt, 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      cudaFree(dt);
+      cudaFree(d_errt);
+      if (e != cudaSuccess) return e;
+      double mt = 0;
+      for (int r = 0; r < 128; ++r)
+        for (int n = 0; n < 64; ++n) mt = fmax(mt, fabs(ht[r * 64 + n] - ref[r * 64 + n]));
+      g_probe.tf32_ok = herrt == 0 && mt < 1e-6;
+    }
     g_probe.ran = true;
   }
   if (m128_ok) *m128_ok = g_probe.m128_ok;
@@ -810,20 +960,22 @@ cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max
 
 struct TcEngine {
   bool valid = false;
+  bool have_tf32 = false;  // the TF32 image matches the current tensors
   int nv = 0;
-  int precision = 0;
   const int* d_off = nullptr;
   const int* d_rev = nullptr;
   const long long* d_moff = nullptr;
-  unsigned char* image = nullptr;  // per vertex [A_pq hi | A_qp hi | A_pq lo | A_qp lo]
+  unsigned char* image = nullptr;  // BF16 per vertex [A_pq hi | A_qp hi | A_pq lo | A_qp lo]
   size_t image_bytes = 0;
+  unsigned char* image_tf32 = nullptr;  // TF32 per vertex [A_pq | A_qp]
+  size_t image_tf32_bytes = 0;
   int* d_err = nullptr;
   unsigned long long* d_tagged = nullptr;  // persistent kernel: 4 buffers of tagged entries
   size_t tagged_stride = 0;
   unsigned* d_epoch = nullptr;
   int sm_count = 0;
-  int occ[2] = {0, 0};
-  bool persist_ok[2] = {false, false};  // cooperative grid of sm_count CTAs fits
+  int occ[kNumOps] = {0, 0, 0};
+  bool persist_ok[kNumOps] = {false, false, false};  // cooperative grid of sm_count CTAs fits
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -831,6 +983,7 @@ TcEngine* tc_create() { return new TcEngine(); }
 void tc_destroy(TcEngine* e) {
   if (!e) return;
   if (e->image) cudaFree(e->image);
+  if (e->image_tf32) cudaFree(e->image_tf32);
   if (e->d_err) cudaFree(e->d_err);
   if (e->d_tagged) cudaFree(e->d_tagged);
   if (e->d_epoch) cudaFree(e->d_epoch);
@@ -838,8 +991,39 @@ void tc_destroy(TcEngine* e) {
 }
 
 void tc_invalidate(TcEngine* e) {
-  if (e) e->valid = false;
+  if (e) {
+    e->valid = false;
+    e->have_tf32 = false;
+  }
 }
+
+namespace {
+template <int OP> const void* k_launch() { return (const void*)bp_tc_kernel<OP, 1, false>; }
+template <int OP> const void* k_persist() { return (const void*)bp_tc_kernel<OP, OpT<OP>::groups, true>; }
+
+// Residency of the per-sweep kernel from its own resources (shared memory plus the 1 KB the
+// runtime reserves per CTA, registers, 512 TMEM columns per SM), and whether the persistent
+// kernel's cooperative grid (one CTA per SM) fits.
+template <int OP>
+void tc_configure(TcEngine* e, int smem_sm, int regs_sm) {
+  constexpr TcSmem L = tc_smem<OP>();
+  const uint32_t ptot = OpT<OP>::groups * L.stride;
+  cudaFuncSetAttribute(k_launch<OP>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  cudaFuncSetAttribute(k_launch<OP>(), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  cudaFuncSetAttribute(k_persist<OP>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ptot);
+  cudaFuncSetAttribute(k_persist<OP>(), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, k_launch<OP>());
+  const int by_smem = smem_sm / (int)(L.total + 1024);
+  const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 4;
+  e->occ[OP] = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTmemCols));
+  int per_sm = 0;
+  const cudaError_t oe =
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist<OP>(), kThreads * OpT<OP>::groups, ptot);
+  e->persist_ok[OP] = oe == cudaSuccess && per_sm >= 1;
+  cudaGetLastError();
+}
+}  // namespace
 
 cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, const int32_t* bond,
                        const int32_t* phys, const int* d_off, const int* d_rev,
@@ -847,11 +1031,12 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
                        int precision, cudaStream_t st, const char** why) {
   (void)toff;
   *why = nullptr;
-  if (e->valid && e->precision == precision) return cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
-  if (precision != 1) {
-    *why = "only the BF16 tensor-core mode is implemented";
+  if (precision != 1 && precision != 2) {
+    *why = "unknown tensor-core precision";
     return cudaSuccess;
   }
+  const bool want_tf32 = precision == 2;
+  if (e->valid && (!want_tf32 || e->have_tf32)) return cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
   if (layers != 2) {
     *why = "tensor-core sweep needs a norm network (layers = 2)";
     return cudaSuccess;
@@ -870,96 +1055,90 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   int m128 = 0, m64 = 0;
   cudaError_t err = tc_run_probe(st, &m128, &m64, nullptr, nullptr);
   if (err != cudaSuccess) return err;
-  if (!m128 || !m64) {
+  if (!m128 || !m64 || (want_tf32 && !g_probe.tf32_ok)) {
     *why = "tensor-core self-test failed on this device";
     return cudaSuccess;
   }
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  const size_t split_bytes = (size_t)nv * 8 * kBlk;
-  if (e->image_bytes < split_bytes) {
-    if (e->image) cudaFree(e->image);
-    e->image = nullptr;
-    err = cudaMalloc(&e->image, split_bytes);
-    if (err != cudaSuccess) return err;
-    e->image_bytes = split_bytes;
-  }
   if (!e->d_err) {
     err = cudaMalloc(&e->d_err, sizeof(int));
     if (err != cudaSuccess) return err;
   }
   cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
   const int grid = (int)std::min<long long>((nv * 8192 + 255) / 256, 4096);
-  tc_image_kernel<true><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image);
-  err = cudaGetLastError();
-  if (err != cudaSuccess) return err;
-  constexpr TcSmem L0 = tc_smem<false>();
-  constexpr TcSmem L1 = tc_smem<true>();
-  const void* k1[2] = {(const void*)bp_tc_kernel<false, 1, false>, (const void*)bp_tc_kernel<true, 1, false>};
-  const void* kp[2] = {(const void*)bp_tc_kernel<false, kGroupsBf16, true>,
-                       (const void*)bp_tc_kernel<true, kGroupsSplit, true>};
-  const uint32_t tot[2] = {L0.total, L1.total};
-  const uint32_t ptot[2] = {kGroupsBf16 * L0.stride, kGroupsSplit * L1.stride};
-  for (int k = 0; k < 2; ++k) {
-    cudaFuncSetAttribute(k1[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tot[k]);
-    cudaFuncSetAttribute(k1[k], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(kp[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ptot[k]);
-    cudaFuncSetAttribute(kp[k], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (!e->valid) {
+    // the BF16 hi/lo image serves the BF16 sweeps and the split sweeps of every mode
+    const size_t split_bytes = (size_t)nv * OpT<kOpSplit>::img_vertex;
+    if (e->image_bytes < split_bytes) {
+      if (e->image) cudaFree(e->image);
+      e->image = nullptr;
+      err = cudaMalloc(&e->image, split_bytes);
+      if (err != cudaSuccess) return err;
+      e->image_bytes = split_bytes;
+    }
+    tc_image_kernel<true><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    int smem_sm = 0, regs_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    tc_configure<kOpBf16>(e, smem_sm, regs_sm);
+    tc_configure<kOpSplit>(e, smem_sm, regs_sm);
+    tc_configure<kOpTf32>(e, smem_sm, regs_sm);
+    if (getenv("ITN_DEBUG"))
+      fprintf(stderr, "[itn] tc residency: bf16 %d, split %d, tf32 %d CTAs/SM; persistent %d/%d/%d; sms %d\n",
+              e->occ[0], e->occ[1], e->occ[2], (int)e->persist_ok[0], (int)e->persist_ok[1],
+              (int)e->persist_ok[2], e->sm_count);
+    // tagged message buffers of the persistent kernel, zeroed once (epochs start at 1)
+    const size_t stride = (size_t)std::max<int64_t>(nv, 1) * 4 * 64;
+    if (e->tagged_stride < stride) {
+      if (e->d_tagged) cudaFree(e->d_tagged);
+      e->d_tagged = nullptr;
+      e->tagged_stride = 0;
+      err = cudaMalloc(&e->d_tagged, 4 * stride * sizeof(unsigned long long));
+      if (err != cudaSuccess) return err;
+      err = cudaMemsetAsync(e->d_tagged, 0, 4 * stride * sizeof(unsigned long long), st);
+      if (err != cudaSuccess) return err;
+      e->tagged_stride = stride;
+    }
+    if (!e->d_epoch) {
+      err = cudaMalloc(&e->d_epoch, 2 * sizeof(unsigned));
+      if (err != cudaSuccess) return err;
+      const unsigned init[2] = {1u, 0u};
+      err = cudaMemcpyAsync(e->d_epoch, init, sizeof(init), cudaMemcpyHostToDevice, st);
+      if (err != cudaSuccess) return err;
+    }
   }
-  // Resident CTAs per SM from the kernel's own resources: shared memory (plus the
-  // 1 KB the runtime reserves per CTA), registers and TMEM columns (512 per SM).
-  int smem_sm = 0, regs_sm = 0;
-  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-  for (int k = 0; k < 2; ++k) {
-    cudaFuncAttributes fa;
-    cudaFuncGetAttributes(&fa, k1[k]);
-    const int by_smem = smem_sm / (int)(tot[k] + 1024);
-    const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 4;
-    e->occ[k] = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTmemCols));
-    // the cooperative launch needs one resident CTA per SM
-    int per_sm = 0;
-    const int groups = k ? kGroupsSplit : kGroupsBf16;
-    cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp[k], kThreads * groups, ptot[k]);
-    e->persist_ok[k] = oe == cudaSuccess && per_sm >= 1;
-  }
-  cudaGetLastError();
-  if (getenv("ITN_DEBUG"))
-    fprintf(stderr, "[itn] tc residency: bf16 %d (smem %u B), split %d (smem %u B), persistent %d/%d, sms %d\n",
-            e->occ[0], L0.total, e->occ[1], L1.total, (int)e->persist_ok[0], (int)e->persist_ok[1], e->sm_count);
-  // tagged message buffers of the persistent kernel, zeroed once (epochs start at 1)
-  const size_t stride = (size_t)std::max<int64_t>(nv, 1) * 4 * 64;
-  if (e->tagged_stride < stride) {
-    if (e->d_tagged) cudaFree(e->d_tagged);
-    e->d_tagged = nullptr;
-    e->tagged_stride = 0;
-    err = cudaMalloc(&e->d_tagged, 4 * stride * sizeof(unsigned long long));
+  if (want_tf32) {
+    const size_t tf32_bytes = (size_t)nv * OpT<kOpTf32>::img_vertex;
+    if (e->image_tf32_bytes < tf32_bytes) {
+      if (e->image_tf32) cudaFree(e->image_tf32);
+      e->image_tf32 = nullptr;
+      err = cudaMalloc(&e->image_tf32, tf32_bytes);
+      if (err != cudaSuccess) return err;
+      e->image_tf32_bytes = tf32_bytes;
+    }
+    tc_image_tf32_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image_tf32);
+    err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    err = cudaMemsetAsync(e->d_tagged, 0, 4 * stride * sizeof(unsigned long long), st);
-    if (err != cudaSuccess) return err;
-    e->tagged_stride = stride;
-  }
-  if (!e->d_epoch) {
-    err = cudaMalloc(&e->d_epoch, 2 * sizeof(unsigned));
-    if (err != cudaSuccess) return err;
-    const unsigned init[2] = {1u, 0u};
-    err = cudaMemcpyAsync(e->d_epoch, init, sizeof(init), cudaMemcpyHostToDevice, st);
-    if (err != cudaSuccess) return err;
+    e->have_tf32 = true;
   }
   e->nv = (int)nv;
   e->d_off = d_off;
   e->d_rev = d_rev;
   e->d_moff = d_moff;
-  e->precision = precision;
   e->valid = true;
   return cudaStreamSynchronize(st);
 }
 
+static int tc_op(const TcRun& r) { return r.split ? kOpSplit : (r.precision == 2 ? kOpTf32 : kOpBf16); }
+
 static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   TcArgs a;
   a.rev = e->d_rev;
-  a.image = e->image;
+  a.image = tc_op(r) == kOpTf32 ? e->image_tf32 : e->image;
   a.msg_in = reinterpret_cast<const float*>(r.msg_in);
   a.msg_out = reinterpret_cast<float*>(r.msg_out);
   a.nv = e->nv;
@@ -974,30 +1153,17 @@ static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   return a;
 }
 
-cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
-  if (!e || !e->valid) return cudaErrorInvalidValue;
-  TcArgs a = tc_args(e, r);
-  const int k = r.split ? 1 : 0;
-  const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[k]));
-  if (r.split) {
-    bp_tc_kernel<true, 1, false><<<grid, kThreads, tc_smem<true>().total, st>>>(a);
-  } else {
-    bp_tc_kernel<false, 1, false><<<grid, kThreads, tc_smem<false>().total, st>>>(a);
-  }
+namespace {
+template <int OP>
+cudaError_t launch_sweep(TcEngine* e, const TcArgs& a, cudaStream_t st) {
+  const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[OP]));
+  bp_tc_kernel<OP, 1, false><<<grid, kThreads, tc_smem<OP>().total, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used) {
-  *used = false;
-  if (!e || !e->valid || r.slot_diff) return cudaErrorInvalidValue;
-  const int k = r.split ? 1 : 0;
-  // two sweeps would write the plain output buffer while the first sweep's readers of
-  // the same buffer may still be running; tags hold 12 bits of sweep index
-  if (!e->persist_ok[k] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
-  TcArgs a = tc_args(e, r);
-  a.nsweeps = nsweeps;
-  cudaError_t err = cudaSuccess;
-  const int groups = r.split ? kGroupsSplit : kGroupsBf16;
+template <int OP>
+cudaError_t launch_persistent(TcEngine* e, const TcArgs& a, cudaStream_t st) {
+  constexpr int groups = OpT<OP>::groups;
   // never more groups than items, so every group has work in every sweep
   const int grid = std::max(1, std::min(e->sm_count, (2 * e->nv + groups - 1) / groups));
   cudaLaunchConfig_t cfg = {};
@@ -1006,16 +1172,38 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
   attr[0].val.cooperative = 1;
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kThreads * groups);
+  cfg.dynamicSmemBytes = groups * tc_smem<OP>().stride;
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (r.split) {
-    cfg.dynamicSmemBytes = kGroupsSplit * tc_smem<true>().stride;
-    err = cudaLaunchKernelEx(&cfg, bp_tc_kernel<true, kGroupsSplit, true>, a);
-  } else {
-    cfg.dynamicSmemBytes = kGroupsBf16 * tc_smem<false>().stride;
-    err = cudaLaunchKernelEx(&cfg, bp_tc_kernel<false, kGroupsBf16, true>, a);
-  }
+  return cudaLaunchKernelEx(&cfg, bp_tc_kernel<OP, groups, true>, a);
+}
+}  // namespace
+
+cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
+  if (!e || !e->valid) return cudaErrorInvalidValue;
+  const int op = tc_op(r);
+  if (op == kOpTf32 && !e->have_tf32) return cudaErrorInvalidValue;
+  TcArgs a = tc_args(e, r);
+  if (op == kOpSplit) return launch_sweep<kOpSplit>(e, a, st);
+  if (op == kOpTf32) return launch_sweep<kOpTf32>(e, a, st);
+  return launch_sweep<kOpBf16>(e, a, st);
+}
+
+cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used) {
+  *used = false;
+  if (!e || !e->valid || r.slot_diff) return cudaErrorInvalidValue;
+  const int op = tc_op(r);
+  if (op == kOpTf32 && !e->have_tf32) return cudaErrorInvalidValue;
+  // two sweeps would write the plain output buffer while the first sweep's readers of
+  // the same buffer may still be running; tags hold 12 bits of sweep index
+  if (!e->persist_ok[op] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
+  TcArgs a = tc_args(e, r);
+  a.nsweeps = nsweeps;
+  cudaError_t err;
+  if (op == kOpSplit) err = launch_persistent<kOpSplit>(e, a, st);
+  else if (op == kOpTf32) err = launch_persistent<kOpTf32>(e, a, st);
+  else err = launch_persistent<kOpBf16>(e, a, st);
   if (err == cudaSuccess) *used = true;
   return err;
 }

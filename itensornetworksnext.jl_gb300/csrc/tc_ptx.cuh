@@ -142,6 +142,28 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T ; issued by a single thread.
+// kind::tf32: A and B TF32 (32-bit storage), D FP32; K = 8 per instruction.
+__host__ __device__ constexpr uint32_t idesc_tf32_f32(int m, int n) {
+  return (1u << 4)                       // D format: F32
+         | (2u << 7)                     // A format: TF32
+         | (2u << 10)                    // B format: TF32
+         | ((uint32_t)(n >> 3) << 17)    // N >> 3
+         | ((uint32_t)(m >> 4) << 24);   // M >> 4
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// FP32 -> TF32 (round to nearest, ties away from zero), as the 32-bit pattern the tensor core reads
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(

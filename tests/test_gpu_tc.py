@@ -3,9 +3,10 @@ CUDA-core path, split-precision recovery, and the 32x32 D=8 log-norm error again
 an FP64 solve.
 
 Stated bounds: one BF16 sweep from the same messages stays within 3e-2 relative per
-message of the FP32 sweep (BF16 operands, FP32 accumulation); one split (hi/lo) sweep
-within 2e-4; the mixed solve (27 BF16 + 3 split sweeps) gives the Bethe log-norm of the
-32x32 periodic D=8 network within 1e-6 relative of the FP64 solve.
+message of the FP32 sweep (BF16 operands, FP32 accumulation); one TF32 sweep within 5e-3;
+one split (hi/lo) sweep within 2e-4; the mixed solves (27 BF16 or TF32 + 3 split sweeps)
+give the Bethe log-norm of the 32x32 periodic D=8 network within 1e-6 relative of the FP64
+solve.
 """
 import numpy as np
 import pytest
@@ -50,15 +51,15 @@ def _one_sweep(g, t, m0, **kw):
         return msg_rel(g, e.messages(), ref)
 
 
-@pytest.mark.parametrize("split,tol", [(False, 3e-2), (True, 2e-4)])
-def test_one_sweep_against_fp32(split, tol):
+@pytest.mark.parametrize("prec,split,tol", [("bf16", False, 3e-2), ("tf32", False, 5e-3), ("bf16", True, 2e-4)])
+def test_one_sweep_against_fp32(prec, split, tol):
     """Non-symmetric messages near the normalised identity (the regime of a BP solve):
     a transposed bra/ket index anywhere would show up as an O(1) error."""
     g, t = _lattice(4, 1)
     rng = np.random.default_rng(5)
     m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
-    err = _one_sweep(g, t, m0, precision="bf16", split_sweeps=1 if split else 0)
-    print(f"split={split}: per-message rel err vs FP32 = {err:.3e}")
+    err = _one_sweep(g, t, m0, precision=prec, split_sweeps=1 if split else 0)
+    print(f"{prec} split={split}: per-message rel err vs FP32 = {err:.3e}")
     assert err < tol
 
 
@@ -74,7 +75,8 @@ def test_split_recovers_ill_conditioned_update():
     assert e_split < 1e-2 and e_split * 20 < e_bf16
 
 
-def test_mixed_logz_32x32_against_fp64():
+@pytest.mark.parametrize("prec", ["bf16", "tf32"])
+def test_mixed_logz_32x32_against_fp64(prec):
     g, t = _lattice(32, 32)
     with BPEngine(g) as e64:
         e64.set_tensors(t)
@@ -85,7 +87,7 @@ def test_mixed_logz_32x32_against_fp64():
     with BPEngine(g) as e:
         e.set_tensors(t.astype(np.float32))
         e.init_messages()
-        r = e.run(maxiter=30, precision="bf16", split_sweeps=3)
+        r = e.run(maxiter=30, precision=prec, split_sweeps=3)
         assert r.iterations == 30
         lz = e.bethe_free_energy()
         lzv = e.logscalars()["logzv"][:, 0]
@@ -93,7 +95,7 @@ def test_mixed_logz_32x32_against_fp64():
         e.run(maxiter=30)
         lz32 = e.bethe_free_energy()
     rel = abs(lz - lz64) / abs(lz64)
-    print(f"log-norm: fp64 {lz64:.12f} mixed {lz:.12f} rel {rel:.3e}; fp32 rel {abs(lz32 - lz64) / abs(lz64):.3e};"
+    print(f"log-norm: fp64 {lz64:.12f} mixed {prec} {lz:.12f} rel {rel:.3e}; fp32 rel {abs(lz32 - lz64) / abs(lz64):.3e};"
           f" max per-site |dlogZv| {np.max(np.abs(lzv - lzv64)):.3e}")
     assert rel <= 1e-6
 
@@ -117,8 +119,9 @@ def test_tc_rejects_unsupported_network():
         assert ei.value.status == 6
 
 
-@pytest.mark.parametrize("L,n,split", [(32, 7, 0), (32, 6, 2), (4, 5, 1)])
-def test_persistent_matches_per_sweep_launches(L, n, split):
+@pytest.mark.parametrize("L,n,split,prec", [(32, 7, 0, "bf16"), (32, 6, 2, "bf16"), (4, 5, 1, "bf16"),
+                                            (32, 5, 0, "tf32"), (4, 6, 3, "tf32")])
+def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     """Without a convergence test the sweeps run as one cooperative launch per precision
     part (per-item completion counters instead of kernel boundaries); with one the engine
     launches once per sweep.  Both run the same per-item arithmetic, so the messages must
@@ -130,10 +133,10 @@ def test_persistent_matches_per_sweep_launches(L, n, split):
     with BPEngine(g) as e:
         e.set_tensors(t.astype(np.float32))
         e.set_messages(m0)
-        r1 = e.run(maxiter=n, precision="bf16", split_sweeps=split)
+        r1 = e.run(maxiter=n, precision=prec, split_sweeps=split)
         a = e.messages()
         e.set_messages(m0)
-        r2 = e.run(maxiter=n, tol=1e-300, precision="bf16", split_sweeps=split)
+        r2 = e.run(maxiter=n, tol=1e-300, precision=prec, split_sweeps=split)
         b = e.messages()
     assert r1.iterations == n and r2.iterations == n
     assert r1.kernel_launches < r2.kernel_launches
