@@ -372,6 +372,8 @@ def run_gpu(args):
         "wall_s": wall,
     }
     if args.extra and world == 1:
+        if mode == "bf16":
+            line["tf32_mixed"] = bench_tf32(device, g, t, t32, args.steps)
         line["grad"] = bench_grad(device)
         line["batched"] = bench_batched(device)
         line["bp_16x16_D4"] = bench_16x16(device)
@@ -379,6 +381,34 @@ def run_gpu(args):
     print(json.dumps(line))
     eng.close()
     return 0
+
+
+def bench_tf32(device, g, t, t32, steps):
+    """The same 32x32 D=8 solve with TF32 tensor-core sweeps (27 TF32 + 3 split), device-timed
+    like the headline value, and its log-norm error against an FP64 GPU solve."""
+    from itn_gb300 import BPEngine
+    e = BPEngine(g, device=device)
+    e.set_tensors(t32)
+    kw = dict(maxiter=SWEEPS, precision="tf32", split_sweeps=SPLIT_SWEEPS)
+    for _ in range(3):
+        e.init_messages()
+        e.run(**kw)
+    ms = []
+    for _ in range(steps):
+        flush_l2(device)
+        e.init_messages()
+        ms.append(e.run(**kw).device_ms)
+    lz = e.bethe_free_energy()
+    e.close()
+    f = BPEngine(g, device=device)
+    f.set_tensors(t)
+    f.init_messages()
+    f.run(maxiter=SWEEPS)
+    lz64 = f.bethe_free_energy()
+    f.close()
+    best = sum(ms) / len(ms)
+    return {"workload": "the headline network and sweeps with TF32 operands", "value": SWEEPS * g.nslots / (best * 1e-3),
+            "unit": UNIT, "ms_per_step": best, "logz_rel_err_vs_fp64": abs(lz - lz64) / abs(lz64)}
 
 
 def bench_grad(device):
