@@ -201,8 +201,16 @@ def cpu_baseline(g, t, seconds=12.0):
         O.bp_sweeps(g, t32, m, 1, nthreads=threads)
         n += 1
     dt = time.perf_counter() - t0
+    # the same sweeps on one host core (bounded sample)
+    n1, t1 = 0, time.perf_counter()
+    while time.perf_counter() - t1 < seconds / 3 or n1 == 0:
+        O.bp_sweeps(g, t32, m, 1, nthreads=1)
+        n1 += 1
+    dt1 = time.perf_counter() - t1
     return {"value": n * g.nslots / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} parallel FP32 sweeps of the 32x32 D=8 norm network ({n * g.nslots} updates, {dt:.1f} s)"}
+            "sample": f"{n} parallel FP32 sweeps of the 32x32 D=8 norm network ({n * g.nslots} updates, {dt:.1f} s)",
+            "one_core": {"value": n1 * g.nslots / dt1, "unit": UNIT,
+                         "sample": f"{n1} sweeps on 1 thread ({dt1:.1f} s)"}}
 
 
 def run_reference(args):
