@@ -132,6 +132,24 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def hbm_roofline(g, mode, sweep_ms, peaks):
+    """Algorithmic bytes of one sweep against the measured copy bandwidth: every site tensor
+    read once in the operand precision (BF16 2 B, TF32/FP32 4 B per entry) and, per message
+    update, its z-1 incoming messages read and the result written (FP32)."""
+    esz = 2 if mode == "bf16" else 4
+    tensor_bytes = esz * float(g.toff[-1])
+    msg_bytes = 0.0
+    for u in range(g.nv):
+        z = int(g.off[u + 1] - g.off[u])
+        for s in range(int(g.off[u]), int(g.off[u + 1])):
+            msg_bytes += 4.0 * float(g.moff[s + 1] - g.moff[s]) * z  # z-1 reads + 1 write
+    total = tensor_bytes + msg_bytes
+    gbs = total / (sweep_ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"algorithmic_bytes_per_sweep": total, "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+            "note": "within a solve the operands stay L2-resident; DRAM traffic per sweep is in traffic"}
+
+
 def ncu_traffic():
     """Per-sweep DRAM bytes of the sweep kernels from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "bp_sweep_32x32_D8.md")
@@ -370,6 +388,9 @@ def run_gpu(args):
                      "traffic": (traffic or {}).get(tkey),
                      "algorithmic_flops_per_sweep": fps,
                      "sweep_ms": sweep_ms,
+                     # the memory side of the same sweep: site tensors once (operand precision)
+                     # plus z-1 message reads and one write per update (FP32)
+                     "hbm": hbm_roofline(g, mode, sweep_ms, peaks),
                      "kernels": "one persistent launch for the BF16 sweeps, one for the split sweeps"
                                 if mode != "native" else "one launch per sweep"},
         "cpu_baseline": cpu_baseline(g, t) if (args.cpu_baseline and world == 1) else None,
