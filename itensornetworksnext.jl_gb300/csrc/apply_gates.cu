@@ -202,13 +202,31 @@ __device__ void herm_eig(T* A, int n, T* V, double* w, T* tmp, Rot* rot, double*
   __syncthreads();
 }
 
+// herm_eig with the working matrices staged in shared memory when they fit (n <= kSmemJacobi):
+// the rounds then read and write on-chip instead of making L2 round trips.
+constexpr int kSmemJacobi = 64;
+template <typename T>
+__device__ void herm_eig_s(T* A, int n, T* V, double* w, T* tmp, Rot* rot, double* red, int* perm, T* sbuf) {
+  if (n > kSmemJacobi) {
+    herm_eig(A, n, V, w, tmp, rot, red, perm);
+    return;
+  }
+  T* sA = sbuf;
+  T* sV = sbuf + kSmemJacobi * kSmemJacobi;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) sA[e] = A[e];
+  __syncthreads();
+  herm_eig(sA, n, sV, w, tmp, rot, red, perm);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) V[e] = sV[e];
+  __syncthreads();
+}
+
 // Gauge of one leg: X = diag(sqrt w+) U^H and X^+ = U diag(1/sqrt w) on w > rtol * w_max.
 template <typename T>
 __device__ void leg_gauge(const T* env, int D, T* X, T* Xp, T* a, T* v, T* tmp, double* w, Rot* rot,
-                          double* red, int* perm) {
+                          double* red, int* perm, T* sbuf) {
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) a[e] = env[e];
   __syncthreads();
-  herm_eig(a, D, v, w, tmp, rot, red, perm);
+  herm_eig_s(a, D, v, w, tmp, rot, red, perm, sbuf);
   const double wmax = fmax(w[0], 0.0);
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
     const int i = e / D, j = e % D;
@@ -281,6 +299,8 @@ __global__ void __launch_bounds__(kGateThreads) gate_kernel(const GateJob* jobs,
   __shared__ double red[32];
   __shared__ int perm[kMaxJacobi];
   __shared__ int s_chi;
+  extern __shared__ __align__(16) unsigned char gate_smem[];
+  T* sbuf = reinterpret_cast<T*>(gate_smem);  // 2 x kSmemJacobi^2 entries for the eigensolver
   const GateJob J = jobs[blockIdx.x];
   GateWs L;
   gate_ws(J, L);
@@ -295,7 +315,7 @@ __global__ void __launch_bounds__(kGateThreads) gate_kernel(const GateJob* jobs,
     for (int j = 0; j < J.nleg[i]; ++j)
       if (J.env_off[i][j] >= 0)
         leg_gauge(envs + J.env_off[i][j], J.leg_dim[i][j], ws + L.X[i][j], ws + L.Xp[i][j], ws + L.ea, ws + L.ev,
-                  ws + L.etmp, wv, rot, red, perm);
+                  ws + L.etmp, wv, rot, red, perm, sbuf);
 
   if (ns == 1) {
     const int d = J.d[0];
@@ -352,7 +372,7 @@ __global__ void __launch_bounds__(kGateThreads) gate_kernel(const GateJob* jobs,
     T* W = ws + L.W[i];
     double* lam = reinterpret_cast<double*>(ws + L.lam[i]);
     gram(a, P[i], n, G);
-    herm_eig(G, n, W, lam, ws + L.etmp, rot, red, perm);
+    herm_eig_s(G, n, W, lam, ws + L.etmp, rot, red, perm, sbuf);
     if (threadIdx.x == 0) {
       int r = 0;
       const double lmax = fmax(lam[0], 0.0);
@@ -405,7 +425,7 @@ __global__ void __launch_bounds__(kGateThreads) gate_kernel(const GateJob* jobs,
     H[e] = acc;
   }
   __syncthreads();
-  herm_eig(H, m, U, s2, ws + L.etmp, rot, red, perm);
+  herm_eig_s(H, m, U, s2, ws + L.etmp, rot, red, perm, sbuf);
   if (threadIdx.x == 0) {
     const double smax2 = fmax(s2[0], 0.0);
     int chi = 0;
@@ -496,11 +516,16 @@ cudaError_t launch_gates(bool complex_data, int n, const GateJob* d_jobs, const 
                          const void* d_ops, void* d_out, double* d_s, int* d_bond, void* d_ws, int max_rank,
                          double cutoff, int normalize, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  const size_t smem = 2 * kSmemJacobi * kSmemJacobi * (complex_data ? sizeof(c128) : sizeof(double));
+  cudaError_t e = complex_data
+                      ? cudaFuncSetAttribute(gate_kernel<c128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                      : cudaFuncSetAttribute(gate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   if (complex_data)
-    gate_kernel<c128><<<n, kGateThreads, 0, st>>>(d_jobs, (const c128*)d_sites, (const c128*)d_envs, (const c128*)d_ops,
+    gate_kernel<c128><<<n, kGateThreads, smem, st>>>(d_jobs, (const c128*)d_sites, (const c128*)d_envs, (const c128*)d_ops,
                                                   (c128*)d_out, d_s, d_bond, (c128*)d_ws, max_rank, cutoff, normalize);
   else
-    gate_kernel<double><<<n, kGateThreads, 0, st>>>(d_jobs, (const double*)d_sites, (const double*)d_envs,
+    gate_kernel<double><<<n, kGateThreads, smem, st>>>(d_jobs, (const double*)d_sites, (const double*)d_envs,
                                                     (const double*)d_ops, (double*)d_out, d_s, d_bond, (double*)d_ws,
                                                     max_rank, cutoff, normalize);
   return cudaGetLastError();
