@@ -163,7 +163,7 @@ struct itn_ctx {
   std::vector<int> slot_dst, slot_eidx;  // per slot: destination vertex, undirected edge index
   DevBuf d_slot_dst, d_slot_eidx;
   // gradient work buffers
-  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_cot, d_stats;
+  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_cot, d_adj;
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
   // data
@@ -1314,7 +1314,7 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
   if (o->adjoint) {
     CK(c->d_g.ensure(std::max<size_t>(mb, 16)));
     CK(c->d_lam.ensure(std::max<size_t>(mb, 16)));
-    CK(c->d_stats.ensure(sizeof(AdjState)));
+    CK(c->d_adj.ensure(sizeof(AdjState)));
     if (int r = adjoint_prepare(c, m, o->normalized)) return r;
     // g = dL/dm, lambda_0 = g
     CK(launch_grad_g(dt, c->d_moff.as<long long>(), c->d_rev.as<int>(), c->d_slot_dst.as<int>(),
@@ -1323,7 +1323,7 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     // adjoint BP: lambda <- g + J^T lambda until the relative change is below tol.  The
     // stopping rule runs on the device (AdjState); iterations are enqueued in chunks and
     // the host reads the state once per chunk (launches after the stop return at once).
-    AdjState* adj = c->d_stats.as<AdjState>();
+    AdjState* adj = c->d_adj.as<AdjState>();
     const int maxit = std::max(o->maxiter, 0);
     CK(launch_adj_reset(adj, o->tol, maxit, c->stream));
     AdjState hs;
