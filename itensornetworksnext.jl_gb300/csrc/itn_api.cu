@@ -553,12 +553,27 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
     }
   }
   {
-    // largest vertices first: persistent CTAs take items round-robin, so a descending
-    // cost order keeps uneven networks balanced
+    // Largest vertices first: persistent CTAs take items round-robin, so a descending cost
+    // order keeps uneven networks balanced.  Among equal sizes, items with the same bond
+    // dimensions in leg order (and the same program) are adjacent, so that the CTAs running
+    // at the same time execute the same D-specialised code paths.
     std::vector<std::pair<int, int>> it;
     for (size_t k = 0; k + 1 < c->items_par.size(); k += 2) it.push_back({c->items_par[k], c->items_par[k + 1]});
+    auto sig_less = [&](int u, int v) {
+      const int64_t zu = c->off[u + 1] - c->off[u], zv = c->off[v + 1] - c->off[v];
+      if (zu != zv) return zu < zv;
+      for (int64_t l = 0; l < zu; ++l) {
+        const int32_t bu = c->bond[c->off[u] + l], bv = c->bond[c->off[v] + l];
+        if (bu != bv) return bu < bv;
+      }
+      return false;
+    };
     std::stable_sort(it.begin(), it.end(), [&](const std::pair<int, int>& x, const std::pair<int, int>& y) {
-      return (c->toff[x.first + 1] - c->toff[x.first]) > (c->toff[y.first + 1] - c->toff[y.first]);
+      const int64_t sx = c->toff[x.first + 1] - c->toff[x.first], sy = c->toff[y.first + 1] - c->toff[y.first];
+      if (sx != sy) return sx > sy;
+      if (sig_less(x.first, y.first)) return true;
+      if (sig_less(y.first, x.first)) return false;
+      return x.second < y.second;
     });
     c->items_par.clear();
     for (auto& p : it) {
