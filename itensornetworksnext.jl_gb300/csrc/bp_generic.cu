@@ -343,7 +343,9 @@ __host__ __device__ inline SmemLayout smem_layout(const GenericArgs& a, int bloc
 
 // ---- the two-layer interpreter ---------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) bp2_kernel(GenericArgs a) {
+// complex64 caps registers at 128 so that small CTAs can co-reside (its D = 8 paths spill a
+// little); the other types keep their full register budget
+__global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2 : 1) bp2_kernel(GenericArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout L = smem_layout<T>(a, blockDim.x, a.gscratch == nullptr);
   T* bufs = a.gscratch ? reinterpret_cast<T*>(a.gscratch) + (size_t)blockIdx.x * a.nbuf * a.buf_elems
@@ -983,6 +985,10 @@ template <typename T>
 int max_active_t(int layers, int block, size_t smem) {
   int n = 0;
   if (layers == 2) {
+    // complex64 (small CTAs, capped registers): all of the unified L1 / shared memory as
+    // shared memory, so that more CTAs co-reside; the real types keep the default split
+    if (is_cplx<T>::value && sizeof(T) == 8)
+      cudaFuncSetAttribute(bp2_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     cudaFuncSetAttribute(bp2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_kernel<T>, block, smem);
   } else {
