@@ -120,14 +120,15 @@ def test_tc_rejects_unsupported_network():
 
 
 @pytest.mark.parametrize("L,n,split,prec", [(32, 7, 0, "bf16"), (32, 6, 2, "bf16"), (4, 5, 1, "bf16"),
-                                            (3, 9, 0, "bf16"), (32, 5, 0, "tf32"), (4, 6, 3, "tf32")])
+                                            (3, 9, 0, "bf16"), (48, 5, 1, "bf16"), (32, 5, 0, "tf32"),
+                                            (4, 6, 3, "tf32")])
 def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     """Without a convergence test the sweeps run as one cooperative launch per precision
     part (per-item completion counters instead of kernel boundaries); with one the engine
     launches once per sweep.  Both run the same per-item arithmetic, so the messages must
     agree bit for bit -- a missed dependency would read a stale or half-written message.
-    32x32 has more half-vertex items (2048) than groups, 4x4 and 3x3 (the smallest periodic
-    lattice, one CTA) fewer."""
+    32x32 and 48x48 (about four items per group per sweep) have more half-vertex items than
+    groups, 4x4 and 3x3 (the smallest periodic lattice, one CTA) fewer."""
     g, t = _lattice(L, 11)
     rng = np.random.default_rng(12)
     m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
