@@ -225,6 +225,19 @@ def incoming_messages(cache: MessageCache, edge):
     return [cache[e] for e in cache.edges() if e[1] == u and e[0] != v]
 
 
+def insertlink(tn: ITensorNetwork, e):
+    """insertlink!(tn, e) (abstracttensornetwork.jl:121-133): joins the two vertices of the
+    edge e by a new link of dimension 1 (an all-ones factor on both tensors); in place,
+    returns tn."""
+    u, v = e
+    link = Index(1, uniquename())
+    for w in (u, v):
+        t = tn.tensors[w]
+        tn.tensors[w] = ITensor(t.data[..., None], list(t.inds) + [link])
+    tn.__init__(tn.tensors)
+    return tn
+
+
 def message_environment(f, nn: NormNetwork):
     """One D x D operator per directed edge (codomain = bra link, domain = ket link),
     mapped by f: ``"one"`` -> identity, ``"ones"`` -> all ones, or a callable on the
@@ -594,9 +607,32 @@ def _trunc_args(trunc):
     return int(trunc), None
 
 
+def operator_message_cache(nn: NormNetwork, messages: MessageCache):
+    """BP messages (bra and ket link indices) as operators with codomain = bra names and
+    domain = ket names: the environment format apply_operator consumes
+    (test/test_apply_operator.jl:42-53; message_environment, messagecache.jl:205-229)."""
+    out = {}
+    for (u, v) in messages.keys():
+        t = messages[(u, v)]
+        ket = nn.ket.linknames(u, v)
+        bra = [nn.bra(n) for n in ket]
+        dims = {i.name: i.dim for i in t.inds}
+        data = t.permute(bra + ket)
+        out[(u, v)] = Operator(data, [Index(dims[n], n) for n in bra], [Index(dims[n], n) for n in ket])
+    return MessageCache(out)
+
+
 def _env_matrix(env: MessageCache, edge, ket_names):
     """The D x D matrix M[bra, ket] of env[edge], ket axes in the order of ket_names."""
     t = env[edge]
+    if isinstance(t, Operator):
+        # codomain (bra) x domain (ket), domain matched to ket_names by position
+        pair = dict(zip(t.domain, t.codomain))
+        if set(pair) != set(ket_names):
+            raise ItnArgumentError(1, f"environment of {edge} does not carry the link names")
+        arr = t.permute([pair[n] for n in ket_names] + list(ket_names))
+        D = int(np.prod([_dim_of(t, n) for n in ket_names]))
+        return arr.reshape(D, D)
     k = len(t.inds) // 2
     bra, ket = list(t.dimnames[:k]), list(t.dimnames[k:])
     if set(ket) != set(ket_names):

@@ -190,3 +190,74 @@ def test_rejects_bad_descriptors():
         assert st == L.ITN_ERR_ARG
         with pytest.raises(ItnArgumentError, match="out of range"):
             L.check(ctx.ctx, st)
+
+
+# ---- the reference's own flow: random_state built by gate layers, operator environments ---------
+def _random_state(rng, dtype, edges, nlayers=2, trunc=4, d=3):
+    """random_state (test/test_apply_operator.jl:19-40): a product state, a dimension-1 link
+    per edge (insertlink!), then nlayers layers of random two-site gates over the edges,
+    each applied with apply_operator and truncation to rank ``trunc`` from identity
+    environments."""
+    vs = sorted({v for e in edges for v in e})
+    s = {v: N.Index(d) for v in vs}
+    tn = N.tensornetwork(lambda v: N.ITensor(_randn(rng, (d,), dtype), [s[v]]), vs)
+    for e in edges:
+        N.insertlink(tn, e)
+    env = N.message_environment("one", N.NormNetwork(tn))
+    for _ in range(nlayers):
+        for (u, v) in edges:
+            tn, env = N.apply_operator(_op(rng, dtype, [s[u], s[v]]), tn, env, trunc=trunc)
+    return tn, [s[v] for v in vs]
+
+
+def _operator_env(tn):
+    nn = N.NormNetwork(tn)
+    env = N.beliefpropagation(nn, N.message_environment("ones", nn),
+                              stopping_criterion=dict(maxiter=100, tol=1e-13))
+    return N.operator_message_cache(nn, env)
+
+
+_CYCLE = [(0, 1), (1, 2), (2, 3), (0, 3)]
+_PATH = [(0, 1), (1, 2), (2, 3)]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex128])
+def test_reference_flow_untruncated_gates_are_exact(dtype):
+    rng = np.random.default_rng(321)
+    tn, s = _random_state(rng, dtype, _CYCLE)
+    assert all(i.dim <= 4 for v in tn.vertices() for i in tn[v].inds)
+    env = _operator_env(tn)
+    psi = _dense(tn, s)
+    g1 = _op(rng, dtype, [s[1]])
+    gated, _ = N.apply_operator(g1, tn, env)
+    assert _rel(_dense(gated, s), np.einsum("ts,asxb->atxb", g1.data, psi)) < _rtol(dtype)
+    g2 = _op(rng, dtype, [s[1], s[2]])
+    gated, _ = N.apply_operator(g2, tn, env)
+    assert _rel(_dense(gated, s), np.einsum("xyst,astb->axyb", g2.data, psi)) < _rtol(dtype)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex128])
+def test_reference_flow_truncated_gate_matches_optimal_svd(k, dtype):
+    rng = np.random.default_rng(321)
+    tn, s = _random_state(rng, dtype, _PATH)
+    env = _operator_env(tn)
+    gate = _op(rng, dtype, [s[1], s[2]])
+    full = np.einsum("xyst,astb->axyb", gate.data, _dense(tn, s))
+    u, sv, vh = np.linalg.svd(full.reshape(9, 9).astype(np.complex128))
+    want = ((u[:, :k] * sv[:k]) @ vh[:k]).reshape(full.shape)
+    gated, _ = N.apply_operator(gate, tn, env, trunc=k)
+    assert _rel(_dense(gated, s), want) < _rtol(dtype)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex128])
+def test_reference_flow_apply_operators_sequence(dtype):
+    rng = np.random.default_rng(321)
+    tn, s = _random_state(rng, dtype, _CYCLE)
+    env = _operator_env(tn)
+    g1 = _op(rng, dtype, [s[1], s[2]])
+    g2 = _op(rng, dtype, [s[2], s[3]])
+    gated, _ = N.apply_operators([g1, g2], tn, env)
+    want = np.einsum("xyst,astb->axyb", g1.data, _dense(tn, s))
+    want = np.einsum("xyst,abst->abxy", g2.data, want)
+    assert _rel(_dense(gated, s), want) < _rtol(dtype)

@@ -96,3 +96,35 @@ def test_apply_operator_argument_errors():
     op3 = N.operator(np.ones((2,) * 6), [N.Index(2) for _ in range(3)], s)
     with pytest.raises(N.ItnArgumentError, match="3-site gate decomposition not implemented"):
         N.apply_operator(op3, tn, None)
+
+
+def test_insertlink_and_operator_environments():
+    """insertlink! (abstracttensornetwork.jl:121-133) adds a dimension-1 link and so an edge;
+    operator_message_cache (test/test_apply_operator.jl:42-53) turns messages into
+    operators (codomain = bra link names, domain = ket link names) that apply_operator
+    reads as the same D x D environment matrices as the messages themselves."""
+    rng = np.random.default_rng(5)
+    s = [N.Index(2) for _ in range(3)]
+    tn = N.tensornetwork(lambda v: N.ITensor(rng.standard_normal(2), [s[v]]), range(3))
+    assert tn.edges() == []
+    N.insertlink(tn, (0, 1))
+    N.insertlink(tn, (1, 2))
+    assert sorted(tn.edges()) == [(0, 1), (1, 2)]
+    assert [i.dim for i in tn[1].inds] == [2, 1, 1]
+    np.testing.assert_array_equal(tn[1].data.ravel(), tn[1].data[:, 0, 0])
+    # a network with a two-name bond: the conversion must keep the names paired
+    a, b, c = N.Index(2), N.Index(3), N.Index(2)
+    tn2 = N.ITensorNetwork({0: N.ITensor(rng.standard_normal((2, 3, 2)), [a, b, s[0]]),
+                            1: N.ITensor(rng.standard_normal((3, 2, 2, 2)), [b, a, c, s[1]]),
+                            2: N.ITensor(rng.standard_normal((2, 2)), [c, s[2]])})
+    nn = N.NormNetwork(tn2)
+    msgs = N.message_environment(lambda m: rng.standard_normal(m.shape), nn)
+    ops = N.operator_message_cache(nn, msgs)
+    assert set(ops.keys()) == set(msgs.keys())
+    for e in msgs.keys():
+        names = nn.ket.linknames(*e)
+        op = ops[e]
+        assert isinstance(op, N.Operator)
+        assert op.domain == tuple(names) and op.codomain == tuple(nn.bra(n) for n in names)
+        for order in (names, names[::-1]):
+            np.testing.assert_array_equal(N._env_matrix(ops, e, order), N._env_matrix(msgs, e, order))
