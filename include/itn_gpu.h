@@ -143,7 +143,7 @@ int32_t itn_iterate_diff(itn_ctx *ctx, int32_t dtype, const void *m1, const void
  * in the context dtype (may be NULL).  logzv / logze: (re, im) pairs in FP64 (may be
  * NULL).  totals: (re, im) of sum log Zv - sum log Ze per network.  flags per network:
  * bit0 any Re Zv < 0, bit1 any Re Ze < 0, bit2 any Ze == 0 (bethe_free_energy returns
- * -Inf then). */
+ * -Inf then).  Every output may be NULL; only the requested ones are copied back. */
 int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *logze,
                        double *totals, int32_t *flags);
 

@@ -796,6 +796,102 @@ __global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
   if (a.conv && a.fused_step) conv_finish_cta(a.conv);
 }
 
+// ---- vertex scalars of norm-network vertices with d = 2 and four legs of dimension 8 -------
+// Z_u = sum_s <A_s| m0 (x) m1 (x) m2 (x) m3 |A_s> (vertex_scalar, messagecache.jl:139-150),
+// with A_s viewed as a 64 x 64 matrix over p = (k0, k1), q = (k2, k3), as two passes of
+// 8 x 8 matrix products; one CTA of 128 threads per vertex:
+//   pass 1, thread (s, p):  W_s[p][(b2 b3)] = sum_{k2,k3} m2[b2,k2] A_s[p][(k2 k3)] m3[b3,k3]
+//   pass 2, thread (s, c):  V_s[(b0 b1)][c] = sum_{k0,k1} m0[b0,k0] W_s[(k0 k1)][c] m1[b1,k1]
+//   Z_u = sum_{s,b,c} conj(A_s[b][c]) V_s[b][c]
+// (m_l[b][k]: bra index b, ket index k, the message into u on leg l).  The same 262,144
+// multiply-adds per vertex as the interpreter's leg-by-leg absorption, but with every
+// 8 x 8 product in registers and a single pass through shared memory (row stride 65:
+// conflict-free row writes in pass 1 and column reads in pass 2).
+constexpr int kVsLd = 65;
+
+template <typename T>
+size_t vertex_scalar_d8_smem() {
+  return (size_t)(128 * kVsLd + 256 + 4) * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) vertex_scalar_d8_kernel(const int* __restrict__ rev,
+                                                               const long long* __restrict__ moff,
+                                                               const long long* __restrict__ toff,
+                                                               const T* __restrict__ tens,
+                                                               const T* __restrict__ msgs, T* __restrict__ zv) {
+  extern __shared__ __align__(16) unsigned char vs_smem[];
+  T* w = reinterpret_cast<T*>(vs_smem);  // [2 x 64][kVsLd]
+  T* m = w + 128 * kVsLd;                // [4][64]
+  T* red = m + 256;                      // [4]
+  const int u = blockIdx.x, t = threadIdx.x;
+  const int s = t >> 6, r = t & 63;
+  for (int j = t; j < 256; j += 128) m[j] = msgs[moff[rev[4 * u + (j >> 6)]] + (j & 63)];
+  __syncthreads();
+  const T* A = tens + toff[u] + (size_t)s * 4096;
+  {
+    T W[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) W[i] = tzero<T>();
+    const T* row = A + r * 64;
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) {
+      T x[8], y[8];
+#pragma unroll
+      for (int k3 = 0; k3 < 8; ++k3) x[k3] = row[k2 * 8 + k3];
+#pragma unroll
+      for (int b3 = 0; b3 < 8; ++b3) {
+        T acc = tzero<T>();
+#pragma unroll
+        for (int k3 = 0; k3 < 8; ++k3) acc = fmac(x[k3], m[192 + b3 * 8 + k3], acc);
+        y[b3] = acc;
+      }
+#pragma unroll
+      for (int b2 = 0; b2 < 8; ++b2) {
+        const T c2 = m[128 + b2 * 8 + k2];
+#pragma unroll
+        for (int b3 = 0; b3 < 8; ++b3) W[b2 * 8 + b3] = fmac(y[b3], c2, W[b2 * 8 + b3]);
+      }
+    }
+    T* wr = w + (s * 64 + r) * kVsLd;
+#pragma unroll
+    for (int c = 0; c < 64; ++c) wr[c] = W[c];
+  }
+  __syncthreads();
+  T part = tzero<T>();
+  {
+    T V[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) V[i] = tzero<T>();
+    const T* col = w + s * 64 * kVsLd + r;  // W_s[p][c = r] at col[p * kVsLd]
+#pragma unroll
+    for (int k0 = 0; k0 < 8; ++k0) {
+      T x[8], y[8];
+#pragma unroll
+      for (int k1 = 0; k1 < 8; ++k1) x[k1] = col[(k0 * 8 + k1) * kVsLd];
+#pragma unroll
+      for (int b1 = 0; b1 < 8; ++b1) {
+        T acc = tzero<T>();
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) acc = fmac(x[k1], m[64 + b1 * 8 + k1], acc);
+        y[b1] = acc;
+      }
+#pragma unroll
+      for (int b0 = 0; b0 < 8; ++b0) {
+        const T c0 = m[b0 * 8 + k0];
+#pragma unroll
+        for (int b1 = 0; b1 < 8; ++b1) V[b0 * 8 + b1] = fmac(y[b1], c0, V[b0 * 8 + b1]);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < 64; ++b) part = fmac(V[b], conjx(A[b * 64 + r]), part);
+  }
+  part = warp_sum(part);
+  if ((t & 31) == 0) red[t >> 5] = part;
+  __syncthreads();
+  if (t == 0) zv[u] = add(add(red[0], red[1]), add(red[2], red[3]));
+}
+
 // ---- edge scalars: Z_e = sum_j m_{u->v}[j] * m_{v->u}[j]  (messagecache.jl:153-157) -----
 template <typename T>
 __global__ void edge_scalar_kernel(const long long* moff, const int* rev, const int* eslots,
@@ -826,13 +922,32 @@ __device__ __forceinline__ void log2d(T z, double& re, double& im) {
   }
 }
 
-// One block per network: FP64 logs of vertex/edge scalars and the Bethe sum
-// log Z = sum_v log Z_v - sum_e log Z_e (messagecache.jl:185-201).
+// FP64 logs of every vertex and edge scalar, one thread each (the double-precision log is
+// slow on this part, so the logs are spread over the whole grid rather than summed by one
+// block per network).
+template <typename T>
+__global__ void log_scalars_kernel(const T* zv, const T* ze, int nv, int ne, double* logzv, double* logze) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double re, im;
+  if (j < nv) {
+    log2d(zv[j], re, im);
+    logzv[2 * j] = re;
+    logzv[2 * j + 1] = im;
+  } else if (j < nv + ne) {
+    const int e = j - nv;
+    log2d(ze[e], re, im);
+    logze[2 * e] = re;
+    logze[2 * e + 1] = im;
+  }
+}
+
+// One block per network: the Bethe sum log Z = sum_v log Z_v - sum_e log Z_e
+// (messagecache.jl:185-201) over the logs above, in a fixed order.
 // flags per net: bit0 any Re Z_v < 0, bit1 any Re Z_e < 0, bit2 any Z_e == 0.
 template <typename T>
 __global__ void logsum_kernel(const T* zv, const T* ze, const int* voff, const int* vlist,
-                              const int* eoff, const int* elist, double* logzv, double* logze,
-                              double* totals, int* flags) {
+                              const int* eoff, const int* elist, const double* logzv,
+                              const double* logze, double* totals, int* flags) {
   __shared__ double sre[32], sim[32];
   __shared__ int sfl[32];
   const int net = blockIdx.x;
@@ -840,24 +955,16 @@ __global__ void logsum_kernel(const T* zv, const T* ze, const int* voff, const i
   int fl = 0;
   for (int j = voff[net] + threadIdx.x; j < voff[net + 1]; j += blockDim.x) {
     const int v = vlist[j];
-    double re, im;
-    log2d(zv[v], re, im);
-    logzv[2 * v] = re;
-    logzv[2 * v + 1] = im;
     if (re_d(zv[v]) < 0) fl |= 1;
-    are += re;
-    aim += im;
+    are += logzv[2 * v];
+    aim += logzv[2 * v + 1];
   }
   for (int j = eoff[net] + threadIdx.x; j < eoff[net + 1]; j += blockDim.x) {
     const int e = elist[j];
-    double re, im;
-    log2d(ze[e], re, im);
-    logze[2 * e] = re;
-    logze[2 * e + 1] = im;
     if (re_d(ze[e]) < 0) fl |= 2;
     if (is_zero(ze[e])) fl |= 4;
-    are -= re;
-    aim -= im;
+    are -= logze[2 * e];
+    aim -= logze[2 * e + 1];
   }
   are = warp_sum_d(are);
   aim = warp_sum_d(aim);
@@ -1033,6 +1140,29 @@ cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg
   ITN_DISPATCH(dtype, return launch_generic_t<T>(a, cfg, st));
 }
 
+template <typename T>
+cudaError_t launch_vertex_scalars_d8_t(int nv, const int* rev, const long long* moff, const long long* toff,
+                                       const void* tens, const void* msgs, void* zv, cudaStream_t st) {
+  const size_t smem = vertex_scalar_d8_smem<T>();
+  cudaError_t e = cudaFuncSetAttribute(vertex_scalar_d8_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  vertex_scalar_d8_kernel<T><<<nv, 128, smem, st>>>(rev, moff, toff, reinterpret_cast<const T*>(tens),
+                                                    reinterpret_cast<const T*>(msgs), reinterpret_cast<T*>(zv));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vertex_scalars_d8(int dtype, int nv, const int* rev, const long long* moff,
+                                     const long long* toff, const void* tens, const void* msgs, void* zv,
+                                     cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  switch (dtype) {
+    case DT_F32: return launch_vertex_scalars_d8_t<float>(nv, rev, moff, toff, tens, msgs, zv, st);
+    case DT_C64: return launch_vertex_scalars_d8_t<c64>(nv, rev, moff, toff, tens, msgs, zv, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,
                                 const int* eslots, int n_e, const void* msgs, void* ze_out,
                                 cudaStream_t st) {
@@ -1049,10 +1179,13 @@ cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int
                           const int* voff, const int* vlist, const int* eoff, const int* elist,
                           int n_nets, double* logzv, double* logze, double* totals, int* flags,
                           cudaStream_t st) {
-  (void)nv;
-  (void)ne;
   if (n_nets <= 0) return cudaSuccess;
-  ITN_DISPATCH(dtype, logsum_kernel<T><<<n_nets, 256, 0, st>>>(
+  if (nv + ne > 0) {
+    ITN_DISPATCH(dtype, log_scalars_kernel<T><<<(nv + ne + 127) / 128, 128, 0, st>>>(
+                            reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), nv, ne, logzv, logze);
+                 break);
+  }
+  ITN_DISPATCH(dtype, logsum_kernel<T><<<n_nets, 1024, 0, st>>>(
                           reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), voff,
                           vlist, eoff, elist, logzv, logze, totals, flags);
                return cudaGetLastError());

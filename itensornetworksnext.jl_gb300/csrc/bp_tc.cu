@@ -607,40 +607,83 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   if (a.conv && !skip) conv_finish_cta(a.conv, nsweeps);
 }
 
-// ---- operand image: per vertex [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ the same for lo] ---------
+// ---- operand images -----------------------------------------------------------------------
+// One CTA per (vertex u, physical index s): the 64 x 64 FP32 block A_s[p][q] is staged in
+// shared memory (row stride 65 floats, so that row and column reads are both free of bank
+// conflicts) and written out in 16-byte chunks of the core-matrix layout, in which chunk i
+// of a block sits at byte 16 i: row r = 8 (i >> 6) + (i & 7), K-entries 8 ((i >> 3) & 7)
+// .. +7 for BF16 (TF32: r = 8 (i >> 7) + (i & 7), K-entries 4 ((i >> 3) & 15) .. +3).
+// Both layouts (A_pq: row p, K = q; A_qp: row q, K = p) come from the same staged block.
+constexpr int kImgLd = 65;
+
+__device__ __forceinline__ void stage_block(const float* __restrict__ tens, int u, int s, float* t) {
+  const float4* src = reinterpret_cast<const float4*>(tens + (size_t)u * 8192 + (size_t)s * 4096);
+  for (int j = threadIdx.x; j < 1024; j += blockDim.x) {
+    const float4 v = __ldcs(src + j);
+    float* d = t + (j >> 4) * kImgLd + (j & 15) * 4;
+    d[0] = v.x;
+    d[1] = v.y;
+    d[2] = v.z;
+    d[3] = v.w;
+  }
+  __syncthreads();
+}
+
+// BF16 image, per vertex [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ the same for lo]
 template <bool SPLIT>
-__global__ void tc_image_kernel(const float* __restrict__ tens, int nv, unsigned char* __restrict__ img) {
+__global__ void __launch_bounds__(256) tc_image_kernel(const float* __restrict__ tens, int nv,
+                                                       unsigned char* __restrict__ img) {
   constexpr uint32_t bytes = (SPLIT ? 8 : 4) * kBlk;
-  const long long total = (long long)nv * 8192;
-  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
-       j += (long long)gridDim.x * blockDim.x) {
-    const int u = (int)(j >> 13), e = (int)(j & 8191);
-    const int s = e >> 12, p = (e >> 6) & 63, q = e & 63;
-    float hi, lo;
-    split_bf16(tens[j], hi, lo);
-    unsigned char* base = img + (size_t)u * bytes;
-    const __nv_bfloat16 bh = __float2bfloat16_rn(hi), bl = __float2bfloat16_rn(lo);
-    *reinterpret_cast<__nv_bfloat16*>(base + s * kBlk + blk_off(p, q)) = bh;
-    *reinterpret_cast<__nv_bfloat16*>(base + 2 * kBlk + s * kBlk + blk_off(q, p)) = bh;
+  __shared__ float t[64 * kImgLd];
+  const int u = blockIdx.x >> 1, s = blockIdx.x & 1;
+  if (u >= nv) return;
+  stage_block(tens, u, s, t);
+  unsigned char* base = img + (size_t)u * bytes + (size_t)s * kBlk;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+    const int r = ((i >> 6) << 3) + (i & 7), k0 = ((i >> 3) & 7) << 3;
+    uint32_t hpq[4], hqp[4], lpq[4], lqp[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float h0, l0, h1, l1;
+      split_bf16(t[r * kImgLd + k0 + 2 * j], h0, l0);
+      split_bf16(t[r * kImgLd + k0 + 2 * j + 1], h1, l1);
+      hpq[j] = pack_bf16(h0, h1);
+      lpq[j] = pack_bf16(l0, l1);
+      split_bf16(t[(k0 + 2 * j) * kImgLd + r], h0, l0);
+      split_bf16(t[(k0 + 2 * j + 1) * kImgLd + r], h1, l1);
+      hqp[j] = pack_bf16(h0, h1);
+      lqp[j] = pack_bf16(l0, l1);
+    }
+    const size_t o = (size_t)i * 16;
+    *reinterpret_cast<uint4*>(base + o) = make_uint4(hpq[0], hpq[1], hpq[2], hpq[3]);
+    *reinterpret_cast<uint4*>(base + 2 * kBlk + o) = make_uint4(hqp[0], hqp[1], hqp[2], hqp[3]);
     if constexpr (SPLIT) {
-      *reinterpret_cast<__nv_bfloat16*>(base + 4 * kBlk + s * kBlk + blk_off(p, q)) = bl;
-      *reinterpret_cast<__nv_bfloat16*>(base + 6 * kBlk + s * kBlk + blk_off(q, p)) = bl;
+      *reinterpret_cast<uint4*>(base + 4 * kBlk + o) = make_uint4(lpq[0], lpq[1], lpq[2], lpq[3]);
+      *reinterpret_cast<uint4*>(base + 6 * kBlk + o) = make_uint4(lqp[0], lqp[1], lqp[2], lqp[3]);
     }
   }
 }
 
-// ---- TF32 operand image: per vertex [A_pq(s=0,1) | A_qp(s=0,1)], 16 KB per block ----------
-__global__ void tc_image_tf32_kernel(const float* __restrict__ tens, int nv, unsigned char* __restrict__ img) {
+// TF32 image, per vertex [A_pq(s=0,1) | A_qp(s=0,1)], 16 KB per block
+__global__ void __launch_bounds__(256) tc_image_tf32_kernel(const float* __restrict__ tens, int nv,
+                                                            unsigned char* __restrict__ img) {
   constexpr uint32_t blk = OpT<kOpTf32>::blk;
-  const long long total = (long long)nv * 8192;
-  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
-       j += (long long)gridDim.x * blockDim.x) {
-    const int u = (int)(j >> 13), e = (int)(j & 8191);
-    const int s = e >> 12, p = (e >> 6) & 63, q = e & 63;
-    const uint32_t v = ptx::to_tf32(tens[j]);
-    unsigned char* base = img + (size_t)u * OpT<kOpTf32>::img_vertex;
-    *reinterpret_cast<uint32_t*>(base + s * blk + op_off<kOpTf32>(p, q)) = v;
-    *reinterpret_cast<uint32_t*>(base + 2 * blk + s * blk + op_off<kOpTf32>(q, p)) = v;
+  __shared__ float t[64 * kImgLd];
+  const int u = blockIdx.x >> 1, s = blockIdx.x & 1;
+  if (u >= nv) return;
+  stage_block(tens, u, s, t);
+  unsigned char* base = img + (size_t)u * OpT<kOpTf32>::img_vertex + (size_t)s * blk;
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+    const int r = ((i >> 7) << 3) + (i & 7), k0 = ((i >> 3) & 15) << 2;
+    uint32_t pq[4], qp[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      pq[j] = ptx::to_tf32(t[r * kImgLd + k0 + j]);
+      qp[j] = ptx::to_tf32(t[(k0 + j) * kImgLd + r]);
+    }
+    const size_t o = (size_t)i * 16;
+    *reinterpret_cast<uint4*>(base + o) = make_uint4(pq[0], pq[1], pq[2], pq[3]);
+    *reinterpret_cast<uint4*>(base + 2 * blk + o) = make_uint4(qp[0], qp[1], qp[2], qp[3]);
   }
 }
 
@@ -976,6 +1019,7 @@ struct TcEngine {
   int sm_count = 0;
   int occ[kNumOps] = {0, 0, 0};
   bool persist_ok[kNumOps] = {false, false, false};  // cooperative grid of sm_count CTAs fits
+  bool configured = false;  // kernel attributes set and residency measured (once per engine)
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -1067,7 +1111,6 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
     if (err != cudaSuccess) return err;
   }
   cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
-  const int grid = (int)std::min<long long>((nv * 8192 + 255) / 256, 4096);
   if (!e->valid) {
     // the BF16 hi/lo image serves the BF16 sweeps and the split sweeps of every mode
     const size_t split_bytes = (size_t)nv * OpT<kOpSplit>::img_vertex;
@@ -1078,15 +1121,19 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       if (err != cudaSuccess) return err;
       e->image_bytes = split_bytes;
     }
-    tc_image_kernel<true><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image);
+    tc_image_kernel<true><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv,
+                                                              e->image);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    int smem_sm = 0, regs_sm = 0;
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-    tc_configure<kOpBf16>(e, smem_sm, regs_sm);
-    tc_configure<kOpSplit>(e, smem_sm, regs_sm);
-    tc_configure<kOpTf32>(e, smem_sm, regs_sm);
+    if (!e->configured) {
+      int smem_sm = 0, regs_sm = 0;
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+      cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+      tc_configure<kOpBf16>(e, smem_sm, regs_sm);
+      tc_configure<kOpSplit>(e, smem_sm, regs_sm);
+      tc_configure<kOpTf32>(e, smem_sm, regs_sm);
+      e->configured = true;
+    }
     if (getenv("ITN_DEBUG"))
       fprintf(stderr, "[itn] tc residency: bf16 %d, split %d, tf32 %d CTAs/SM; persistent %d/%d/%d; sms %d\n",
               e->occ[0], e->occ[1], e->occ[2], (int)e->persist_ok[0], (int)e->persist_ok[1],
@@ -1120,7 +1167,8 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       if (err != cudaSuccess) return err;
       e->image_tf32_bytes = tf32_bytes;
     }
-    tc_image_tf32_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv, e->image_tf32);
+    tc_image_tf32_kernel<<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv,
+                                                             e->image_tf32);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     e->have_tf32 = true;
@@ -1130,7 +1178,8 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   e->d_rev = d_rev;
   e->d_moff = d_moff;
   e->valid = true;
-  return cudaStreamSynchronize(st);
+  // the image kernels are ordered before the sweeps on the same stream: no host wait
+  return cudaGetLastError();
 }
 
 static int tc_op(const TcRun& r) { return r.split ? kOpSplit : (r.precision == 2 ? kOpTf32 : kOpBf16); }
@@ -1208,12 +1257,7 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
   return err;
 }
 
-int tc_error_flag(TcEngine* e, cudaStream_t st) {
-  if (!e || !e->d_err) return 0;
-  int h = 0;
-  cudaMemcpyAsync(&h, e->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaStreamSynchronize(st);
-  return h;
-}
+const int* tc_err_ptr(const TcEngine* e) { return e ? e->d_err : nullptr; }
+
 
 }  // namespace itn

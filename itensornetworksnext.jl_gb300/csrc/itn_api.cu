@@ -146,6 +146,7 @@ struct itn_ctx {
   int max_d2 = 1;
   int64_t max_tensor = 1;
   std::vector<int> eslots;  // undirected edges: slot < rev[slot]
+  bool scal_d8 = false;     // every vertex: two layers, d = 2, four legs of dimension 8
 
   // network (device)
   DevBuf d_off, d_rev, d_bond, d_phys, d_toff, d_moff, d_eslots;
@@ -175,6 +176,9 @@ struct itn_ctx {
   DevBuf d_zv, d_ze, d_logzv, d_logze, d_tot, d_flags;
   DevBuf d_scratch;
   DevBuf d_stage;  // upload staging
+  // pinned host staging for small results read back together (one copy, one sync)
+  void* h_pin = nullptr;
+  size_t h_pin_bytes = 0;
 
   // convergence state (device): dmax, nan, done, at, iters, delta, counter
   DevBuf d_slot_diff, d_state;
@@ -190,6 +194,7 @@ struct itn_ctx {
 
   ~itn_ctx() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (h_pin) cudaFreeHost(h_pin);
     if (tc) tc_destroy(tc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -224,6 +229,21 @@ int cuda_fail(itn_ctx* c, cudaError_t e, const char* what) {
 int ensure_device(itn_ctx* c) {
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  return ITN_OK;
+}
+
+// Pinned host staging of at least `bytes` (grown, never shrunk).
+int ensure_pinned(itn_ctx* c, size_t bytes) {
+  if (bytes <= c->h_pin_bytes) return ITN_OK;
+  if (c->h_pin) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFreeHost(c->h_pin);
+    c->h_pin = nullptr;
+    c->h_pin_bytes = 0;
+  }
+  const size_t want = std::max<size_t>(bytes, 4096);
+  CK(cudaMallocHost(&c->h_pin, want));
+  c->h_pin_bytes = want;
   return ITN_OK;
 }
 
@@ -580,6 +600,12 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       c->items_par.push_back(p.first);
       c->items_par.push_back(p.second);
     }
+  }
+  c->scal_d8 = layers == 2 && nv > 0;
+  for (int64_t u = 0; u < nv && c->scal_d8; ++u) {
+    if (c->off[u] != 4 * u || c->off[u + 1] != 4 * u + 4 || c->phys[u] != 2) c->scal_d8 = false;
+    for (int64_t q = c->off[u]; q < c->off[u + 1] && c->scal_d8; ++q)
+      if (c->bond[q] != 8) c->scal_d8 = false;
   }
   c->tuned_block.assign(4, 0);
   if (c->prog_host.empty()) c->prog_host.push_back(0);
@@ -1067,6 +1093,13 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   float total_ms = 0.f;
   ConvState hs;
   memset(&hs, 0, sizeof(hs));
+  // the convergence state and the tensor-core error flag come back in one pinned area
+  const size_t err_at = (sizeof(ConvState) + 15) & ~size_t(15);
+  if (int r = ensure_pinned(c, err_at + 16)) return r;
+  ConvState* h_state = static_cast<ConvState*>(c->h_pin);
+  int* h_tcerr = reinterpret_cast<int*>(static_cast<unsigned char*>(c->h_pin) + err_at);
+  const int* d_tcerr = o->precision != ITN_PREC_NATIVE ? tc_err_ptr(c->tc) : nullptr;
+  *h_tcerr = 0;
   while (issued < cap) {
     const int n = (int)std::min<int64_t>(chunk, cap - issued);
     if (grow) chunk = std::min(2 * chunk, 64);
@@ -1103,8 +1136,10 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(cudaGraphLaunch(exec, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
-    CK(cudaMemcpyAsync(&hs, conv(c), sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h_state, conv(c), sizeof(ConvState), cudaMemcpyDeviceToHost, c->stream));
+    if (d_tcerr) CK(cudaMemcpyAsync(h_tcerr, d_tcerr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    hs = *h_state;
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     total_ms += ms;
@@ -1112,8 +1147,7 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     issued += n;
     if (hs.done) break;
   }
-  if (o->precision != ITN_PREC_NATIVE && tc_error_flag(c->tc, c->stream))
-    return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
+  if (d_tcerr && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
   // messages now live in buffer (cur + executed sweeps) for the parallel schedule
   if (o->schedule == ITN_SCHED_PARALLEL) c->cur = (c->cur + hs.iters) & 1;
   if (res) {
@@ -1178,7 +1212,11 @@ int compute_scalars(itn_ctx* c, const void* m) {
   const int ne = (int)c->eslots.size();
   CK(c->d_zv.ensure(std::max<int64_t>(c->nv, 1) * es));
   CK(c->d_ze.ensure(std::max(ne, 1) * es));
-  if (c->nv > 0) {
+  // the register-resident kernel for float / complex64 (the 8-byte types would spill)
+  if (c->nv > 0 && c->scal_d8 && (c->dtype == ITN_F32 || c->dtype == ITN_C64)) {
+    CK(launch_vertex_scalars_d8(c->dtype, (int)c->nv, c->d_rev.as<int>(), c->d_moff.as<long long>(),
+                                c->d_toff.as<long long>(), c->d_tens.p, m, c->d_zv.p, c->stream));
+  } else if (c->nv > 0) {
     GenericArgs a;
     LaunchCfg cfg;
     if (int r = plan_generic(c, a, cfg, c->d_items_scal.as<int>(), (int)c->items_scal.size() / 2, m,
@@ -1414,13 +1452,28 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
                    c->d_net_vlist.as<int>(), c->d_net_eoff.as<int>(), c->d_net_elist.as<int>(), c->n_nets,
                    c->d_logzv.as<double>(), c->d_logze.as<double>(), c->d_tot.as<double>(),
                    c->d_flags.as<int>(), c->stream));
-  if (zv && c->nv) CK(cudaMemcpyAsync(zv, c->d_zv.p, c->nv * es, cudaMemcpyDeviceToHost, c->stream));
-  if (ze && ne) CK(cudaMemcpyAsync(ze, c->d_ze.p, ne * es, cudaMemcpyDeviceToHost, c->stream));
-  if (logzv && c->nv) CK(cudaMemcpyAsync(logzv, c->d_logzv.p, c->nv * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (logze && ne) CK(cudaMemcpyAsync(logze, c->d_logze.p, ne * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (totals) CK(cudaMemcpyAsync(totals, c->d_tot.p, c->n_nets * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (flags) CK(cudaMemcpyAsync(flags, c->d_flags.p, c->n_nets * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  // every requested result goes through one pinned staging area: the copies are queued
+  // back to back and waited for once
+  struct Part { void* dst; const void* src; size_t bytes; size_t at; };
+  Part parts[6] = {{zv, c->d_zv.p, c->nv ? (size_t)c->nv * es : 0, 0},
+                   {ze, c->d_ze.p, (size_t)ne * es, 0},
+                   {logzv, c->d_logzv.p, (size_t)c->nv * 2 * sizeof(double), 0},
+                   {logze, c->d_logze.p, (size_t)ne * 2 * sizeof(double), 0},
+                   {totals, c->d_tot.p, (size_t)c->n_nets * 2 * sizeof(double), 0},
+                   {flags, c->d_flags.p, (size_t)c->n_nets * sizeof(int), 0}};
+  size_t need = 0;
+  for (Part& p : parts)
+    if (p.dst && p.bytes) {
+      p.at = need;
+      need += (p.bytes + 15) & ~size_t(15);
+    }
+  if (int r = ensure_pinned(c, need)) return r;
+  unsigned char* h = static_cast<unsigned char*>(c->h_pin);
+  for (const Part& p : parts)
+    if (p.dst && p.bytes) CK(cudaMemcpyAsync(h + p.at, p.src, p.bytes, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  for (const Part& p : parts)
+    if (p.dst && p.bytes) memcpy(p.dst, h + p.at, p.bytes);
   return ITN_OK;
 }
 

@@ -96,6 +96,12 @@ int generic_max_active(int dtype, int layers, int block, size_t smem);
 cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,
                                 const int* eslots, int n_e, const void* msgs, void* ze_out,
                                 cudaStream_t st);
+// Vertex scalars (float or complex64) when every vertex of a two-layer network has d = 2
+// and four legs of dimension 8 (vertex u's legs are slots 4u..4u+3, its tensor 8192 entries
+// at toff[u]).
+cudaError_t launch_vertex_scalars_d8(int dtype, int nv, const int* rev, const long long* moff,
+                                     const long long* toff, const void* tens, const void* msgs, void* zv,
+                                     cudaStream_t st);
 cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
                           const int* net_voff, const int* net_vlist, const int* net_eoff,
                           const int* net_elist, int n_nets, double* logzv, double* logze,

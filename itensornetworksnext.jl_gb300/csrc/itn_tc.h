@@ -36,8 +36,9 @@ cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st);
 // convergence test inside).  *used = false (and nothing enqueued) when the device cannot
 // host the cooperative grid, or for nsweeps == 2 or > 4095.
 cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used);
-// Non-zero when a bounded wait inside the tensor-core kernel gave up.
-int tc_error_flag(TcEngine* e, cudaStream_t st);
+// Device address of the engine's error flag, non-zero once a bounded wait inside the
+// tensor-core kernel gave up (reset by tc_prepare; null before the first prepare).
+const int* tc_err_ptr(const TcEngine* e);
 // One-CTA tcgen05 self-test (cached per process): M=128 product exact, M=64
 // accumulator lane map found.  lane_of_row may be null (64 entries otherwise).
 cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max_err, int* lane_of_row);

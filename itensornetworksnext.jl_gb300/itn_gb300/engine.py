@@ -185,9 +185,14 @@ class BPEngine:
 
     def bethe_free_energy(self, net: int | None = None):
         """bethe_free_energy (messagecache.jl:185-201) of one network (or a list for all)."""
-        r = self.logscalars()
+        nn = self.graph.n_nets
+        tot = np.empty((nn, 2))
+        fl = np.empty(nn, dtype=np.int32)
+        # only the per-network totals and flags are read back
+        self._check(self.lib.itn_logscalars(self._ctx, None, None, None, None, L.ptr(tot), L.ptr(fl)))
+        r = dict(totals=tot, flags=fl)
         out = []
-        for k in range(self.graph.n_nets):
+        for k in range(nn):
             f = int(r["flags"][k])
             if f & 4:
                 out.append(-np.inf)

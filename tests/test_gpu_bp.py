@@ -258,3 +258,21 @@ def test_zero_sum_message_is_not_normalised():
         assert np.array_equal(m[:4], [5.0, -5.0, -5.0, 5.0])
         ref = O.message_update(g, t, m0.copy(), 0)
         assert np.array_equal(m, ref)
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.float32, 1e-5), (np.complex64, 1e-5), (np.float64, 1e-12)])
+def test_vertex_scalars_of_d8_norm_vertices(dtype, tol):
+    """Vertex and edge log-scalars on a 4x4 periodic D=8 d=2 norm network (every vertex has
+    four legs of dimension 8: float32 / complex64 take the register-resident vertex-scalar
+    kernel, float64 the interpreter) against the FP64 oracle, with random Hermitian PSD
+    messages (no normalisation, so the scalars also carry the messages' scale)."""
+    rng = np.random.default_rng(88)
+    g = G.square_lattice(4, 4, 8, periodic=True, phys=2)
+    t = G.random_tensors(g, rng, dtype, G.peps_scale(g))
+    m = np.zeros(int(g.moff[-1]), dtype=dtype)
+    cplx = np.iscomplexobj(m)
+    for s in range(g.nslots):
+        x = rng.standard_normal((8, 8)) + (1j * rng.standard_normal((8, 8)) if cplx else 0)
+        m[g.moff[s]:g.moff[s + 1]] = (x @ np.conj(x).T / 8 + 0.5 * np.eye(8)).ravel()
+    with _engine(g, t, m) as e:
+        _check_scalars(g, t, m, e, tol)
