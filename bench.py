@@ -308,7 +308,9 @@ def run_gpu(args):
             flush_l2(device)
             r, logz = device_step()
             dev_ms.append(r.device_ms)
-            launches += r.kernel_launches + 1 + 3  # + message init + log-scalar kernels
+            # + message init + the log-norm's kernels (vertex scalars, edge scalars, FP64
+            # logs with per-block shares, the single-network sum)
+            launches += r.kernel_launches + 1 + 4
         for _ in range(args.steps):
             flush_l2(device)
             fp32_ms.append(fp32_step().device_ms)

@@ -804,36 +804,61 @@ __global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
 //   pass 2, thread (s, c):  V_s[(b0 b1)][c] = sum_{k0,k1} m0[b0,k0] W_s[(k0 k1)][c] m1[b1,k1]
 //   Z_u = sum_{s,b,c} conj(A_s[b][c]) V_s[b][c]
 // (m_l[b][k]: bra index b, ket index k, the message into u on leg l).  The same 262,144
-// multiply-adds per vertex as the interpreter's leg-by-leg absorption, but with every
-// 8 x 8 product in registers and a single pass through shared memory (row stride 65:
-// conflict-free row writes in pass 1 and column reads in pass 2).
+// multiply-adds per vertex as the interpreter's leg-by-leg absorption, with every 8 x 8
+// product in registers.  Shared memory holds W and, for float, the site tensor (staged by
+// coalesced 16-byte loads, all in flight at once); both with row stride 65, so that the row
+// accesses of pass 1 and the column accesses of pass 2 are free of bank conflicts.
 constexpr int kVsLd = 65;
 
 template <typename T>
+__host__ __device__ constexpr bool vs_stage() { return sizeof(T) == 4; }
+
+template <typename T>
 size_t vertex_scalar_d8_smem() {
-  return (size_t)(128 * kVsLd + 256 + 4) * sizeof(T);
+  return (size_t)((vs_stage<T>() ? 2 : 1) * 128 * kVsLd + 256 + 4) * sizeof(T);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) vertex_scalar_d8_kernel(const int* __restrict__ rev,
+__global__ void __launch_bounds__(128, vs_stage<T>() ? 3 : 1) vertex_scalar_d8_kernel(const int* __restrict__ rev,
                                                                const long long* __restrict__ moff,
                                                                const long long* __restrict__ toff,
                                                                const T* __restrict__ tens,
                                                                const T* __restrict__ msgs, T* __restrict__ zv) {
+  constexpr bool STAGE = vs_stage<T>();
   extern __shared__ __align__(16) unsigned char vs_smem[];
-  T* w = reinterpret_cast<T*>(vs_smem);  // [2 x 64][kVsLd]
-  T* m = w + 128 * kVsLd;                // [4][64]
-  T* red = m + 256;                      // [4]
+  T* w = reinterpret_cast<T*>(vs_smem);           // [2 x 64][kVsLd]
+  T* as = w + 128 * kVsLd;                        // STAGE: A_s[p][q] at (64 s + p) kVsLd + q
+  T* m = as + (STAGE ? 128 * kVsLd : 0);          // [4][64]
+  T* red = m + 256;                               // [4]
   const int u = blockIdx.x, t = threadIdx.x;
   const int s = t >> 6, r = t & 63;
+  const T* Ag = tens + toff[u];
+  if constexpr (STAGE) {
+    // 8192 entries as 2048 16-byte loads (the tensor starts on a 32 KB boundary)
+    const float4* src = reinterpret_cast<const float4*>(Ag);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float4 v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = __ldg(src + t + 128 * (8 * h + i));
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int j = t + 128 * (8 * h + i);
+        float* d = reinterpret_cast<float*>(as) + (j >> 4) * kVsLd + (j & 15) * 4;
+        d[0] = v[i].x;
+        d[1] = v[i].y;
+        d[2] = v[i].z;
+        d[3] = v[i].w;
+      }
+    }
+  }
   for (int j = t; j < 256; j += 128) m[j] = msgs[moff[rev[4 * u + (j >> 6)]] + (j & 63)];
   __syncthreads();
-  const T* A = tens + toff[u] + (size_t)s * 4096;
   {
     T W[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) W[i] = tzero<T>();
-    const T* row = A + r * 64;
+    const T* row = STAGE ? as + (s * 64 + r) * kVsLd : Ag + (size_t)s * 4096 + r * 64;
 #pragma unroll
     for (int k2 = 0; k2 < 8; ++k2) {
       T x[8], y[8];
@@ -883,8 +908,9 @@ __global__ void __launch_bounds__(128) vertex_scalar_d8_kernel(const int* __rest
         for (int b1 = 0; b1 < 8; ++b1) V[b0 * 8 + b1] = fmac(y[b1], c0, V[b0 * 8 + b1]);
       }
     }
+    const T* acol = STAGE ? as + s * 64 * kVsLd + r : Ag + (size_t)s * 4096 + r;
 #pragma unroll
-    for (int b = 0; b < 64; ++b) part = fmac(V[b], conjx(A[b * 64 + r]), part);
+    for (int b = 0; b < 64; ++b) part = fmac(V[b], conjx(acol[b * (STAGE ? kVsLd : 64)]), part);
   }
   part = warp_sum(part);
   if ((t & 31) == 0) red[t >> 5] = part;
@@ -924,20 +950,74 @@ __device__ __forceinline__ void log2d(T z, double& re, double& im) {
 
 // FP64 logs of every vertex and edge scalar, one thread each (the double-precision log is
 // slow on this part, so the logs are spread over the whole grid rather than summed by one
-// block per network).
+// block per network).  With `part` non-null (a single network), each block also leaves its
+// share of sum log Z_v - sum log Z_e as (re, im) in part[2 b], and its flag bits in
+// pflags[b], for logsum_single_kernel.
 template <typename T>
-__global__ void log_scalars_kernel(const T* zv, const T* ze, int nv, int ne, double* logzv, double* logze) {
+__global__ void __launch_bounds__(128) log_scalars_kernel(const T* zv, const T* ze, int nv, int ne, double* logzv,
+                                                          double* logze, double* part, int* pflags) {
+  __shared__ double sre[4], sim[4];
+  __shared__ int sfl[4];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  double re, im;
+  double re = 0, im = 0;
+  int fl = 0;
   if (j < nv) {
     log2d(zv[j], re, im);
     logzv[2 * j] = re;
     logzv[2 * j + 1] = im;
+    if (re_d(zv[j]) < 0) fl |= 1;
   } else if (j < nv + ne) {
     const int e = j - nv;
     log2d(ze[e], re, im);
     logze[2 * e] = re;
     logze[2 * e + 1] = im;
+    if (re_d(ze[e]) < 0) fl |= 2;
+    if (is_zero(ze[e])) fl |= 4;
+    re = -re;
+    im = -im;
+  }
+  if (!part) return;
+  re = warp_sum_d(re);
+  im = warp_sum_d(im);
+  for (int o = 16; o >= 1; o >>= 1) fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sre[warp] = re; sim[warp] = im; sfl[warp] = fl; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0, i = 0;
+    int f = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { r += sre[w]; i += sim[w]; f |= sfl[w]; }
+    part[2 * blockIdx.x] = r;
+    part[2 * blockIdx.x + 1] = i;
+    pflags[blockIdx.x] = f;
+  }
+}
+
+// The single-network total: the blocks' shares summed in block order.
+__global__ void __launch_bounds__(256) logsum_single_kernel(const double* part, const int* pflags, int nblocks,
+                                                            double* totals, int* flags) {
+  __shared__ double sre[8], sim[8];
+  __shared__ int sfl[8];
+  double re = 0, im = 0;
+  int fl = 0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    re += part[2 * b];
+    im += part[2 * b + 1];
+    fl |= pflags[b];
+  }
+  re = warp_sum_d(re);
+  im = warp_sum_d(im);
+  for (int o = 16; o >= 1; o >>= 1) fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sre[warp] = re; sim[warp] = im; sfl[warp] = fl; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0, i = 0;
+    int f = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { r += sre[w]; i += sim[w]; f |= sfl[w]; }
+    totals[0] = r;
+    totals[1] = i;
+    flags[0] = f;
   }
 }
 
@@ -1178,12 +1258,22 @@ cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, co
 cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
                           const int* voff, const int* vlist, const int* eoff, const int* elist,
                           int n_nets, double* logzv, double* logze, double* totals, int* flags,
-                          cudaStream_t st) {
+                          void* scratch, size_t scratch_bytes, cudaStream_t st) {
   if (n_nets <= 0) return cudaSuccess;
-  if (nv + ne > 0) {
-    ITN_DISPATCH(dtype, log_scalars_kernel<T><<<(nv + ne + 127) / 128, 128, 0, st>>>(
-                            reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), nv, ne, logzv, logze);
+  const int nblocks = (nv + ne + 127) / 128;
+  // one network: block shares (two doubles and a flag word per block) in `scratch`
+  const bool single = n_nets == 1 && nblocks > 0 && scratch && scratch_bytes >= (size_t)nblocks * 20;
+  double* part = single ? static_cast<double*>(scratch) : nullptr;
+  int* pflags = single ? reinterpret_cast<int*>(part + 2 * nblocks) : nullptr;
+  if (nblocks > 0) {
+    ITN_DISPATCH(dtype, log_scalars_kernel<T><<<nblocks, 128, 0, st>>>(
+                            reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), nv, ne, logzv, logze,
+                            part, pflags);
                  break);
+  }
+  if (single) {
+    logsum_single_kernel<<<1, 256, 0, st>>>(part, pflags, nblocks, totals, flags);
+    return cudaGetLastError();
   }
   ITN_DISPATCH(dtype, logsum_kernel<T><<<n_nets, 1024, 0, st>>>(
                           reinterpret_cast<const T*>(zv), reinterpret_cast<const T*>(ze), voff,

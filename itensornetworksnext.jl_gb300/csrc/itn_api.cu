@@ -173,7 +173,7 @@ struct itn_ctx {
   DevBuf d_tens;
   DevBuf d_msg[2];
   int cur = 0;
-  DevBuf d_zv, d_ze, d_logzv, d_logze, d_tot, d_flags;
+  DevBuf d_zv, d_ze, d_logzv, d_logze, d_tot, d_flags, d_lspart;
   DevBuf d_scratch;
   DevBuf d_stage;  // upload staging
   // pinned host staging for small results read back together (one copy, one sync)
@@ -1448,10 +1448,12 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
   CK(c->d_tot.ensure(c->n_nets * 2 * sizeof(double)));
   CK(c->d_flags.ensure(c->n_nets * sizeof(int)));
   if (int r = compute_scalars(c, c->d_msg[c->cur].p)) return r;
+  const size_t part_bytes = (size_t)((c->nv + ne + 127) / 128 + 1) * 20;
+  CK(c->d_lspart.ensure(part_bytes));
   CK(launch_logsum(c->dtype, c->d_zv.p, c->d_ze.p, (int)c->nv, ne, c->d_net_voff.as<int>(),
                    c->d_net_vlist.as<int>(), c->d_net_eoff.as<int>(), c->d_net_elist.as<int>(), c->n_nets,
                    c->d_logzv.as<double>(), c->d_logze.as<double>(), c->d_tot.as<double>(),
-                   c->d_flags.as<int>(), c->stream));
+                   c->d_flags.as<int>(), c->d_lspart.p, part_bytes, c->stream));
   // every requested result goes through one pinned staging area: the copies are queued
   // back to back and waited for once
   struct Part { void* dst; const void* src; size_t bytes; size_t at; };

@@ -105,7 +105,8 @@ cudaError_t launch_vertex_scalars_d8(int dtype, int nv, const int* rev, const lo
 cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
                           const int* net_voff, const int* net_vlist, const int* net_eoff,
                           const int* net_elist, int n_nets, double* logzv, double* logze,
-                          double* totals, int* flags, cudaStream_t st);
+                          double* totals, int* flags, void* scratch, size_t scratch_bytes,
+                          cudaStream_t st);
 cudaError_t launch_init_messages(int dtype, int layers, int kind, const long long* moff,
                                  const int* bond, int nslots, void* msgs, cudaStream_t st);
 cudaError_t launch_iterate_diff(int dtype, const long long* moff, int nslots, const void* m1,
