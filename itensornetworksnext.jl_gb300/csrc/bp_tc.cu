@@ -42,6 +42,13 @@ constexpr int kBlk = 8192;                 // bytes of one 64 x 64 BF16 operand 
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
 constexpr uint32_t kMaxDepPolls = 1u << 22; // bounded waits on another item (64 ns apart)
 constexpr int kTmemCols = 64;
+// TMEM columns a CTA of `groups` groups allocates: 64 per group, rounded up to the power of
+// two that tcgen05.alloc requires
+__host__ __device__ constexpr uint32_t tmem_cols_for(int groups) {
+  uint32_t n = 32;
+  while (n < (uint32_t)(kTmemCols * groups)) n <<= 1;
+  return n;
+}
 // operand modes of the sweep kernel
 constexpr int kOpBf16 = 0;   // BF16 operands
 constexpr int kOpSplit = 1;  // BF16 hi/lo split operands (3 MMAs per product)
@@ -289,6 +296,7 @@ template <int OP, int GROUPS, bool PERSIST>
 __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::per_sm) bp_tc_kernel(TcArgs a) {
   using O = OpT<OP>;
   constexpr bool SPLIT = O::split;
+  static_assert(tmem_cols_for(GROUPS) <= 512, "at most 512 TMEM columns per CTA");
   extern __shared__ __align__(1024) unsigned char sm_all[];
   constexpr TcSmem L = tc_smem<OP>();
   const int g = GROUPS > 1 ? (int)(threadIdx.x >> 7) : 0;
@@ -310,7 +318,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   const uint32_t epoch = PERSIST ? a.epoch[0] : 0u;
 
   if (threadIdx.x < 32) {
-    ptx::tmem_alloc(taddr_s, kTmemCols * GROUPS);
+    ptx::tmem_alloc(taddr_s, tmem_cols_for(GROUPS));
     ptx::tmem_relinquish();
   }
   if (tid == 0) {
@@ -593,7 +601,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   __syncthreads();
   if (threadIdx.x < 32) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(*taddr_s, kTmemCols * GROUPS);
+    ptx::tmem_dealloc(*taddr_s, tmem_cols_for(GROUPS));
   }
   if (PERSIST && threadIdx.x == 0) {
     // the last CTA to finish advances the epoch, so the next launch's tags differ
