@@ -661,26 +661,6 @@ __global__ void grad_mu_kernel(const long long* moff, int nslots, const T* lam, 
   for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) mu[j] = (lam[j] - dot) * is;
 }
 
-// lambda <- g + cot; stats[0] = max |change|, stats[1] = max |lambda| (order-encoded)
-template <typename T>
-__global__ void grad_update_kernel(long long n, const T* g, const T* cot, T* lam, AdjState* adj) {
-  if (*reinterpret_cast<const volatile int*>(&adj->done)) return;
-  double dmax = 0, lmax = 0;
-  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
-    const T v = g[j] + cot[j];
-    dmax = fmax(dmax, fabs((double)(v - lam[j])));
-    lmax = fmax(lmax, fabs((double)v));
-    lam[j] = v;
-  }
-  dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, 16));
-  for (int o = 8; o >= 1; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-  for (int o = 16; o >= 1; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&adj->dmax, enc_double(dmax));
-    atomicMax(&adj->lmax, enc_double(lmax));
-  }
-}
-
 __global__ void adj_reset_kernel(AdjState* s, double tol, int maxiter) {
   s->dmax = s->lmax = enc_double(0.0);
   s->done = maxiter <= 0;
@@ -689,13 +669,15 @@ __global__ void adj_reset_kernel(AdjState* s, double tol, int maxiter) {
   s->maxiter = maxiter;
   s->tol = tol;
   s->resid = 0.0;
+  s->ticket = 0;
 }
 
 // One step of the adjoint loop's stopping rule (single thread, after the update).
-__global__ void adj_step_kernel(AdjState* s) {
+__device__ void adj_step_dev(AdjState* s) {
   if (s->done) return;
   const int it = ++s->iters;
-  const double dmax = dec_double(s->dmax), lmax = dec_double(s->lmax);
+  const double dmax = dec_double(*reinterpret_cast<volatile unsigned long long*>(&s->dmax)),
+               lmax = dec_double(*reinterpret_cast<volatile unsigned long long*>(&s->lmax));
   const double r = lmax > 0 ? dmax / lmax : 0.0;
   s->resid = r;
   if (r != r) {
@@ -705,6 +687,51 @@ __global__ void adj_step_kernel(AdjState* s) {
     s->done = 1;
   }
   s->dmax = s->lmax = enc_double(0.0);
+}
+
+__global__ void adj_step_kernel(AdjState* s) { adj_step_dev(s); }
+
+// The tail of one adjoint iteration in one launch, one warp per slot: lambda <- g + cot
+// (max |lambda_new - lambda| and max |lambda_new| folded into the state, order-encoded), the
+// next iteration's mu exactly as grad_mu_kernel computes it, and the stopping rule in the
+// last block to finish (the other blocks have folded their maxima by then).  A stopped
+// loop returns at once in every block, so the ticket stays at zero.
+template <typename T>
+__global__ void __launch_bounds__(256) adj_update_kernel(const long long* moff, int nslots, const T* g, const T* cot,
+                                                         T* lam, const T* F, const T* S, T* mu, int normalize,
+                                                         AdjState* adj) {
+  if (*reinterpret_cast<const volatile int*>(&adj->done)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  double dmax = 0, lmax = 0;
+  if (warp < nslots) {
+    T dot = 0;
+    for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) {
+      const T v = g[j] + cot[j];
+      dmax = fmax(dmax, fabs((double)(v - lam[j])));
+      lmax = fmax(lmax, fabs((double)v));
+      lam[j] = v;
+      if (normalize) dot += v * F[j];
+    }
+    dot = warp_sum(dot);
+    const T is = T(1) / S[warp];
+    for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) mu[j] = (lam[j] - dot) * is;
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  }
+  if (lane == 0) {
+    atomicMax(&adj->dmax, enc_double(dmax));
+    atomicMax(&adj->lmax, enc_double(lmax));
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(&adj->ticket, 1u) == gridDim.x - 1) {
+    __threadfence();
+    adj_step_dev(adj);
+    adj->ticket = 0;
+    __threadfence();
+  }
 }
 
 // ---- the one-layer kernel ----------------------------------------------------------------
@@ -1374,12 +1401,14 @@ cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const v
                     return cudaGetLastError());
 }
 
-cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
-                               AdjState* adj, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  const int grid = (int)std::min<long long>((n + 255) / 256, 1024);
-  ITN_REAL_DISPATCH(dtype, grad_update_kernel<T><<<grid, 256, 0, st>>>(n, (const T*)g, (const T*)cot, (T*)lam,
-                                                                      adj);
+cudaError_t launch_adj_update(int dtype, const long long* moff, int nslots, const void* g, const void* cot,
+                              void* lam, const void* F, const void* S, void* mu, int normalize, AdjState* adj,
+                              cudaStream_t st) {
+  if (nslots <= 0) return launch_adj_step(adj, st);
+  const int grid = (nslots * 32 + 255) / 256;
+  ITN_REAL_DISPATCH(dtype, adj_update_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)g, (const T*)cot,
+                                                                     (T*)lam, (const T*)F, (const T*)S, (T*)mu,
+                                                                     normalize, adj);
                     return cudaGetLastError());
 }
 

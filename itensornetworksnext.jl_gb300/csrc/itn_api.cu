@@ -1292,6 +1292,21 @@ int adjoint_prepare(itn_ctx* c, const void* m, int normalized) {
 // cot = J^T lam for the sweep m -> F(m) (needs adjoint_prepare): lam is projected through
 // the normalisation (mu = (lam - <lam, F>) / S) and pushed back through the products by
 // the dual interpreter (tangent of the leave-one-out contraction on every leg).
+// cot = J^T-product of the dual interpreter for tangents mu already in c->d_mu.
+int apply_dual_mu(itn_ctx* c, const void* m, void* cot, const int* done) {
+  const int np = (int)c->items_par.size() / 2;
+  GenericArgs da;
+  LaunchCfg dcfg;
+  if (int r = plan_dual(c, da, dcfg, c->d_items_par.as<int>(), np, m)) return r;
+  DualArgs dd;
+  memset(&dd, 0, sizeof(dd));
+  dd.tan_in = c->d_mu.p;
+  dd.tan_out = cot;
+  dd.done = done;
+  CK(launch_dual(c->dtype, da, dd, dcfg, c->stream));
+  return ITN_OK;
+}
+
 int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normalized, const int* done = nullptr) {
   const int ns = (int)c->nslots, np = (int)c->items_par.size() / 2;
   CK(launch_grad_mu(c->dtype, c->d_moff.as<long long>(), ns, lam, c->d_F.p, c->d_S.p, c->d_mu.p, normalized,
@@ -1376,17 +1391,21 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     // adjoint BP: lambda <- g + J^T lambda until the relative change is below tol.  The
     // stopping rule runs on the device (AdjState); iterations are enqueued in chunks and
     // the host reads the state once per chunk (launches after the stop return at once).
+    // An iteration is two launches: the dual interpreter (J^T through the products, from
+    // mu) and the fused update (lambda, the next mu and the stopping rule).
     AdjState* adj = c->d_adj.as<AdjState>();
     const int maxit = std::max(o->maxiter, 0);
     CK(launch_adj_reset(adj, o->tol, maxit, c->stream));
+    CK(launch_grad_mu(dt, c->d_moff.as<long long>(), ns, c->d_lam.p, c->d_F.p, c->d_S.p, c->d_mu.p,
+                      o->normalized, nullptr, c->stream));
     AdjState hs;
     memset(&hs, 0, sizeof(hs));
     for (int issued = 0; issued < maxit;) {
       const int chunk = std::min(maxit - issued, 8);
       for (int k = 0; k < chunk; ++k) {
-        if (int r = apply_jt(c, m, c->d_lam.p, c->d_cot.p, o->normalized, &adj->done)) return r;
-        CK(launch_grad_update(dt, (long long)c->moff[c->nslots], c->d_g.p, c->d_cot.p, c->d_lam.p, adj, c->stream));
-        CK(launch_adj_step(adj, c->stream));
+        if (int r = apply_dual_mu(c, m, c->d_cot.p, &adj->done)) return r;
+        CK(launch_adj_update(dt, c->d_moff.as<long long>(), ns, c->d_g.p, c->d_cot.p, c->d_lam.p, c->d_F.p,
+                             c->d_S.p, c->d_mu.p, o->normalized, adj, c->stream));
       }
       issued += chunk;
       CK(cudaMemcpyAsync(&hs, adj, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));

@@ -69,9 +69,9 @@ struct DualArgs {
 };
 
 // Device-side state of the adjoint fixed-point iteration lambda <- g + J^T lambda: the
-// update kernel folds max|lambda_new - lambda| and max|lambda_new| into dmax / lmax
-// (order-encoded), a one-thread step kernel turns them into the relative change and
-// stops the loop; launches after the stop return at once.
+// fused update kernel folds max|lambda_new - lambda| and max|lambda_new| into dmax / lmax
+// (order-encoded) and its last block turns them into the relative change and stops the
+// loop; launches after the stop return at once.
 struct AdjState {
   unsigned long long dmax, lmax;
   int done;       // stopped (converged, NaN or maxiter)
@@ -80,6 +80,7 @@ struct AdjState {
   int maxiter;
   double tol;
   double resid;   // last relative change
+  unsigned ticket;  // blocks of the fused update finished in this iteration
 };
 
 struct LaunchCfg {
@@ -124,10 +125,13 @@ cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, cons
                           const void* ze, void* g, cudaStream_t st);
 cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const void* lam, const void* F,
                            const void* S, void* mu, int normalize, const int* done, cudaStream_t st);
-cudaError_t launch_grad_update(int dtype, long long n, const void* g, const void* cot, void* lam,
-                               AdjState* adj, cudaStream_t st);
 cudaError_t launch_adj_reset(AdjState* adj, double tol, int maxiter, cudaStream_t st);
 cudaError_t launch_adj_step(AdjState* adj, cudaStream_t st);
+// lambda <- g + cot, then mu <- (lambda - <lambda, F>) / S (normalised) or lambda, and the
+// stopping rule, in one launch (the step runs in the last block to finish).
+cudaError_t launch_adj_update(int dtype, const long long* moff, int nslots, const void* g, const void* cot,
+                              void* lam, const void* F, const void* S, void* mu, int normalize, AdjState* adj,
+                              cudaStream_t st);
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st);
 cudaError_t launch_step_check(ConvState* s, cudaStream_t st);
 
