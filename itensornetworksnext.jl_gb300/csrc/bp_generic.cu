@@ -37,12 +37,84 @@ constexpr int kRedWidth = 64;  // per-warp partial-sum slots for D*D <= 64
 struct LegMeta {
   uint64_t bar;            // mbarrier of the bulk copy of the site tensor
   unsigned phase;          // its current phase parity
+  int bulk;                // the site tensor of the current item arrives by bulk copy
   int z, d, n;          // legs, physical dim, tensor elements
+  int s0, mtot;         // first slot of the vertex; message entries staged
   int dims[kMaxLegs];
   int inner[kMaxLegs];  // prod of dims after the leg
   int outer[kMaxLegs];  // d * prod of dims before the leg
   int moffs[kMaxLegs];  // offset of the leg's incoming message in shared staging
+  long long msrc[kMaxLegs];  // offset of the incoming message m_{w->u} (slot rev(s0 + l))
+  long long tsrc[kMaxLegs];  // offset of the outgoing slot s0 + l (tangents of the dual kernel)
 };
+
+// Per-item set-up shared by the two-layer kernels, done by warp 0 alone and followed by
+// one barrier: (1) every lane reads the vertex's slot range and physical dimension, and
+// lane 0 starts the bulk copy of the site tensor into buffer 0 when `allow_bulk` and the
+// tensor is 16-byte aligned and 4 KB .. 1 MB; (2) lane l < z reads leg l's bond dimension
+// and incoming-message offset; (3) the prefix sums / products of the legs by shuffles.
+template <typename T, bool DUAL>
+__device__ void item_meta(const GenericArgs& a, int u, LegMeta* meta, T* A, bool allow_bulk) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int s0 = a.off[u], z = a.off[u + 1] - s0, dph = a.phys[u];
+    if (lane == 0) {
+      const long long t0 = a.toff[u], tn = a.toff[u + 1] - t0;
+      const bool bulk = allow_bulk && ((t0 * (long long)sizeof(T)) & 15) == 0 &&
+                        ((tn * (long long)sizeof(T)) & 15) == 0 && tn * (long long)sizeof(T) >= 4096 &&
+                        tn * (long long)sizeof(T) < (1ll << 20);
+      meta->bulk = bulk;
+      if (bulk) {
+        const T* A_g = reinterpret_cast<const T*>(a.tens) + t0;
+        ptx::fence_proxy_async_smem();  // earlier generic accesses to buffer 0 come first
+        ptx::mbar_arrive_expect_tx(&meta->bar, (uint32_t)(tn * sizeof(T)));
+        ptx::bulk_g2s(A, A_g, (uint32_t)(tn * sizeof(T)), &meta->bar);
+      }
+    }
+    int dim = 1;
+    if (lane < z) {
+      dim = a.bond[s0 + lane];
+      meta->msrc[lane] = a.moff[a.rev[s0 + lane]];
+      if (DUAL) meta->tsrc[lane] = a.moff[s0 + lane];
+    }
+    // exclusive prefix sum of dim^2 (message offsets) and inclusive suffix product of dim
+    const int sq = lane < z ? dim * dim : 0;
+    int psum = sq, sprod = dim;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int up = __shfl_up_sync(0xffffffffu, psum, o);
+      const int dn = __shfl_down_sync(0xffffffffu, sprod, o);
+      if (lane >= o) psum += up;
+      if (lane + o < 32) sprod *= dn;
+    }
+    const int inner = __shfl_down_sync(0xffffffffu, sprod, 1);  // product of the dims after the leg
+    const int all = __shfl_sync(0xffffffffu, sprod, 0);
+    const int tot = __shfl_sync(0xffffffffu, psum, 31);
+    const int n = dph * all;
+    if (lane < z) {
+      const int in = lane == 31 ? 1 : inner;
+      meta->dims[lane] = dim;
+      meta->moffs[lane] = psum - sq;
+      meta->inner[lane] = in;
+      meta->outer[lane] = n / (in * dim);
+    }
+    if (lane == 0) {
+      meta->s0 = s0;
+      meta->z = z;
+      meta->d = dph;
+      meta->n = n;
+      meta->mtot = tot;
+    }
+  }
+  __syncthreads();
+}
+
+// Leg of staged message entry j (messages staged back to back in leg order).
+__device__ __forceinline__ int staged_leg(const LegMeta* meta, int j) {
+  int l = 0;
+  while (l + 1 < meta->z && j >= meta->moffs[l + 1]) ++l;
+  return l;
+}
 
 // ---- warp reduce-scatter of NV (power of two) values -------------------------------
 // After the call, lane holds in v[j] (j < max(NV/32, 1)) the warp sum of index base+j.
@@ -368,48 +440,20 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
     const unsigned* prog = a.prog + a.items[2 * it + 1];
-    if (threadIdx.x == 0) {
-      const int s0 = a.off[u];
-      const int z = a.off[u + 1] - s0;
-      meta->z = z;
-      meta->d = a.phys[u];
-      int n = meta->d, mo = 0;
-      for (int l = 0; l < z; ++l) {
-        meta->dims[l] = a.bond[s0 + l];
-        n *= meta->dims[l];
-        meta->moffs[l] = mo;
-        mo += meta->dims[l] * meta->dims[l];
-      }
-      meta->n = n;
-      int inner = 1;
-      for (int l = z - 1; l >= 0; --l) {
-        meta->inner[l] = inner;
-        inner *= meta->dims[l];
-      }
-      for (int l = 0; l < z; ++l) meta->outer[l] = n / (meta->inner[l] * meta->dims[l]);
-    }
-    __syncthreads();
-    const int z = meta->z, n = meta->n;
-    // stage the site tensor (buffer 0) and the incoming messages m_{w->u}; a 16-byte
-    // aligned tensor in shared-memory buffers arrives by one bulk (TMA) copy
-    const T* A_g = tens + a.toff[u];
+    // the site tensor goes to buffer 0 (a 16-byte aligned tensor in shared-memory buffers
+    // by one bulk copy, started inside item_meta), the incoming messages m_{w->u} to the
+    // staging area
     T* A = bufs;
-    const bool bulk = a.gscratch == nullptr && ((a.toff[u] * sizeof(T)) & 15) == 0 &&
-                      ((n * sizeof(T)) & 15) == 0 && n * sizeof(T) >= 4096 && n * sizeof(T) < (1u << 20);
-    if (bulk) {
-      if (threadIdx.x == 0) {
-        ptx::fence_proxy_async_smem();  // earlier generic accesses to buffer 0 come first
-        ptx::mbar_arrive_expect_tx(&meta->bar, (uint32_t)(n * sizeof(T)));
-        ptx::bulk_g2s(A, A_g, (uint32_t)(n * sizeof(T)), &meta->bar);
-      }
-    } else {
+    item_meta<T, false>(a, u, meta, A, a.gscratch == nullptr);
+    const int z = meta->z, n = meta->n;
+    const T* A_g = tens + a.toff[u];
+    const bool bulk = meta->bulk != 0;
+    if (!bulk)
       for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
-    }
-    const int s0 = a.off[u];
-    for (int l = 0; l < z; ++l) {
-      const int D2 = meta->dims[l] * meta->dims[l];
-      const T* src = min_ + a.moff[a.rev[s0 + l]];
-      for (int j = threadIdx.x; j < D2; j += blockDim.x) msgs[meta->moffs[l] + j] = src[j];
+    const int s0 = meta->s0;
+    for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+      const int l = staged_leg(meta, j);
+      msgs[j] = min_[meta->msrc[l] + (j - meta->moffs[l])];
     }
     if (bulk) {
       // bounded wait; on timeout the copy is re-done with plain loads
@@ -542,45 +586,37 @@ __global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d
   const T* tin = reinterpret_cast<const T*>(d.tan_in);
   const int half = a.msg_cap / 2;
   if (d.done && *reinterpret_cast<const volatile int*>(d.done)) return;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(&meta->bar, 1);
+    ptx::fence_mbar_init();
+    meta->phase = 0;
+  }
+  __syncthreads();
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
     const unsigned* prog = a.prog + a.items[2 * it + 1];
-    if (threadIdx.x == 0) {
-      const int s0 = a.off[u];
-      const int z = a.off[u + 1] - s0;
-      meta->z = z;
-      meta->d = a.phys[u];
-      int n = meta->d, mo = 0;
-      for (int l = 0; l < z; ++l) {
-        meta->dims[l] = a.bond[s0 + l];
-        n *= meta->dims[l];
-        meta->moffs[l] = mo;
-        mo += meta->dims[l] * meta->dims[l];
-      }
-      meta->n = n;
-      int inner = 1;
-      for (int l = z - 1; l >= 0; --l) {
-        meta->inner[l] = inner;
-        inner *= meta->dims[l];
-      }
-      for (int l = 0; l < z; ++l) meta->outer[l] = n / (meta->inner[l] * meta->dims[l]);
-    }
-    __syncthreads();
-    const int z = meta->z, n = meta->n;
-    const T* A_g = tens + a.toff[u];
     T* A = bufs;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
-    const int s0 = a.off[u];
-    for (int l = 0; l < z; ++l) {
-      const int Dl = meta->dims[l], D2 = Dl * Dl;
-      const T* src = min_ + a.moff[a.rev[s0 + l]];
-      const T* tsrc = tin ? tin + a.moff[s0 + l] : nullptr;
-      for (int j = threadIdx.x; j < D2; j += blockDim.x) {
-        const int jj = d.transpose ? (j % Dl) * Dl + j / Dl : j;
-        msgs[meta->moffs[l] + j] = src[jj];
-        msgs[half + meta->moffs[l] + j] = tsrc ? tsrc[jj] : T(0);
+    item_meta<T, true>(a, u, meta, A, a.gscratch == nullptr);
+    const int n = meta->n;
+    const T* A_g = tens + a.toff[u];
+    const bool bulk = meta->bulk != 0;
+    if (!bulk)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
+    const int s0 = meta->s0;
+    for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+      const int l = staged_leg(meta, j);
+      const int Dl = meta->dims[l], jl = j - meta->moffs[l];
+      const int jj = d.transpose ? (jl % Dl) * Dl + jl / Dl : jl;
+      msgs[j] = min_[meta->msrc[l] + jj];
+      msgs[half + j] = tin ? tin[meta->tsrc[l] + jj] : T(0);
+    }
+    if (bulk) {
+      // bounded wait; on timeout the copy is re-done with plain loads
+      if (!__syncthreads_and(ptx::mbar_wait_bounded(&meta->bar, meta->phase, 1u << 26))) {
+        for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
       }
+      if (threadIdx.x == 0) meta->phase ^= 1;
     }
     __syncthreads();
     const int nops = (int)prog[0];
