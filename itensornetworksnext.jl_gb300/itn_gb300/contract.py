@@ -130,6 +130,31 @@ def norm_network_tensors(g: Graph, packed):
     return ts, ls
 
 
+def plain_network_tensors(g: Graph, packed):
+    """A single-layer network (a partition function such as ising_network / delta_network)
+    as a tensor list: tensor u with its links named by undirected edge, the site index
+    (when phys > 1) left open."""
+    ts, ls = [], []
+    for u in range(g.nv):
+        A = np.asarray(packed[g.toff[u]:g.toff[u + 1]]).reshape(g.tensor_shape(u))
+        legs = [("k", int(min(s, g.rev[s]))) for s in range(g.off[u], g.off[u + 1])]
+        if A.shape[0] == 1:
+            ts.append(A.reshape(A.shape[1:]))
+            ls.append(legs)
+        else:
+            ts.append(A)
+            ls.append([("s", u)] + legs)
+    return ts, ls
+
+
+def contract_plain_network(g: Graph, packed, **kw):
+    """Exact contraction of a single-layer network (contract_network(tn),
+    contract_network.jl:7-58); a scalar for a closed network."""
+    ts, ls = plain_network_tensors(g, packed)
+    out, lo = contract_network(ts, ls, **kw)[:2]
+    return out[()] if not lo else (out, lo)
+
+
 def contract_norm_network(g: Graph, packed, **kw):
     """Exact <psi|psi> of a PEPS given as a Graph + packed site tensors."""
     ts, ls = norm_network_tensors(g, packed)

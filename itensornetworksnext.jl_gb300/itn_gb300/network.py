@@ -209,6 +209,21 @@ class MessageCache:
     def copy(self):
         return MessageCache(self.messages)
 
+    def copyto(self, src, edges=None):
+        """copyto!(dst, src[, edges]) of the DataGraphs interface that MessageCache implements
+        (messagecache.jl:84-101; exercised by test/test_beliefpropagation.jl:63-81): src is
+        another cache, a dict or a list of (edge, message) pairs; with ``edges``, only those
+        directed edges of the cache ``src`` are copied.  In place; returns self."""
+        if edges is not None:
+            for e in edges:
+                self.messages[tuple(e)] = src[tuple(e)]
+            return self
+        items = src.messages.items() if isinstance(src, MessageCache) else (
+            src.items() if isinstance(src, dict) else src)
+        for e, m in items:
+            self.messages[tuple(e)] = m
+        return self
+
     def __len__(self):
         return len(self.messages)
 

@@ -136,6 +136,15 @@ def test_norm_network_contraction(dtype):
                       N.contract_network(N.NormNetwork(tn))[()])
 
 
+def test_single_normalized_tensor_contracts_to_one():
+    """test_normnetwork.jl:137-146: <psi|psi> of one normalised site tensor is 1."""
+    rng = np.random.default_rng(8)
+    s = N.Index(3)
+    v = rng.standard_normal(3)
+    tn = N.ITensorNetwork({1: N.ITensor(v / np.linalg.norm(v), [s])})
+    assert np.isclose(N.contract_network(N.NormNetwork(tn))[()], 1.0, rtol=1e-14)
+
+
 def test_bp_on_norm_network_matches_exact_on_tree():
     """BP on a NormNetwork (the path used by apply_operator's environment,
     test_apply_operator.jl:70-74) is exact on a tree."""

@@ -128,3 +128,26 @@ def test_insertlink_and_operator_environments():
         assert op.domain == tuple(names) and op.codomain == tuple(nn.bra(n) for n in names)
         for order in (names, names[::-1]):
             np.testing.assert_array_equal(N._env_matrix(ops, e, order), N._env_matrix(msgs, e, order))
+
+
+def test_message_cache_basics():
+    """test_beliefpropagation.jl:40-81: a cache of arbitrary values keyed by directed
+    edge; setting a message, copyto! from pairs / a dict, and copyto! of selected edges."""
+    edges = [((1, 1), (1, 2)), ((1, 2), (2, 2)), ((2, 2), (2, 3))]
+    alle = edges + [(b, a) for a, b in edges]
+    bpc = N.messagecache(lambda e: f"{e[0]} => {e[1]}", alle)
+    assert len(bpc) == 2 * len(edges)
+    assert bpc[((1, 1), (1, 2))] == "(1, 1) => (1, 2)"
+    bpc[((1, 1), (1, 2))] = "new message"
+    assert bpc[((1, 1), (1, 2))] == "new message"
+    pairs = [(((1, 2), (2, 2)), "m1"), (((2, 2), (2, 3)), "m2")]
+    for src in (pairs, dict(pairs)):
+        new = bpc.copy().copyto(src)
+        assert new[((1, 1), (1, 2))] == "new message"
+        assert new[((1, 2), (2, 2))] == "m1" and new[((2, 2), (2, 3))] == "m2"
+        assert bpc[((1, 2), (2, 2))] == "(1, 2) => (2, 2)"  # the source cache is unchanged
+    dst = N.messagecache(lambda e: "", alle)
+    dst.copyto(bpc, [((1, 2), (2, 2)), ((2, 2), (2, 3))])
+    assert dst[((1, 1), (1, 2))] == ""
+    assert dst[((1, 2), (2, 2))] == "(1, 2) => (2, 2)"
+    assert dst[((2, 2), (2, 3))] == "(2, 2) => (2, 3)"
