@@ -196,6 +196,45 @@ __device__ __forceinline__ void store_row(T* __restrict__ p, const T (&t)[D]) {
   }
 }
 
+// Thread-strided walk p = threadIdx.x, +blockDim.x, ... over p = o * inner + i.  Real types
+// step (o, i) by additions instead of an integer division per element (6% on the FP32
+// 32x32 D=8 sweep); complex types divide per element as before, with no state carried:
+// their D-specialised paths are bound by instruction fetch, and carrying the walk measured
+// 5% slower on the batched complex64 networks.
+template <typename T, bool INC = !is_cplx<T>::value>
+struct OiWalk {
+  int o, i, bo, bi, inner;
+  __device__ __forceinline__ explicit OiWalk(int inner_) : inner(inner_) {
+    const int p0 = (int)threadIdx.x, st = (int)blockDim.x;
+    o = p0 / inner_;
+    i = p0 - o * inner_;
+    bo = st / inner_;
+    bi = st - bo * inner_;
+  }
+  __device__ __forceinline__ void get(int, int& oo, int& ii) const {
+    oo = o;
+    ii = i;
+  }
+  __device__ __forceinline__ void next() {
+    o += bo;
+    i += bi;
+    if (i >= inner) {
+      i -= inner;
+      ++o;
+    }
+  }
+};
+template <typename T>
+struct OiWalk<T, false> {
+  int inner;
+  __device__ __forceinline__ explicit OiWalk(int inner_) : inner(inner_) {}
+  __device__ __forceinline__ void get(int p, int& oo, int& ii) const {
+    oo = p / inner;
+    ii = p - oo * inner;
+  }
+  __device__ __forceinline__ void next() {}
+};
+
 // ---- ABSORB with compile-time bond dimension ---------------------------------------
 template <typename T, int D>
 __device__ __forceinline__ void absorb_fixed(const T* __restrict__ src, T* __restrict__ dst,
@@ -219,8 +258,10 @@ __device__ __forceinline__ void absorb_fixed(const T* __restrict__ src, T* __res
     }
     return;
   }
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int o = p / inner, i = p - o * inner;
+  OiWalk<T> w(inner);
+  for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+    int o, i;
+    w.get(p, o, i);
     const T* s = src + o * D * inner + i;
     T t[D];
 #pragma unroll
@@ -240,8 +281,10 @@ template <typename T>
 __device__ void absorb_rt(const T* __restrict__ src, T* __restrict__ dst, int outer, int D,
                           int inner, const T* __restrict__ m) {
   const int n = outer * inner;
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int o = p / inner, i = p - o * inner;
+  OiWalk<T> w(inner);
+  for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+    int o, i;
+    w.get(p, o, i);
     const T* s = src + o * D * inner + i;
     T* dd = dst + o * D * inner + i;
     for (int b = 0; b < D; ++b) {
@@ -262,8 +305,10 @@ __device__ __forceinline__ void final_fixed(const T* __restrict__ src, const T* 
 #pragma unroll
   for (int j = 0; j < NV; ++j) acc[j] = tzero<T>();
   const int n = outer * inner;
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int o = p / inner, i = p - o * inner;
+  OiWalk<T> w(inner);
+  for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+    int o, i;
+    w.get(p, o, i);
     const T* s = src + o * D * inner + i;
     const T* a = A + o * D * inner + i;
     T t[D], c[D];
@@ -305,8 +350,10 @@ __device__ void final_rt(const T* __restrict__ src, const T* __restrict__ A, int
   for (int e = 0; e < D * D; ++e) {
     const int b = e / D, k = e - b * D;
     T acc = tzero<T>();
-    for (int p = threadIdx.x; p < n; p += blockDim.x) {
-      const int o = p / inner, i = p - o * inner;
+    OiWalk<T> w(inner);
+    for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+      int o, i;
+      w.get(p, o, i);
       acc = fmac(src[(o * D + k) * inner + i], conjx(A[(o * D + b) * inner + i]), acc);
     }
     acc = block_sum(acc, red);
@@ -512,8 +559,10 @@ __device__ __forceinline__ void absorb_dual_fixed(const T* __restrict__ src, con
     dr[j] = dm[j];
   }
   const int n = outer * inner;
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int o = p / inner, i = p - o * inner;
+  OiWalk<T> w(inner);
+  for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+    int o, i;
+    w.get(p, o, i);
     const int base = o * D * inner + i;
     T t[D], dt[D];
 #pragma unroll
@@ -540,8 +589,10 @@ __device__ void absorb_dual_rt(const T* __restrict__ src, const T* __restrict__ 
                                T* __restrict__ dstT, int outer, int D, int inner, const T* __restrict__ m,
                                const T* __restrict__ dm) {
   const int n = outer * inner;
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int o = p / inner, i = p - o * inner;
+  OiWalk<T> w(inner);
+  for (int p = threadIdx.x; p < n; p += blockDim.x, w.next()) {
+    int o, i;
+    w.get(p, o, i);
     const int base = o * D * inner + i;
     for (int b = 0; b < D; ++b) {
       T acc = 0, dacc = 0;
