@@ -205,6 +205,20 @@ def flush_l2(device):
     torch.cuda.synchronize(device)
 
 
+def host_cpu():
+    """Model name of the host cores (lscpu), else the machine type."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip() + f" ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(g, t, seconds=12.0):
     """Oracle (CPU restatement of the reference algorithm), FP32 parallel sweeps with
     OpenMP over all host threads, on the same 32x32 D=8 network; a bounded sample."""
@@ -225,7 +239,7 @@ def cpu_baseline(g, t, seconds=12.0):
         O.bp_sweeps(g, t32, m, 1, nthreads=1)
         n1 += 1
     dt1 = time.perf_counter() - t1
-    return {"value": n * g.nslots / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": n * g.nslots / dt, "unit": UNIT, "cores": threads, "kind": "port", "cpu": host_cpu(),
             "sample": f"{n} parallel FP32 sweeps of the 32x32 D=8 norm network ({n * g.nslots} updates, {dt:.1f} s)",
             "one_core": {"value": n1 * g.nslots / dt1, "unit": UNIT,
                          "sample": f"{n1} sweeps on 1 thread ({dt1:.1f} s)"}}
@@ -258,7 +272,7 @@ def run_reference(args):
             "data": "synthetic (seeded N(0,1)/sqrt(d D^4) PEPS)",
             "config": {"workload": f"peps {LX}x{LY} periodic norm network D={BOND} d={PHYS}, parallel schedule",
                        "step": f"{sweeps_per_step} sweeps (bounded CPU sample of the GPU step's {SWEEPS})"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "cpu": host_cpu(),
                              "sample": f"{args.steps} steps x {sweeps_per_step} FP32 sweeps, OpenMP"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
