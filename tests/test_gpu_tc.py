@@ -121,14 +121,17 @@ def test_tc_rejects_unsupported_network():
 
 @pytest.mark.parametrize("L,n,split,prec", [(32, 7, 0, "bf16"), (32, 6, 2, "bf16"), (4, 5, 1, "bf16"),
                                             (3, 9, 0, "bf16"), (48, 5, 1, "bf16"), (32, 5, 0, "tf32"),
-                                            (4, 6, 3, "tf32")])
+                                            (4, 6, 3, "tf32"), (4, 2, 0, "bf16"), (4, 1, 0, "bf16"),
+                                            (4, 3, 5, "bf16")])
 def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     """Without a convergence test the sweeps run as one cooperative launch per precision
-    part (per-item completion counters instead of kernel boundaries); with one the engine
+    part (tagged message entries instead of kernel boundaries); with one the engine
     launches once per sweep.  Both run the same per-item arithmetic, so the messages must
     agree bit for bit -- a missed dependency would read a stale or half-written message.
     32x32 and 48x48 (about four items per group per sweep) have more half-vertex items than
-    groups, 4x4 and 3x3 (the smallest periodic lattice, one CTA) fewer."""
+    groups, 4x4 and 3x3 (the smallest periodic lattice, one CTA) fewer.  Two-sweep parts run
+    as per-sweep launches in both forms, one-sweep parts read the plain input and write the
+    plain output in the same sweep, and more split sweeps than sweeps makes every sweep split."""
     g, t = _lattice(L, 11)
     rng = np.random.default_rng(12)
     m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
@@ -141,5 +144,6 @@ def test_persistent_matches_per_sweep_launches(L, n, split, prec):
         r2 = e.run(maxiter=n, tol=1e-300, precision=prec, split_sweeps=split)
         b = e.messages()
     assert r1.iterations == n and r2.iterations == n
-    assert r1.kernel_launches < r2.kernel_launches
+    if n > 2:
+        assert r1.kernel_launches < r2.kernel_launches
     np.testing.assert_array_equal(a, b)
