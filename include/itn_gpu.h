@@ -128,6 +128,19 @@ int32_t itn_messages_init(itn_ctx *ctx, int32_t kind);
  * runs the whole solve on the device on the uploaded messages, in place. */
 int32_t itn_bp_run(itn_ctx *ctx, const itn_bp_opts *opts, itn_bp_result *result);
 
+/* One end-to-end call: beliefpropagation(factors, messages; ...) followed by
+ * bethe_free_energy(factors, messages) (beliefpropagation.jl:69-92, messagecache.jl:185-201)
+ * on host inputs.  Uploads the packed site tensors and initial messages (layouts of
+ * itn_tensors_upload / itn_messages_upload, one dtype for both), runs the solve of
+ * itn_bp_run with `opts`, computes the log-norm totals and flags of itn_logscalars and
+ * downloads the final messages -- all queued on the context's stream with a single host
+ * synchronisation at the end (one more per convergence check when opts has a tolerance).
+ * messages_out, totals and flags may each be NULL.  Pinned host buffers make the copies
+ * asynchronous.  The context keeps the uploaded data, as after the separate calls. */
+int32_t itn_bp_solve(itn_ctx *ctx, int32_t dtype, const void *tensors, const void *messages_in,
+                     const itn_bp_opts *opts, itn_bp_result *result, void *messages_out,
+                     double *totals, int32_t *flags);
+
 /* message_update!(SimpleMessageUpdate(normalize), cache, factors, edge)
  * (src/beliefpropagation/beliefpropagation.jl:242-257) for the directed slot. */
 int32_t itn_message_update(itn_ctx *ctx, int64_t slot, int32_t normalize);

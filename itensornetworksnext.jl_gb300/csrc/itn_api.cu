@@ -179,6 +179,14 @@ struct itn_ctx {
   // pinned host staging for small results read back together (one copy, one sync)
   void* h_pin = nullptr;
   size_t h_pin_bytes = 0;
+  // a solve whose last host synchronisation was left to the caller (itn_bp_solve)
+  struct {
+    bool active = false;
+    bool use_tol = false;
+    bool tc = false;
+    int launches = 0;
+    float ms_before = 0.f;
+  } pending;
 
   // convergence state (device): dmax, nan, done, at, iters, delta, counter
   DevBuf d_slot_diff, d_state;
@@ -1025,8 +1033,21 @@ int record_sequential(itn_ctx* c, const std::vector<SeqLaunch>& lv, int nsweeps,
 
 extern "C" {
 
-int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
+}  // extern "C"
+
+namespace {
+
+// Pinned staging layout: the convergence state and the tensor-core error flag first, the
+// log-norm totals and flags of itn_bp_solve after them.
+constexpr size_t kPinErrAt = (sizeof(ConvState) + 15) & ~size_t(15);
+constexpr size_t kPinLogzAt = kPinErrAt + 16;
+
+// The solve behind itn_bp_run.  With `defer`, a run without a tolerance (one chunk) leaves
+// its final host synchronisation to the caller: the state copies are enqueued, c->pending
+// is filled, and bp_run_finish completes `res` after the caller has synchronised.
+int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer) {
   if (int r = check_ready(c, true)) return r;
+  c->pending.active = false;
   if (!o) return fail(c, ITN_ERR_ARG, "null options");
   if (int r = ensure_device(c)) return r;
   if (o->maxiter < 0 && !(o->tol >= 0))
@@ -1094,10 +1115,9 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   ConvState hs;
   memset(&hs, 0, sizeof(hs));
   // the convergence state and the tensor-core error flag come back in one pinned area
-  const size_t err_at = (sizeof(ConvState) + 15) & ~size_t(15);
-  if (int r = ensure_pinned(c, err_at + 16)) return r;
+  if (int r = ensure_pinned(c, kPinErrAt + 16)) return r;
   ConvState* h_state = static_cast<ConvState*>(c->h_pin);
-  int* h_tcerr = reinterpret_cast<int*>(static_cast<unsigned char*>(c->h_pin) + err_at);
+  int* h_tcerr = reinterpret_cast<int*>(static_cast<unsigned char*>(c->h_pin) + kPinErrAt);
   const int* d_tcerr = o->precision != ITN_PREC_NATIVE ? tc_err_ptr(c->tc) : nullptr;
   *h_tcerr = 0;
   while (issued < cap) {
@@ -1138,6 +1158,17 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaMemcpyAsync(h_state, conv(c), sizeof(ConvState), cudaMemcpyDeviceToHost, c->stream));
     if (d_tcerr) CK(cudaMemcpyAsync(h_tcerr, d_tcerr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (defer && !use_tol && issued + n >= cap) {
+      // the last (only) chunk of a run without a tolerance: every sweep runs, so the
+      // messages end in buffer cur + n whatever the state says
+      if (o->schedule == ITN_SCHED_PARALLEL) c->cur = (c->cur + n) & 1;
+      c->pending.active = true;
+      c->pending.use_tol = false;
+      c->pending.tc = d_tcerr != nullptr;
+      c->pending.launches = launches + rec_launches;
+      c->pending.ms_before = total_ms;
+      return ITN_OK;
+    }
     CK(cudaStreamSynchronize(c->stream));
     hs = *h_state;
     float ms = 0.f;
@@ -1159,6 +1190,33 @@ int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   }
   if (o->maxiter < 0 && !hs.done) return fail(c, ITN_ERR_TIMEOUT, "no convergence within %lld iterations", (long long)cap);
   return ITN_OK;
+}
+
+// Completes a deferred run after the caller's synchronisation.
+int bp_run_finish(itn_ctx* c, itn_bp_result* res) {
+  if (!c->pending.active) return ITN_OK;
+  c->pending.active = false;
+  const ConvState* h_state = static_cast<const ConvState*>(c->h_pin);
+  const int* h_tcerr = reinterpret_cast<const int*>(static_cast<const unsigned char*>(c->h_pin) + kPinErrAt);
+  if (c->pending.tc && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (res) {
+    res->iterations = h_state->iters;
+    res->at_iteration = h_state->at_iter;
+    res->delta = INFINITY;
+    res->device_ms = c->pending.ms_before + ms;
+    res->kernel_launches = c->pending.launches;
+  }
+  return ITN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
+  return bp_run_impl(c, o, res, false);
 }
 
 int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
@@ -1456,11 +1514,13 @@ int32_t itn_tc_selftest(itn_ctx* c, int32_t* m128_ok, int32_t* m64_ok, double* m
   return ITN_OK;
 }
 
-int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* logze,
-                       double* totals, int32_t* flags) {
-  if (int r = check_ready(c, true)) return r;
-  if (int r = ensure_device(c)) return r;
-  const size_t es = dtype_size(c->dtype);
+}  // extern "C"
+
+namespace {
+
+// Enqueue the vertex / edge scalars, their FP64 logs and the per-network totals and flags
+// of the current messages (no copies, no synchronisation).
+int enqueue_logscalars(itn_ctx* c) {
   const int ne = (int)c->eslots.size();
   CK(c->d_logzv.ensure(std::max<int64_t>(c->nv, 1) * 2 * sizeof(double)));
   CK(c->d_logze.ensure(std::max(ne, 1) * 2 * sizeof(double)));
@@ -1473,6 +1533,20 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
                    c->d_net_vlist.as<int>(), c->d_net_eoff.as<int>(), c->d_net_elist.as<int>(), c->n_nets,
                    c->d_logzv.as<double>(), c->d_logze.as<double>(), c->d_tot.as<double>(),
                    c->d_flags.as<int>(), c->d_lspart.p, part_bytes, c->stream));
+  return ITN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* logze,
+                       double* totals, int32_t* flags) {
+  if (int r = check_ready(c, true)) return r;
+  if (int r = ensure_device(c)) return r;
+  const size_t es = dtype_size(c->dtype);
+  const int ne = (int)c->eslots.size();
+  if (int r = enqueue_logscalars(c)) return r;
   // every requested result goes through one pinned staging area: the copies are queued
   // back to back and waited for once
   struct Part { void* dst; const void* src; size_t bytes; size_t at; };
@@ -1495,6 +1569,50 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
   CK(cudaStreamSynchronize(c->stream));
   for (const Part& p : parts)
     if (p.dst && p.bytes) memcpy(p.dst, h + p.at, p.bytes);
+  return ITN_OK;
+}
+
+int32_t itn_bp_solve(itn_ctx* c, int32_t dtype, const void* tensors, const void* messages_in,
+                     const itn_bp_opts* o, itn_bp_result* res, void* messages_out, double* totals,
+                     int32_t* flags) {
+  if (!c) return ITN_ERR_ARG;
+  if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
+  if (!o) return fail(c, ITN_ERR_ARG, "null options");
+  const size_t tb = (size_t)c->toff[c->nv] * (dtype >= ITN_F32 && dtype <= ITN_C128 ? dtype_size(dtype) : 0);
+  if (int r = set_dtype(c, dtype)) return r;
+  const size_t mb = (size_t)c->moff[c->nslots] * dtype_size(dtype);
+  if ((tb && !tensors) || (mb && !messages_in)) return fail(c, ITN_ERR_ARG, "null tensor or message pointer");
+  if (int r = ensure_device(c)) return r;
+  // inputs: copies queued on the context's stream, no host wait
+  CK(c->d_tens.ensure(tb));
+  if (tb) CK(cudaMemcpyAsync(c->d_tens.p, tensors, tb, cudaMemcpyHostToDevice, c->stream));
+  CK(c->d_msg[0].ensure(mb));
+  CK(c->d_msg[1].ensure(mb));
+  if (mb) CK(cudaMemcpyAsync(c->d_msg[0].p, messages_in, mb, cudaMemcpyHostToDevice, c->stream));
+  c->cur = 0;
+  c->have_tensors = true;
+  c->have_messages = true;
+  if (c->tc) tc_invalidate(c->tc);
+  // the staging is sized before the solve queues its state copies into it (growing it
+  // afterwards would move it under those copies)
+  if (int r = ensure_pinned(c, kPinLogzAt + 20 * (size_t)c->n_nets + 16)) return r;
+  // the solve (its last synchronisation deferred when it has no tolerance)
+  if (int r = bp_run_impl(c, o, res, true)) return r;
+  // log-norm and the messages, then one wait for everything
+  unsigned char* h = static_cast<unsigned char*>(c->h_pin) + kPinLogzAt;
+  double* h_tot = reinterpret_cast<double*>(h);
+  int32_t* h_fl = reinterpret_cast<int32_t*>(h + 16 * (size_t)c->n_nets);
+  if (totals || flags) {
+    if (int r = enqueue_logscalars(c)) return r;
+    CK(cudaMemcpyAsync(h_tot, c->d_tot.p, 16 * (size_t)c->n_nets, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h_fl, c->d_flags.p, 4 * (size_t)c->n_nets, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (messages_out && mb)
+    CK(cudaMemcpyAsync(messages_out, c->d_msg[c->cur].p, mb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (int r = bp_run_finish(c, res)) return r;
+  if (totals) memcpy(totals, h_tot, 16 * (size_t)c->n_nets);
+  if (flags) memcpy(flags, h_fl, 4 * (size_t)c->n_nets);
   return ITN_OK;
 }
 

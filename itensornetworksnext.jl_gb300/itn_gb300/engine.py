@@ -113,8 +113,7 @@ class BPEngine:
         return out
 
     # -- hot path ------------------------------------------------------------------------
-    def run(self, *, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
-            precision="native", split_sweeps=0) -> RunResult:
+    def _opts(self, schedule, edges, maxiter, tol, normalize, precision, split_sweeps):
         o = L.BpOpts()
         o.schedule = {"parallel": L.SCHED_PARALLEL, "sequential": L.SCHED_SEQUENTIAL}[schedule]
         o.maxiter = -1 if maxiter is None else int(maxiter)
@@ -127,6 +126,34 @@ class BPEngine:
             ed = np.ascontiguousarray(edges, dtype=np.int64)
             o.edges = ed.ctypes.data
             o.n_edges = len(ed)
+        return o, ed
+
+    def solve(self, tensors: np.ndarray, messages: np.ndarray, *, messages_out: np.ndarray | None = None,
+              logz: bool = True, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
+              precision="native", split_sweeps=0):
+        """Upload, solve, log-norm and download in one call with one host synchronisation
+        (itn_bp_solve).  Returns (RunResult, log-norm or None, messages)."""
+        t = np.ascontiguousarray(tensors)
+        m = np.ascontiguousarray(messages, dtype=t.dtype)
+        if t.size != int(self.graph.toff[-1]) or m.size != int(self.graph.moff[-1]):
+            raise ValueError("packed tensor or message size does not match the network")
+        out = messages_out if messages_out is not None else np.empty(int(self.graph.moff[-1]), dtype=t.dtype)
+        if out.dtype != t.dtype or out.size != m.size or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("messages_out must be a contiguous array of the network's message size and dtype")
+        o, _keep = self._opts(schedule, edges, maxiter, tol, normalize, precision, split_sweeps)
+        r = L.BpResult()
+        nn = self.graph.n_nets
+        tot = np.empty((nn, 2)) if logz else None
+        fl = np.empty(nn, dtype=np.int32) if logz else None
+        self._check(self.lib.itn_bp_solve(self._ctx, L.DTYPE_CODE[t.dtype], L.ptr(t), L.ptr(m), ctypes.byref(o),
+                                          ctypes.byref(r), L.ptr(out), L.ptr(tot), L.ptr(fl)))
+        self.dtype = t.dtype
+        res = RunResult(r.iterations, r.at_iteration, r.delta, r.device_ms, r.kernel_launches)
+        return res, (self._bethe(tot, fl) if logz else None), out
+
+    def run(self, *, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
+            precision="native", split_sweeps=0) -> RunResult:
+        o, _keep = self._opts(schedule, edges, maxiter, tol, normalize, precision, split_sweeps)
         r = L.BpResult()
         self._check(self.lib.itn_bp_run(self._ctx, ctypes.byref(o), ctypes.byref(r)))
         return RunResult(r.iterations, r.at_iteration, r.delta, r.device_ms, r.kernel_launches)
@@ -190,6 +217,11 @@ class BPEngine:
         fl = np.empty(nn, dtype=np.int32)
         # only the per-network totals and flags are read back
         self._check(self.lib.itn_logscalars(self._ctx, None, None, None, None, L.ptr(tot), L.ptr(fl)))
+        return self._bethe(tot, fl, net)
+
+    def _bethe(self, tot, fl, net=None):
+        """bethe_free_energy from the per-network totals and flags of itn_logscalars."""
+        nn = self.graph.n_nets
         r = dict(totals=tot, flags=fl)
         out = []
         for k in range(nn):

@@ -47,6 +47,7 @@ def test_null_arguments_rejected(lib_built):
     assert lib.itn_create(None, 0, 0) == L.ITN_ERR_ARG
     assert lib.itn_destroy(None) == L.ITN_ERR_ARG
     assert lib.itn_bp_run(None, None, None) == L.ITN_ERR_ARG
+    assert lib.itn_bp_solve(None, 0, None, None, None, None, None, None, None) == L.ITN_ERR_ARG
     assert lib.itn_last_error(None) == b"null context"
 
 

@@ -276,3 +276,48 @@ def test_vertex_scalars_of_d8_norm_vertices(dtype, tol):
         m[g.moff[s]:g.moff[s + 1]] = (x @ np.conj(x).T / 8 + 0.5 * np.eye(8)).ravel()
     with _engine(g, t, m) as e:
         _check_scalars(g, t, m, e, tol)
+
+
+@pytest.mark.parametrize("case", ["tc_mixed", "fp64_tol", "sequential", "fp32_no_logz"])
+def test_one_call_solve_matches_separate_calls(case):
+    """itn_bp_solve (upload, solve, log-norm, download with one host synchronisation) gives
+    exactly what the separate calls give: same messages bit for bit, same iteration count and
+    log-norm -- for a deferred-synchronisation run (no tolerance, tensor cores), a run with a
+    tolerance, the sequential schedule, and without the log-norm."""
+    rng = np.random.default_rng(31)
+    kw, logz = {}, True
+    if case == "tc_mixed":
+        g = G.square_lattice(4, 4, 8, periodic=True, phys=2)
+        t = G.random_tensors(g, rng, np.float32, G.peps_scale(g))
+        m0 = G.identity_messages(g, np.float32)
+        kw = dict(maxiter=6, precision="bf16", split_sweeps=2)
+    elif case == "fp64_tol":
+        g = G.square_lattice(4, 4, 2, periodic=False, phys=2)
+        t = G.random_tensors(g, rng, np.float64)
+        m0 = G.identity_messages(g)
+        kw = dict(maxiter=100, tol=1e-12)
+    elif case == "sequential":
+        g = G.square_lattice(4, 4, 2, periodic=False, phys=2)
+        t = G.random_tensors(g, rng, np.float64)
+        m0 = G.identity_messages(g)
+        kw = dict(schedule="sequential", edges=G.tree_edge_sequence(g), maxiter=3)
+    else:
+        g = G.square_lattice(6, 6, 3, periodic=True, phys=2)
+        t = G.random_tensors(g, rng, np.float32, G.peps_scale(g))
+        m0 = G.identity_messages(g, np.float32)
+        kw = dict(maxiter=9)
+        logz = False
+    with _engine(g, t, m0) as e:
+        r1 = e.run(**kw)
+        want_m = e.messages()
+        want_z = e.bethe_free_energy()
+    with BPEngine(g) as e:
+        r2, z, m = e.solve(t, m0, logz=logz, **kw)
+        assert r2.iterations == r1.iterations and r2.at_iteration == r1.at_iteration
+        np.testing.assert_array_equal(m, want_m)
+        if logz:
+            assert z == want_z
+        else:
+            assert z is None
+        # the context keeps the data, as after the separate calls
+        np.testing.assert_array_equal(e.messages(), want_m)
