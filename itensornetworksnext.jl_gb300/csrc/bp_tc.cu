@@ -1028,6 +1028,8 @@ struct TcEngine {
   int occ[kNumOps] = {0, 0, 0};
   bool persist_ok[kNumOps] = {false, false, false};  // cooperative grid of sm_count CTAs fits
   bool configured = false;  // kernel attributes set and residency measured (once per engine)
+  // persistent launches since the tagged buffers were last cleared (host-side upper bound)
+  uint64_t epoch_uses = 0;
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -1266,6 +1268,23 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
 }
 
 const int* tc_err_ptr(const TcEngine* e) { return e ? e->d_err : nullptr; }
+
+cudaError_t tc_note_launches(TcEngine* e, int n, cudaStream_t st) {
+  // Tags carry a 20-bit epoch that the persistent kernel advances once per launch.  Before
+  // it could come round to the epoch of an entry that was never overwritten since, the
+  // tagged buffers are cleared and the epoch restarts at 1 (all on the stream, ahead of the
+  // launch).
+  if (!e || !e->d_tagged || !e->d_epoch) return cudaSuccess;
+  e->epoch_uses += (uint64_t)std::max(n, 0);
+  if (e->epoch_uses < (1u << 20) - 4096) return cudaSuccess;
+  cudaError_t err = cudaMemsetAsync(e->d_tagged, 0, 4 * e->tagged_stride * sizeof(unsigned long long), st);
+  if (err != cudaSuccess) return err;
+  static const unsigned init[2] = {1u, 0u};
+  err = cudaMemcpyAsync(e->d_epoch, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (err != cudaSuccess) return err;
+  e->epoch_uses = (uint64_t)std::max(n, 0);
+  return cudaSuccess;
+}
 
 
 }  // namespace itn

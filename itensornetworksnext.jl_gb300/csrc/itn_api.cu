@@ -1153,6 +1153,7 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
       c->graphs[key] = exec;
       c->graph_launches[key] = rec_launches;
     }
+    if (o->precision != ITN_PREC_NATIVE) CK(tc_note_launches(c->tc, 2, c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(cudaGraphLaunch(exec, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));

@@ -39,6 +39,10 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
 // Device address of the engine's error flag, non-zero once a bounded wait inside the
 // tensor-core kernel gave up (reset by tc_prepare; null before the first prepare).
 const int* tc_err_ptr(const TcEngine* e);
+// Account for up to `n` persistent launches about to be enqueued (a solve graph holds at
+// most two); clears the tagged buffers and restarts the epoch on the stream before the
+// 20-bit epoch could wrap onto a stale entry.
+cudaError_t tc_note_launches(TcEngine* e, int n, cudaStream_t st);
 // One-CTA tcgen05 self-test (cached per process): M=128 product exact, M=64
 // accumulator lane map found.  lane_of_row may be null (64 entries otherwise).
 cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max_err, int* lane_of_row);
