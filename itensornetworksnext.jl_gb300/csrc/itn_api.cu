@@ -31,6 +31,15 @@ using namespace itn;
 
 namespace {
 
+// Two-layer vertices of at most this many tensor entries form the parallel sweep's small
+// class, launched with CTAs of kSmallBlock threads (one warp: small shared staging and a
+// single-warp barrier let many items share an SM), when the network has at least
+// kSmallMinItemsPerSm items per SM.  Batched complex64 networks: 1.12e8 -> 1.38e8 updates/s
+// (256 entries / 32 threads; 64 threads gave 1.19e8, 512 entries 1.27e8).
+constexpr int64_t kSmallTensor = 256;
+constexpr int kSmallBlock = 32;
+constexpr int kSmallMinItemsPerSm = 16;
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -147,6 +156,12 @@ struct itn_ctx {
   int64_t max_tensor = 1;
   std::vector<int> eslots;  // undirected edges: slot < rev[slot]
   bool scal_d8 = false;     // every vertex: two layers, d = 2, four legs of dimension 8
+  // Parallel-sweep items in two size classes (items_par is sorted by tensor size, largest
+  // first): [0, par_split) large, [par_split, n) small, each class launched with shared
+  // staging sized for its own largest vertex (par_split == n: one class).
+  int par_split = 0;
+  int64_t small_tensor = 1;
+  int small_msg_cap = 1, small_d2 = 1;
 
   // network (device)
   DevBuf d_off, d_rev, d_bond, d_phys, d_toff, d_moff, d_eslots;
@@ -291,9 +306,15 @@ int block_for(itn_ctx* c) {
   return 256;
 }
 
+// Staging limits and CTA size of one item class (null: the whole network's, tuned CTA size).
+struct ClassLimits {
+  int64_t max_tensor;
+  int msg_cap, max_d2, block;
+};
+
 // Prepare GenericArgs and a launch configuration for a list of items.
 int plan_generic(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items, int n_items,
-                 const void* msg_in, void* msg_out) {
+                 const void* msg_in, void* msg_out, const ClassLimits* lim = nullptr) {
   memset(&a, 0, sizeof(a));
   a.layers = c->layers;
   a.off = c->d_off.as<int>();
@@ -309,11 +330,11 @@ int plan_generic(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items,
   a.n_items = n_items;
   a.prog = c->d_prog.as<unsigned>();
   a.nbuf = c->layers == 2 ? c->nbuf : 0;
-  a.buf_elems = (c->max_tensor + 15) & ~15LL;
-  a.msg_cap = c->msg_cap;
-  a.max_d2 = c->max_d2;
+  a.buf_elems = ((lim ? lim->max_tensor : c->max_tensor) + 15) & ~15LL;
+  a.msg_cap = lim ? lim->msg_cap : c->msg_cap;
+  a.max_d2 = lim ? lim->max_d2 : c->max_d2;
   a.normalize = 1;
-  cfg.block = block_for(c);
+  cfg.block = lim ? lim->block : block_for(c);
   bool in_smem = true;
   size_t smem = generic_smem_bytes(c->dtype, a, cfg.block, true);
   if (c->layers == 2 && smem > (size_t)c->smem_optin) {
@@ -609,6 +630,38 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       c->items_par.push_back(p.second);
     }
   }
+  {
+    // size classes of the two-layer parallel sweep: vertices of at most kSmallTensor entries
+    // get their own launch, whose small shared staging lets many more CTAs share an SM
+    const int n = (int)c->items_par.size() / 2;
+    int k = n;
+    if (layers == 2)
+      for (int i = 0; i < n; ++i) {
+        const int u = c->items_par[2 * i];
+        if (c->toff[u + 1] - c->toff[u] <= kSmallTensor) {
+          k = i;
+          break;
+        }
+      }
+    // only networks with many items per SM: for a few waves the second launch's latency
+    // outweighs the residency it buys
+    if (n < kSmallMinItemsPerSm * std::max(c->sm_count, 1)) k = n;
+    c->par_split = k == 0 ? n : k;
+    c->small_tensor = 1;
+    c->small_msg_cap = 1;
+    c->small_d2 = 1;
+    for (int i = c->par_split; i < n; ++i) {
+      const int u = c->items_par[2 * i];
+      c->small_tensor = std::max<int64_t>(c->small_tensor, c->toff[u + 1] - c->toff[u]);
+      int64_t mc = 0;
+      for (int64_t q = c->off[u]; q < c->off[u + 1]; ++q) {
+        const int64_t d2 = (int64_t)c->bond[q] * c->bond[q];
+        mc += d2;
+        c->small_d2 = (int)std::max<int64_t>(c->small_d2, d2);
+      }
+      c->small_msg_cap = (int)std::max<int64_t>(c->small_msg_cap, mc);
+    }
+  }
   c->scal_d8 = layers == 2 && nv > 0;
   for (int64_t u = 0; u < nv && c->scal_d8; ++u) {
     if (c->off[u] != 4 * u || c->off[u + 1] != 4 * u + 4 || c->phys[u] != 2) c->scal_d8 = false;
@@ -857,8 +910,11 @@ int get_seq_plan(itn_ctx* c, const int64_t* edges, int64_t n, SeqPlan& plan) {
 // Launch plans are computed before stream capture (no allocation or occupancy query
 // happens while capturing).
 struct ParPlan {
-  GenericArgs a[2];  // a[i]: reads buffer i, writes buffer i ^ 1
+  GenericArgs a[2];  // a[i]: reads buffer i, writes buffer i ^ 1 (the large-item class)
   LaunchCfg cfg[2];
+  bool two = false;  // a second launch per sweep for the small-item class
+  GenericArgs s[2];
+  LaunchCfg scfg[2];
 };
 
 // Autotuner for the parallel sweep: time one sweep per candidate CTA size (64, 128, 256
@@ -880,13 +936,17 @@ int autotune_sweep(itn_ctx* c) {
     if (plan_generic(c, a, cfg, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, c->d_msg[c->cur].p,
                      c->d_msg[c->cur ^ 1].p))
       continue;
-    float ms = 0.f;
-    for (int rep = 0; rep < 2; ++rep) {  // first launch warms the caches
+    // the first launch warms the caches; the best of the next three is the candidate's time
+    // (single launches of a few microseconds scatter by several percent)
+    float ms = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      float t = 0.f;
       CK(cudaEventRecord(c->ev0, c->stream));
       CK(launch_generic(c->dtype, a, cfg, c->stream));
       CK(cudaEventRecord(c->ev1, c->stream));
       CK(cudaEventSynchronize(c->ev1));
-      CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+      if (rep > 0) ms = std::min(ms, t);
     }
     if (ms < best) {
       best = ms;
@@ -903,14 +963,26 @@ int autotune_sweep(itn_ctx* c) {
 
 int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   const bool use_tol = o->tol >= 0;
+  const int n = (int)c->items_par.size() / 2;
+  p.two = c->layers == 2 && c->par_split > 0 && c->par_split < n;
+  const int nl = p.two ? c->par_split : n;
+  const ClassLimits small{c->small_tensor, c->small_msg_cap, c->small_d2, kSmallBlock};
   for (int in = 0; in < 2; ++in) {
-    if (int r = plan_generic(c, p.a[in], p.cfg[in], c->d_items_par.as<int>(), (int)c->items_par.size() / 2,
-                             c->d_msg[in].p, c->d_msg[in ^ 1].p))
+    if (int r = plan_generic(c, p.a[in], p.cfg[in], c->d_items_par.as<int>(), nl, c->d_msg[in].p,
+                             c->d_msg[in ^ 1].p))
       return r;
     p.a[in].normalize = o->normalize;
     p.a[in].conv = conv(c);
-    p.a[in].fused_step = 1;
+    p.a[in].fused_step = p.two ? 0 : 1;  // with two launches the second one steps the loop
     if (use_tol) p.a[in].slot_diff = c->d_slot_diff.as<double>();
+    if (!p.two) continue;
+    if (int r = plan_generic(c, p.s[in], p.scfg[in], c->d_items_par.as<int>() + 2 * nl, n - nl, c->d_msg[in].p,
+                             c->d_msg[in ^ 1].p, &small))
+      return r;
+    p.s[in].normalize = o->normalize;
+    p.s[in].conv = conv(c);
+    p.s[in].fused_step = 1;
+    if (use_tol) p.s[in].slot_diff = c->d_slot_diff.as<double>();
   }
   return ITN_OK;
 }
@@ -971,6 +1043,10 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
     } else {
       CK(launch_generic(c->dtype, p.a[in], p.cfg[in], c->stream));
+      if (p.two) {
+        CK(launch_generic(c->dtype, p.s[in], p.scfg[in], c->stream));
+        *launches += 1;
+      }
     }
     *launches += 1;
   }

@@ -321,3 +321,29 @@ def test_one_call_solve_matches_separate_calls(case):
             assert z is None
         # the context keeps the data, as after the separate calls
         np.testing.assert_array_equal(e.messages(), want_m)
+
+
+def test_batched_size_classes_match_oracle():
+    """A batch large enough (more than 16 items per SM) for the parallel sweep to launch its
+    small vertices (at most 256 tensor entries) as a second class of one-warp CTAs: the
+    messages of every network still match the oracle, in FP64 to 1e-10 and complex64 to
+    the FP32 bound."""
+    rng = np.random.default_rng(257)
+    nets = []
+    for k in range(96):
+        n = 40 + 2 * (k % 13)
+        edges = G.random_regular_edges(n, 3, rng)
+        bonds = rng.choice([2, 3, 4, 6, 8], size=len(edges))
+        nets.append(G.from_edges(n, edges, bonds, phys=2))
+    g = G.batched(nets)
+    sizes = np.diff(g.toff)
+    assert g.nv >= 16 * 152 and (sizes <= 256).any() and (sizes > 256).any()
+    for dtype, tol in ((np.float64, FP64_TOL), (np.complex64, FP32_TOL)):
+        t = G.random_tensors(g, rng, dtype, G.peps_scale(g))
+        m0 = G.identity_messages(g, dtype)
+        with _engine(g, t, m0) as e:
+            e.run(maxiter=8)
+            m = e.messages()
+        wide = np.complex128 if np.iscomplexobj(t) else np.float64
+        ref, *_ = O.bp_run(g, t.astype(wide), m0.astype(wide), maxiter=8)
+        assert msg_rel(g, m, ref) < tol
