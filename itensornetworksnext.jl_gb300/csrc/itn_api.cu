@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <map>
 #include <memory>
 #include <string>
@@ -31,13 +32,17 @@ using namespace itn;
 
 namespace {
 
-// Two-layer vertices of at most this many tensor entries form the parallel sweep's small
-// class, launched with CTAs of kSmallBlock threads (one warp: small shared staging and a
-// single-warp barrier let many items share an SM), when the network has at least
-// kSmallMinItemsPerSm items per SM.  Batched complex64 networks: 1.12e8 -> 1.38e8 updates/s
-// (256 entries / 32 threads; 64 threads gave 1.19e8, 512 entries 1.27e8).
-constexpr int64_t kSmallTensor = 256;
-constexpr int kSmallBlock = 32;
+// Size classes of the two-layer parallel sweep, for networks with at least
+// kSmallMinItemsPerSm items per SM: vertices of at most kClassMax[i] tensor entries (and more
+// than the next bound) form class i + 1, launched after the larger ones with CTAs of
+// kClassBlock[i] threads and shared staging sized for that class alone; the vertices above
+// kClassMax[0] keep the tuned CTA size.  Small CTAs with small staging let many items share
+// an SM (one warp: a single-warp barrier).  Batched complex64 networks (random 3-regular,
+// bonds 2..8): one launch 1.12e8 updates/s; <= 256 entries in 32-thread CTAs 1.37e8 (64
+// threads 1.19e8); + 257..512 in 64-thread CTAs 1.39e8; + <= 64 entries apart 1.42e8.
+constexpr int kNumSubClasses = 3;
+constexpr int64_t kClassMax[kNumSubClasses] = {512, 256, 64};
+constexpr int kClassBlock[kNumSubClasses] = {64, 32, 32};
 constexpr int kSmallMinItemsPerSm = 16;
 
 struct DevBuf {
@@ -156,12 +161,16 @@ struct itn_ctx {
   int64_t max_tensor = 1;
   std::vector<int> eslots;  // undirected edges: slot < rev[slot]
   bool scal_d8 = false;     // every vertex: two layers, d = 2, four legs of dimension 8
-  // Parallel-sweep items in two size classes (items_par is sorted by tensor size, largest
-  // first): [0, par_split) large, [par_split, n) small, each class launched with shared
-  // staging sized for its own largest vertex (par_split == n: one class).
-  int par_split = 0;
-  int64_t small_tensor = 1;
-  int small_msg_cap = 1, small_d2 = 1;
+  // Parallel-sweep items in size classes (items_par is sorted by tensor size, largest
+  // first), in launch order: contiguous item ranges with their own staging limits and CTA
+  // size; a single class uses the whole network's limits and the tuned CTA size.
+  struct ItemClass {
+    int begin = 0, end = 0;
+    bool own = false;  // own limits (a sub-class), else the network's and the tuned size
+    int64_t max_tensor = 1;
+    int msg_cap = 1, max_d2 = 1, block = 0;
+  };
+  std::vector<ItemClass> par_classes;
 
   // network (device)
   DevBuf d_off, d_rev, d_bond, d_phys, d_toff, d_moff, d_eslots;
@@ -631,36 +640,44 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
     }
   }
   {
-    // size classes of the two-layer parallel sweep: vertices of at most kSmallTensor entries
-    // get their own launch, whose small shared staging lets many more CTAs share an SM
+    // size classes of the two-layer parallel sweep (see kClassMax)
     const int n = (int)c->items_par.size() / 2;
-    int k = n;
-    if (layers == 2)
-      for (int i = 0; i < n; ++i) {
-        const int u = c->items_par[2 * i];
-        if (c->toff[u + 1] - c->toff[u] <= kSmallTensor) {
-          k = i;
-          break;
+    c->par_classes.clear();
+    auto size_of = [&](int i) { const int u = c->items_par[2 * i]; return c->toff[u + 1] - c->toff[u]; };
+    std::vector<int> cut;  // first item of each sub-class (non-increasing sizes)
+    const bool split = layers == 2 && n >= kSmallMinItemsPerSm * std::max(c->sm_count, 1);
+    for (int k = 0; k < kNumSubClasses; ++k) {
+      int i = 0;
+      while (i < n && size_of(i) > kClassMax[k]) ++i;
+      cut.push_back(split ? i : n);
+    }
+    int begin = 0;
+    for (int k = 0; k <= kNumSubClasses; ++k) {
+      const int end = k < kNumSubClasses ? cut[k] : n;
+      if (end <= begin) continue;
+      itn_ctx::ItemClass ic;
+      ic.begin = begin;
+      ic.end = end;
+      ic.own = k > 0;
+      if (ic.own) {
+        ic.block = kClassBlock[k - 1];
+        for (int i = begin; i < end; ++i) {
+          const int u = c->items_par[2 * i];
+          ic.max_tensor = std::max<int64_t>(ic.max_tensor, size_of(i));
+          int64_t mc = 0;
+          for (int64_t q = c->off[u]; q < c->off[u + 1]; ++q) {
+            const int64_t d2 = (int64_t)c->bond[q] * c->bond[q];
+            mc += d2;
+            ic.max_d2 = (int)std::max<int64_t>(ic.max_d2, d2);
+          }
+          ic.msg_cap = (int)std::max<int64_t>(ic.msg_cap, mc);
         }
       }
-    // only networks with many items per SM: for a few waves the second launch's latency
-    // outweighs the residency it buys
-    if (n < kSmallMinItemsPerSm * std::max(c->sm_count, 1)) k = n;
-    c->par_split = k == 0 ? n : k;
-    c->small_tensor = 1;
-    c->small_msg_cap = 1;
-    c->small_d2 = 1;
-    for (int i = c->par_split; i < n; ++i) {
-      const int u = c->items_par[2 * i];
-      c->small_tensor = std::max<int64_t>(c->small_tensor, c->toff[u + 1] - c->toff[u]);
-      int64_t mc = 0;
-      for (int64_t q = c->off[u]; q < c->off[u + 1]; ++q) {
-        const int64_t d2 = (int64_t)c->bond[q] * c->bond[q];
-        mc += d2;
-        c->small_d2 = (int)std::max<int64_t>(c->small_d2, d2);
-      }
-      c->small_msg_cap = (int)std::max<int64_t>(c->small_msg_cap, mc);
+      c->par_classes.push_back(ic);
+      begin = end;
     }
+    // a lone sub-class covers the whole network: plan it as the single class
+    if (c->par_classes.size() == 1) c->par_classes[0].own = false;
   }
   c->scal_d8 = layers == 2 && nv > 0;
   for (int64_t u = 0; u < nv && c->scal_d8; ++u) {
@@ -910,11 +927,9 @@ int get_seq_plan(itn_ctx* c, const int64_t* edges, int64_t n, SeqPlan& plan) {
 // Launch plans are computed before stream capture (no allocation or occupancy query
 // happens while capturing).
 struct ParPlan {
-  GenericArgs a[2];  // a[i]: reads buffer i, writes buffer i ^ 1 (the large-item class)
-  LaunchCfg cfg[2];
-  bool two = false;  // a second launch per sweep for the small-item class
-  GenericArgs s[2];
-  LaunchCfg scfg[2];
+  // per item class, in launch order: a[k][i] reads buffer i, writes buffer i ^ 1
+  std::vector<std::array<GenericArgs, 2>> a;
+  std::vector<std::array<LaunchCfg, 2>> cfg;
 };
 
 // Autotuner for the parallel sweep: time one sweep per candidate CTA size (64, 128, 256
@@ -963,26 +978,22 @@ int autotune_sweep(itn_ctx* c) {
 
 int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   const bool use_tol = o->tol >= 0;
-  const int n = (int)c->items_par.size() / 2;
-  p.two = c->layers == 2 && c->par_split > 0 && c->par_split < n;
-  const int nl = p.two ? c->par_split : n;
-  const ClassLimits small{c->small_tensor, c->small_msg_cap, c->small_d2, kSmallBlock};
-  for (int in = 0; in < 2; ++in) {
-    if (int r = plan_generic(c, p.a[in], p.cfg[in], c->d_items_par.as<int>(), nl, c->d_msg[in].p,
-                             c->d_msg[in ^ 1].p))
-      return r;
-    p.a[in].normalize = o->normalize;
-    p.a[in].conv = conv(c);
-    p.a[in].fused_step = p.two ? 0 : 1;  // with two launches the second one steps the loop
-    if (use_tol) p.a[in].slot_diff = c->d_slot_diff.as<double>();
-    if (!p.two) continue;
-    if (int r = plan_generic(c, p.s[in], p.scfg[in], c->d_items_par.as<int>() + 2 * nl, n - nl, c->d_msg[in].p,
-                             c->d_msg[in ^ 1].p, &small))
-      return r;
-    p.s[in].normalize = o->normalize;
-    p.s[in].conv = conv(c);
-    p.s[in].fused_step = 1;
-    if (use_tol) p.s[in].slot_diff = c->d_slot_diff.as<double>();
+  const size_t nc = c->par_classes.size();
+  p.a.assign(nc, {});
+  p.cfg.assign(nc, {});
+  for (size_t k = 0; k < nc; ++k) {
+    const itn_ctx::ItemClass& ic = c->par_classes[k];
+    const ClassLimits lim{ic.max_tensor, ic.msg_cap, ic.max_d2, ic.block};
+    for (int in = 0; in < 2; ++in) {
+      GenericArgs& a = p.a[k][in];
+      if (int r = plan_generic(c, a, p.cfg[k][in], c->d_items_par.as<int>() + 2 * ic.begin, ic.end - ic.begin,
+                               c->d_msg[in].p, c->d_msg[in ^ 1].p, ic.own ? &lim : nullptr))
+        return r;
+      a.normalize = o->normalize;
+      a.conv = conv(c);
+      a.fused_step = k + 1 == nc ? 1 : 0;  // the last launch of a sweep steps the loop
+      if (use_tol) a.slot_diff = c->d_slot_diff.as<double>();
+    }
   }
   return ITN_OK;
 }
@@ -1042,10 +1053,9 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       cudaError_t e = tc_sweep(c->tc, tr, c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
     } else {
-      CK(launch_generic(c->dtype, p.a[in], p.cfg[in], c->stream));
-      if (p.two) {
-        CK(launch_generic(c->dtype, p.s[in], p.scfg[in], c->stream));
-        *launches += 1;
+      for (size_t k = 0; k < p.a.size(); ++k) {
+        CK(launch_generic(c->dtype, p.a[k][in], p.cfg[k][in], c->stream));
+        if (k > 0) *launches += 1;
       }
     }
     *launches += 1;
