@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
     // staging area
     T* A = bufs;
     item_meta<T, false>(a, u, meta, A, a.gscratch == nullptr);
-    const int z = meta->z, n = meta->n;
+    const int n = meta->n;
     const T* A_g = tens + a.toff[u];
     const bool bulk = meta->bulk != 0;
     if (!bulk)
