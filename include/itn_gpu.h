@@ -49,8 +49,10 @@ enum { ITN_SCHED_PARALLEL = 0, ITN_SCHED_SEQUENTIAL = 1 };
 /* ITN_PREC_NATIVE: arithmetic in the stored dtype on CUDA cores.
  * ITN_PREC_BF16 / ITN_PREC_TF32: tensor-core (tcgen05) contractions with FP32
  * accumulation for all but the last split_sweeps sweeps, which run in split
- * (hi/lo) precision; requires ITN_F32 storage. */
-enum { ITN_PREC_NATIVE = 0, ITN_PREC_BF16 = 1, ITN_PREC_TF32 = 2 };
+ * (hi/lo) precision; requires ITN_F32 storage.
+ * ITN_PREC_TF32X3: every sweep on the tensor cores with TF32 hi/lo operands (three TF32
+ * products per contraction, about FP32 accuracy); split_sweeps is ignored; ITN_F32 storage. */
+enum { ITN_PREC_NATIVE = 0, ITN_PREC_BF16 = 1, ITN_PREC_TF32 = 2, ITN_PREC_TF32X3 = 3 };
 enum { ITN_MSG_IDENTITY_NORMALIZED = 0, ITN_MSG_IDENTITY = 1, ITN_MSG_ONES = 2 };
 
 typedef struct itn_ctx itn_ctx;

@@ -53,18 +53,23 @@ __host__ __device__ constexpr uint32_t tmem_cols_for(int groups) {
 constexpr int kOpBf16 = 0;   // BF16 operands
 constexpr int kOpSplit = 1;  // BF16 hi/lo split operands (3 MMAs per product)
 constexpr int kOpTf32 = 2;   // TF32 operands (kind::tf32, K = 8 per MMA)
-constexpr int kNumOps = 3;
+constexpr int kOpTf32Split = 3;  // TF32 hi/lo split operands (3 kind::tf32 MMAs per product)
+constexpr int kNumOps = 4;
 template <int OP> struct OpT {
-  static constexpr bool split = OP == kOpSplit;
-  static constexpr bool tf32 = OP == kOpTf32;
+  static constexpr bool split = OP == kOpSplit || OP == kOpTf32Split;
+  static constexpr bool tf32 = OP == kOpTf32 || OP == kOpTf32Split;
   static constexpr uint32_t blk = tf32 ? 16384u : 8192u;  // bytes of one 64 x 64 operand block
   static constexpr uint32_t sbo = tf32 ? 2048u : 1024u;   // bytes between 8-row core groups
   static constexpr int ksteps = tf32 ? 8 : 4;             // MMAs per K = 64 (32 bytes of a row each)
   static constexpr int planes = split ? 2 : 1;            // hi [+ lo]
-  // operand image bytes per vertex: BF16 [A_pq hi | A_qp hi | A_pq lo | A_qp lo], TF32 [A_pq | A_qp]
-  static constexpr uint32_t img_vertex = tf32 ? 4u * 16384u : 8u * 8192u;
-  static constexpr int groups = OP == kOpBf16 ? 8 : 4;    // persistent kernel: 4-warp groups per CTA
-  static constexpr int per_sm = OP == kOpBf16 ? 8 : 4;    // per-sweep kernel: CTAs per SM
+  // operand image bytes per vertex: [A_pq hi | A_qp hi (| A_pq lo | A_qp lo)], two 64 x 64
+  // blocks (s = 0, 1) each: BF16 hi + lo (one image serves the BF16 and the split sweeps),
+  // TF32, or TF32 hi + lo
+  static constexpr uint32_t img_vertex = 2u * 2u * (tf32 ? planes : 2u) * blk;
+  // persistent kernel: 4-warp groups per CTA; per-sweep kernel: CTAs per SM (shared memory
+  // per group: 27 KB BF16, 51 KB split / TF32, 99 KB TF32 split)
+  static constexpr int groups = OP == kOpBf16 ? 8 : (OP == kOpTf32Split ? 2 : 4);
+  static constexpr int per_sm = groups;
 };
 
 
@@ -76,7 +81,7 @@ __host__ __device__ __forceinline__ uint32_t blk_off(int r, int k) {
 // byte offset of element (r, k) inside a 64 x 64 block of the mode's element type
 template <int OP>
 __host__ __device__ __forceinline__ uint32_t op_off(int r, int k) {
-  if constexpr (OP == kOpTf32)
+  if constexpr (OpT<OP>::tf32)
     return (uint32_t)((((r >> 3) << 4) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
   else
     return blk_off(r, k);
@@ -179,8 +184,8 @@ __device__ __forceinline__ void store_row_tf32(unsigned char* blk, int r, const 
         make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
 }
 
-// Issue D (+)= A * B^T over K = 64 (K-steps of 32 bytes per row), with the split terms
-// for kOpSplit and kind::tf32 MMAs for kOpTf32.
+// Issue D (+)= A * B^T over K = 64 (K-steps of 32 bytes per row): kind::f16 MMAs on BF16
+// operands or kind::tf32 on TF32 operands, with the hi*lo and lo*hi terms for the split modes.
 template <int OP>
 __device__ __forceinline__ void mma_k64(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t b, uint32_t b_lo,
                                         uint32_t idesc, bool accumulate) {
@@ -188,9 +193,13 @@ __device__ __forceinline__ void mma_k64(uint32_t d, uint32_t a, uint32_t a_lo, u
 #pragma unroll
   for (int j = 0; j < OpT<OP>::ksteps; ++j) {
     const uint32_t ko = (uint32_t)(2 * j) * 128;  // core columns 2j, 2j+1
-    if constexpr (OP == kOpTf32) {
+    if constexpr (OpT<OP>::tf32) {
       ptx::mma_tf32(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc,
                     accumulate || j > 0);
+      if constexpr (OpT<OP>::split) {
+        ptx::mma_tf32(d, ptx::smem_desc(a_lo + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc, 1);
+        ptx::mma_tf32(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b_lo + ko, 128, sbo), idesc, 1);
+      }
     } else {
       ptx::mma_bf16(d, ptx::smem_desc(a + ko, 128, sbo), ptx::smem_desc(b + ko, 128, sbo), idesc,
                     accumulate || j > 0);
@@ -384,13 +393,21 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
         const float w = ma[bo * 8 + ko];
         const uint32_t off = op_off<OP>(bo * 8 + bi, ko * 8);
         if constexpr (O::tf32) {
-          // 8 K-entries = two 16-byte core rows
-          *reinterpret_cast<uint4*>(reg + off) =
-              make_uint4(ptx::to_tf32(w * mb[0]), ptx::to_tf32(w * mb[1]), ptx::to_tf32(w * mb[2]),
-                         ptx::to_tf32(w * mb[3]));
-          *reinterpret_cast<uint4*>(reg + op_off<OP>(bo * 8 + bi, ko * 8 + 4)) =
-              make_uint4(ptx::to_tf32(w * mb[4]), ptx::to_tf32(w * mb[5]), ptx::to_tf32(w * mb[6]),
-                         ptx::to_tf32(w * mb[7]));
+          // 8 K-entries = two 16-byte core rows (and the same in the lo plane when split:
+          // lo = the TF32 rounding of x - hi, exact in FP32)
+          const uint32_t off2 = op_off<OP>(bo * 8 + bi, ko * 8 + 4);
+          uint32_t h[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) h[k] = ptx::to_tf32(w * mb[k]);
+          *reinterpret_cast<uint4*>(reg + off) = make_uint4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<uint4*>(reg + off2) = make_uint4(h[4], h[5], h[6], h[7]);
+          if constexpr (SPLIT) {
+            uint32_t l[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) l[k] = ptx::to_tf32(w * mb[k] - __uint_as_float(h[k]));
+            *reinterpret_cast<uint4*>(reg + O::blk + off) = make_uint4(l[0], l[1], l[2], l[3]);
+            *reinterpret_cast<uint4*>(reg + O::blk + off2) = make_uint4(l[4], l[5], l[6], l[7]);
+          }
         } else if constexpr (SPLIT) {
           float hv[8], lv[8];
 #pragma unroll
@@ -424,15 +441,19 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     //    hold s = 0 and store XT0 now; warps 2, 3 keep s = 1 packed in registers until the
     //    first half of G2 has consumed XT0 (G2's accumulator overwrites their TMEM lanes).
     const int xr = (warp * 32 + lane) & 63;
-    // BF16: 32 packed pairs (+ 32 lo pairs when split); TF32: 64 TF32 patterns
-    uint32_t hk[O::tf32 ? 64 : 32], lk[SPLIT ? 32 : 1];
+    // BF16: 32 packed pairs (+ 32 lo pairs when split); TF32: 64 TF32 patterns (+ 64 lo)
+    constexpr int kHk = O::tf32 ? 64 : 32;
+    uint32_t hk[kHk], lk[SPLIT ? kHk : 1];
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       float v[32];
       tmem_ld32(tq + 32 * half, v);
       if constexpr (O::tf32) {
 #pragma unroll
-        for (int e = 0; e < 32; ++e) hk[32 * half + e] = ptx::to_tf32(v[e]);
+        for (int e = 0; e < 32; ++e) {
+          hk[32 * half + e] = ptx::to_tf32(v[e]);
+          if constexpr (SPLIT) lk[32 * half + e] = ptx::to_tf32(v[e] - __uint_as_float(hk[32 * half + e]));
+        }
       } else {
         pack_row32<SPLIT>(v, hk + 16 * half, lk + (SPLIT ? 16 * half : 0));
       }
@@ -440,6 +461,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     auto store_xt = [&]() {
       if constexpr (O::tf32) {
         store_row_tf32(reg, xr, *reinterpret_cast<uint32_t(*)[64]>(hk));
+        if constexpr (SPLIT) store_row_tf32(reg + O::blk, xr, *reinterpret_cast<uint32_t(*)[64]>(lk));
       } else {
         store_row_packed(reg, xr, *reinterpret_cast<uint32_t(*)[32]>(hk));
         if constexpr (SPLIT) store_row_packed(reg + O::blk, xr, *reinterpret_cast<uint32_t(*)[32]>(lk));
@@ -672,15 +694,18 @@ __global__ void __launch_bounds__(256) tc_image_kernel(const float* __restrict__
   }
 }
 
-// TF32 image, per vertex [A_pq(s=0,1) | A_qp(s=0,1)], 16 KB per block
+// TF32 image, per vertex [A_pq(s=0,1) | A_qp(s=0,1)] (+ the same for the lo parts when
+// SPLIT: lo = the TF32 rounding of x - hi), 16 KB per block
+template <bool SPLIT>
 __global__ void __launch_bounds__(256) tc_image_tf32_kernel(const float* __restrict__ tens, int nv,
                                                             unsigned char* __restrict__ img) {
-  constexpr uint32_t blk = OpT<kOpTf32>::blk;
+  using O = OpT<SPLIT ? kOpTf32Split : kOpTf32>;
+  constexpr uint32_t blk = O::blk;
   __shared__ float t[64 * kImgLd];
   const int u = blockIdx.x >> 1, s = blockIdx.x & 1;
   if (u >= nv) return;
   stage_block(tens, u, s, t);
-  unsigned char* base = img + (size_t)u * OpT<kOpTf32>::img_vertex + (size_t)s * blk;
+  unsigned char* base = img + (size_t)u * O::img_vertex + (size_t)s * blk;
   for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
     const int r = ((i >> 7) << 3) + (i & 7), k0 = ((i >> 3) & 15) << 2;
     uint32_t pq[4], qp[4];
@@ -692,6 +717,16 @@ __global__ void __launch_bounds__(256) tc_image_tf32_kernel(const float* __restr
     const size_t o = (size_t)i * 16;
     *reinterpret_cast<uint4*>(base + o) = make_uint4(pq[0], pq[1], pq[2], pq[3]);
     *reinterpret_cast<uint4*>(base + 2 * blk + o) = make_uint4(qp[0], qp[1], qp[2], qp[3]);
+    if constexpr (SPLIT) {
+      uint32_t lpq[4], lqp[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        lpq[j] = ptx::to_tf32(t[r * kImgLd + k0 + j] - __uint_as_float(pq[j]));
+        lqp[j] = ptx::to_tf32(t[(k0 + j) * kImgLd + r] - __uint_as_float(qp[j]));
+      }
+      *reinterpret_cast<uint4*>(base + 4 * blk + o) = make_uint4(lpq[0], lpq[1], lpq[2], lpq[3]);
+      *reinterpret_cast<uint4*>(base + 6 * blk + o) = make_uint4(lqp[0], lqp[1], lqp[2], lqp[3]);
+    }
   }
 }
 
@@ -1020,13 +1055,16 @@ struct TcEngine {
   size_t image_bytes = 0;
   unsigned char* image_tf32 = nullptr;  // TF32 per vertex [A_pq | A_qp]
   size_t image_tf32_bytes = 0;
+  bool have_tf32x3 = false;  // the TF32 hi/lo image matches the current tensors
+  unsigned char* image_tf32x3 = nullptr;  // TF32 per vertex [A_pq hi | A_qp hi | A_pq lo | A_qp lo]
+  size_t image_tf32x3_bytes = 0;
   int* d_err = nullptr;
   unsigned long long* d_tagged = nullptr;  // persistent kernel: 4 buffers of tagged entries
   size_t tagged_stride = 0;
   unsigned* d_epoch = nullptr;
   int sm_count = 0;
-  int occ[kNumOps] = {0, 0, 0};
-  bool persist_ok[kNumOps] = {false, false, false};  // cooperative grid of sm_count CTAs fits
+  int occ[kNumOps] = {0, 0, 0, 0};
+  bool persist_ok[kNumOps] = {false, false, false, false};  // cooperative grid of sm_count CTAs fits
   bool configured = false;  // kernel attributes set and residency measured (once per engine)
   // persistent launches since the tagged buffers were last cleared (host-side upper bound)
   uint64_t epoch_uses = 0;
@@ -1038,6 +1076,7 @@ void tc_destroy(TcEngine* e) {
   if (!e) return;
   if (e->image) cudaFree(e->image);
   if (e->image_tf32) cudaFree(e->image_tf32);
+  if (e->image_tf32x3) cudaFree(e->image_tf32x3);
   if (e->d_err) cudaFree(e->d_err);
   if (e->d_tagged) cudaFree(e->d_tagged);
   if (e->d_epoch) cudaFree(e->d_epoch);
@@ -1048,6 +1087,7 @@ void tc_invalidate(TcEngine* e) {
   if (e) {
     e->valid = false;
     e->have_tf32 = false;
+    e->have_tf32x3 = false;
   }
 }
 
@@ -1085,12 +1125,13 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
                        int precision, cudaStream_t st, const char** why) {
   (void)toff;
   *why = nullptr;
-  if (precision != 1 && precision != 2) {
+  if (precision < 1 || precision > 3) {
     *why = "unknown tensor-core precision";
     return cudaSuccess;
   }
-  const bool want_tf32 = precision == 2;
-  if (e->valid && (!want_tf32 || e->have_tf32)) return cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
+  const bool want_tf32 = precision == 2, want_tf32x3 = precision == 3;
+  if (e->valid && (!want_tf32 || e->have_tf32) && (!want_tf32x3 || e->have_tf32x3))
+    return cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
   if (layers != 2) {
     *why = "tensor-core sweep needs a norm network (layers = 2)";
     return cudaSuccess;
@@ -1109,7 +1150,7 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   int m128 = 0, m64 = 0;
   cudaError_t err = tc_run_probe(st, &m128, &m64, nullptr, nullptr);
   if (err != cudaSuccess) return err;
-  if (!m128 || !m64 || (want_tf32 && !g_probe.tf32_ok)) {
+  if (!m128 || !m64 || ((want_tf32 || want_tf32x3) && !g_probe.tf32_ok)) {
     *why = "tensor-core self-test failed on this device";
     return cudaSuccess;
   }
@@ -1142,12 +1183,15 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       tc_configure<kOpBf16>(e, smem_sm, regs_sm);
       tc_configure<kOpSplit>(e, smem_sm, regs_sm);
       tc_configure<kOpTf32>(e, smem_sm, regs_sm);
+      tc_configure<kOpTf32Split>(e, smem_sm, regs_sm);
       e->configured = true;
     }
     if (getenv("ITN_DEBUG"))
-      fprintf(stderr, "[itn] tc residency: bf16 %d, split %d, tf32 %d CTAs/SM; persistent %d/%d/%d; sms %d\n",
-              e->occ[0], e->occ[1], e->occ[2], (int)e->persist_ok[0], (int)e->persist_ok[1],
-              (int)e->persist_ok[2], e->sm_count);
+      fprintf(stderr,
+              "[itn] tc residency: bf16 %d, split %d, tf32 %d, tf32 split %d CTAs/SM; persistent %d/%d/%d/%d; "
+              "sms %d\n",
+              e->occ[0], e->occ[1], e->occ[2], e->occ[3], (int)e->persist_ok[0], (int)e->persist_ok[1],
+              (int)e->persist_ok[2], (int)e->persist_ok[3], e->sm_count);
     // tagged message buffers of the persistent kernel, zeroed once (epochs start at 1)
     const size_t stride = (size_t)std::max<int64_t>(nv, 1) * 4 * 64;
     if (e->tagged_stride < stride) {
@@ -1177,11 +1221,26 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       if (err != cudaSuccess) return err;
       e->image_tf32_bytes = tf32_bytes;
     }
-    tc_image_tf32_kernel<<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv,
-                                                             e->image_tf32);
+    tc_image_tf32_kernel<false><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens),
+                                                                    (int)nv, e->image_tf32);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     e->have_tf32 = true;
+  }
+  if (want_tf32x3) {
+    const size_t bytes = (size_t)nv * OpT<kOpTf32Split>::img_vertex;
+    if (e->image_tf32x3_bytes < bytes) {
+      if (e->image_tf32x3) cudaFree(e->image_tf32x3);
+      e->image_tf32x3 = nullptr;
+      err = cudaMalloc(&e->image_tf32x3, bytes);
+      if (err != cudaSuccess) return err;
+      e->image_tf32x3_bytes = bytes;
+    }
+    tc_image_tf32_kernel<true><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens),
+                                                                   (int)nv, e->image_tf32x3);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    e->have_tf32x3 = true;
   }
   e->nv = (int)nv;
   e->d_off = d_off;
@@ -1192,12 +1251,18 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   return cudaGetLastError();
 }
 
-static int tc_op(const TcRun& r) { return r.split ? kOpSplit : (r.precision == 2 ? kOpTf32 : kOpBf16); }
+// precision 3 (TF32 hi/lo) runs every sweep in that mode; otherwise the split flag picks the
+// BF16 hi/lo sweep and precision 2 TF32 for the others
+static int tc_op(const TcRun& r) {
+  if (r.precision == 3) return kOpTf32Split;
+  return r.split ? kOpSplit : (r.precision == 2 ? kOpTf32 : kOpBf16);
+}
 
 static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   TcArgs a;
   a.rev = e->d_rev;
-  a.image = tc_op(r) == kOpTf32 ? e->image_tf32 : e->image;
+  const int op = tc_op(r);
+  a.image = op == kOpTf32 ? e->image_tf32 : op == kOpTf32Split ? e->image_tf32x3 : e->image;
   a.msg_in = reinterpret_cast<const float*>(r.msg_in);
   a.msg_out = reinterpret_cast<float*>(r.msg_out);
   a.nv = e->nv;
@@ -1242,10 +1307,11 @@ cudaError_t launch_persistent(TcEngine* e, const TcArgs& a, cudaStream_t st) {
 cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st) {
   if (!e || !e->valid) return cudaErrorInvalidValue;
   const int op = tc_op(r);
-  if (op == kOpTf32 && !e->have_tf32) return cudaErrorInvalidValue;
+  if ((op == kOpTf32 && !e->have_tf32) || (op == kOpTf32Split && !e->have_tf32x3)) return cudaErrorInvalidValue;
   TcArgs a = tc_args(e, r);
   if (op == kOpSplit) return launch_sweep<kOpSplit>(e, a, st);
   if (op == kOpTf32) return launch_sweep<kOpTf32>(e, a, st);
+  if (op == kOpTf32Split) return launch_sweep<kOpTf32Split>(e, a, st);
   return launch_sweep<kOpBf16>(e, a, st);
 }
 
@@ -1253,7 +1319,7 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
   *used = false;
   if (!e || !e->valid || r.slot_diff) return cudaErrorInvalidValue;
   const int op = tc_op(r);
-  if (op == kOpTf32 && !e->have_tf32) return cudaErrorInvalidValue;
+  if ((op == kOpTf32 && !e->have_tf32) || (op == kOpTf32Split && !e->have_tf32x3)) return cudaErrorInvalidValue;
   // two sweeps would write the plain output buffer while the first sweep's readers of
   // the same buffer may still be running; tags hold 12 bits of sweep index
   if (!e->persist_ok[op] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
@@ -1262,6 +1328,7 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
   cudaError_t err;
   if (op == kOpSplit) err = launch_persistent<kOpSplit>(e, a, st);
   else if (op == kOpTf32) err = launch_persistent<kOpTf32>(e, a, st);
+  else if (op == kOpTf32Split) err = launch_persistent<kOpTf32Split>(e, a, st);
   else err = launch_persistent<kOpBf16>(e, a, st);
   if (err == cudaSuccess) *used = true;
   return err;

@@ -1007,7 +1007,7 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
     // Without a convergence test the BF16 sweeps and then the split sweeps each run as
     // one persistent launch; a device that cannot host the cooperative grid gets one
     // launch per sweep.
-    const int nsplit = std::min(nsweeps, std::max(0, o->split_sweeps));
+    const int nsplit = o->precision == ITN_PREC_TF32X3 ? 0 : std::min(nsweeps, std::max(0, o->split_sweeps));
     int t = 0;
     for (int part = 0; part < 2; ++part) {
       const int n = part ? nsplit : nsweeps - nsplit;

@@ -18,7 +18,7 @@ ITN_OK, ITN_ERR_ARG, ITN_ERR_CUDA, ITN_ERR_OOM, ITN_ERR_NAN, ITN_ERR_TIMEOUT, \
     ITN_ERR_UNSUPPORTED, ITN_ERR_STATE = range(8)
 F32, F64, C64, C128 = range(4)
 SCHED_PARALLEL, SCHED_SEQUENTIAL = 0, 1
-PREC_NATIVE, PREC_BF16, PREC_TF32 = 0, 1, 2
+PREC_NATIVE, PREC_BF16, PREC_TF32, PREC_TF32X3 = 0, 1, 2, 3
 MSG_IDENTITY_NORMALIZED, MSG_IDENTITY, MSG_ONES = 0, 1, 2
 
 DTYPE_CODE = {np.dtype(np.float32): F32, np.dtype(np.float64): F64,

@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib as L
 from .graphs import Graph
 
-_PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16, "tf32": L.PREC_TF32}
+_PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16, "tf32": L.PREC_TF32, "tf32x3": L.PREC_TF32X3}
 
 
 @dataclass

@@ -185,7 +185,7 @@ function download_messages!(cache, d::DeviceNetwork, nn::NormNetwork)
 end
 
 precision_code(p::Symbol) = p === :native ? Int32(0) : p === :bf16 ? Int32(1) :
-    p === :tf32 ? Int32(2) : throw(ArgumentError("unknown precision $p"))
+    p === :tf32 ? Int32(2) : p === :tf32x3 ? Int32(3) : throw(ArgumentError("unknown precision $p"))
 
 # The whole solve in one call: beliefpropagation(nn, messages; edges, stopping_criterion,
 # message_update_algorithm = GPUMessageUpdate(...)) dispatches here through AI.solve.

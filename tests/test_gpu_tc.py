@@ -51,7 +51,8 @@ def _one_sweep(g, t, m0, **kw):
         return msg_rel(g, e.messages(), ref)
 
 
-@pytest.mark.parametrize("prec,split,tol", [("bf16", False, 3e-2), ("tf32", False, 5e-3), ("bf16", True, 2e-4)])
+@pytest.mark.parametrize("prec,split,tol", [("bf16", False, 3e-2), ("tf32", False, 5e-3), ("bf16", True, 2e-4),
+                                            ("tf32x3", False, 1e-5)])
 def test_one_sweep_against_fp32(prec, split, tol):
     """Non-symmetric messages near the normalised identity (the regime of a BP solve):
     a transposed bra/ket index anywhere would show up as an O(1) error."""
@@ -73,6 +74,9 @@ def test_split_recovers_ill_conditioned_update():
     e_split = _one_sweep(g, t, m0, precision="bf16", split_sweeps=1)
     print(f"ill-conditioned: bf16 {e_bf16:.3e} split {e_split:.3e}")
     assert e_split < 1e-2 and e_split * 20 < e_bf16
+    e_x3 = _one_sweep(g, t, m0, precision="tf32x3")
+    print(f"ill-conditioned: tf32x3 {e_x3:.3e}")
+    assert e_x3 * 20 < e_split
 
 
 @pytest.mark.parametrize("prec", ["bf16", "tf32"])
@@ -100,6 +104,35 @@ def test_mixed_logz_32x32_against_fp64(prec):
     assert rel <= 1e-6
 
 
+def test_tf32x3_solve_matches_fp32_accuracy():
+    """Every sweep in TF32 hi/lo on the tensor cores: the log-norm and the per-site
+    log-scalars of a 30-sweep 32x32 solve are as close to the FP64 solve as the FP32
+    CUDA-core solve's are (within 3x, plus a 1e-6 floor per site)."""
+    g, t = _lattice(32, 32)
+    with BPEngine(g) as e64:
+        e64.set_tensors(t)
+        e64.init_messages()
+        e64.run(maxiter=30)
+        lz64 = e64.bethe_free_energy()
+        lzv64 = e64.logscalars()["logzv"][:, 0]
+    with BPEngine(g) as e:
+        e.set_tensors(t.astype(np.float32))
+        e.init_messages()
+        r = e.run(maxiter=30, precision="tf32x3")
+        assert r.iterations == 30
+        lz = e.bethe_free_energy()
+        lzv = e.logscalars()["logzv"][:, 0]
+        e.init_messages()
+        e.run(maxiter=30)
+        lz32 = e.bethe_free_energy()
+        lzv32 = e.logscalars()["logzv"][:, 0]
+    site, site32 = np.max(np.abs(lzv - lzv64)), np.max(np.abs(lzv32 - lzv64))
+    print(f"tf32x3: rel {abs(lz - lz64) / abs(lz64):.3e} site {site:.3e}; fp32 rel {abs(lz32 - lz64) / abs(lz64):.3e}"
+          f" site {site32:.3e}")
+    assert abs(lz - lz64) <= 1e-8 * abs(lz64)
+    assert site <= 3 * site32 + 1e-6
+
+
 def test_tc_convergence_flag():
     g, t = _lattice(6, 3)
     with BPEngine(g) as e:
@@ -122,7 +155,7 @@ def test_tc_rejects_unsupported_network():
 @pytest.mark.parametrize("L,n,split,prec", [(32, 7, 0, "bf16"), (32, 6, 2, "bf16"), (4, 5, 1, "bf16"),
                                             (3, 9, 0, "bf16"), (48, 5, 1, "bf16"), (32, 5, 0, "tf32"),
                                             (4, 6, 3, "tf32"), (4, 2, 0, "bf16"), (4, 1, 0, "bf16"),
-                                            (4, 3, 5, "bf16")])
+                                            (4, 3, 5, "bf16"), (32, 5, 0, "tf32x3"), (4, 4, 0, "tf32x3")])
 def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     """Without a convergence test the sweeps run as one cooperative launch per precision
     part (tagged message entries instead of kernel boundaries); with one the engine
