@@ -397,7 +397,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if mode == "native" else f"{mode}+split",
+        "dtype": "f32" if mode == "native" else ("tf32 hi/lo" if mode == "tf32x3" else f"{mode}+split"),
         "data": "synthetic (seeded N(0,1)/sqrt(d D^4) PEPS)",
         "config": {"workload": f"peps {LX}x{LY} periodic norm network D={BOND} d={PHYS}, "
                                f"{SWEEPS} parallel sweeps per step (device-timed solve; the Bethe "
@@ -661,7 +661,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
-                    choices=["native", "bf16", "tf32"])
+                    choices=["native", "bf16", "tf32", "tf32x3"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
                     help="skip the secondary configurations (gradient, batched, 16x16, exact 6x6)")
