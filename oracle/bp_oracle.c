@@ -2,9 +2,9 @@
  * bp_oracle.c -- CPU restatement of ITensorNetworksNext.jl's belief-propagation hot
  * path (message updates, iterate_diff, vertex/edge scalars, bethe_free_energy).
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke check
- * and the CPU-baseline leg of the benchmark call it; the GPU library never links,
- * loads or falls back to it.
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU results are compared with:
+ * the tests, the smoke check and the CPU-baseline leg of the benchmark call it; the GPU
+ * library never links, loads or falls back to it.
  *
  * Reference semantics restated (paths inside ITensorNetworksNext.jl):
  *   src/beliefpropagation/beliefpropagation.jl:69-92   beliefpropagation entry

@@ -1,7 +1,7 @@
 """CPU oracle for the belief-propagation / contract_network hot path.
 
 TEST INFRASTRUCTURE ONLY.  The tests, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` import this module as the checker; the GPU library
+leg of ``bench.py`` import this module to compare against; the GPU library
 (``libitn_gpu.so``) and the ``itn_gb300`` package never import, link or call it.
 
 The BP arithmetic lives in ``bp_oracle.c`` (a C restatement of
