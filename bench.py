@@ -644,7 +644,7 @@ def bench_apply_layer(device):
         cpu = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": len(gates) / cpu, "unit": "gates/s", "cores": 1, "kind": "port",
                                "sample": "the same 128 gates, numpy restatement, one by one"}
-    except Exception as exc:  # the oracle is a checker; its absence does not void the GPU number
+    except Exception as exc:  # the CPU restatement is only a baseline: its absence leaves the GPU number
         out["cpu_baseline"] = {"unavailable": str(exc)}
     return out
 
