@@ -277,8 +277,12 @@ int32_t itn_sweep_vjp(itn_ctx *ctx, int32_t normalized, const void *cot_out, voi
  * Device arrays use the layout of itn_graph_upload / itn_tensors_upload: int32 d_off
  * (nv+1), d_rev, d_bond (per slot), d_phys (nv); int64 d_toff (nv+1), d_moff (nslots+1);
  * max_tensor_elems bounds every vertex's tensor.  Outputs: d_total = (re, im) of
- * sum log Zv - sum log Ze, d_flags as in itn_logscalars.  Work is enqueued on `stream`
- * (a cudaStream_t, may be NULL) and the outputs are ready when it completes. */
+ * sum log Zv - sum log Ze, d_flags as in itn_logscalars plus three bits for vertices the
+ * call cannot contract (each makes its Z_u NaN, so the total is NaN): bit3 a tensor larger
+ * than max_tensor_elems, bit4 more than 16 legs, bit5 a one-layer vertex whose physical
+ * dimension is not 1 (one-layer networks need phys = 1, as in itn_graph_upload).  Work is
+ * enqueued on `stream` (a cudaStream_t, may be NULL) and the outputs are ready when it
+ * completes. */
 int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int32_t layers,
                                 int64_t nv, int64_t nslots, int64_t max_tensor_elems,
                                 const int32_t *d_off, const int32_t *d_rev, const int32_t *d_bond,

@@ -10,10 +10,16 @@
 // contraction buffers) in one file-scope __device__ array of kStaticScratchBytes.
 //
 // The array belongs to the process: every GPU that loads the library holds it until the
-// process exits.  All calls share it and it keeps the last call's contents; nothing in it
-// needs to start at zero (every entry read by a call is written earlier in the same call),
-// but two calls that overlap on the GPU (different streams, or different host threads on
-// one device) race on it and must be ordered by the caller.
+// process exits.  All calls share it and it keeps the last call's contents; the one word
+// that must start at zero (the bad-vertex bits) is cleared on the stream at the start of
+// every call, and every other entry a call reads is written earlier in the same call.  Two
+// calls that overlap on the GPU (different streams, or different host threads on one
+// device) race on it and must be ordered by the caller.
+//
+// Limits checked on the device, where the caller's arrays are: a vertex with more than
+// kNaMaxLegs legs, a vertex whose tensor exceeds max_tensor_elems, and (one-layer networks)
+// a vertex whose physical dimension is not 1 each make that Z_u NaN and set a flag bit
+// (bits 3, 4 and 5 of d_flags) instead of reading or writing out of bounds.
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current (host code may not use the symbol
@@ -36,6 +42,11 @@ namespace {
 constexpr size_t kStaticScratchBytes = 16u << 20;  // 16 MiB
 constexpr int kMaxDevices = 64;
 constexpr int kNaThreads = 256;
+constexpr int kNaMaxLegs = 16;              // legs per vertex (shared index tables)
+constexpr size_t kNaHeaderBytes = 256;      // bad-vertex bits at the start of the array
+constexpr int kBadTooLarge = 8;             // flag bit 3: tensor larger than max_tensor_elems
+constexpr int kBadTooManyLegs = 16;         // flag bit 4: more than kNaMaxLegs legs
+constexpr int kBadPlainPhys = 32;           // flag bit 5: one-layer vertex with phys != 1
 
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
@@ -60,13 +71,30 @@ __device__ T na_block_sum(T v, T* red) {
 template <typename T>
 __global__ void na_vertex_kernel(int layers, int nv, const int* off, const int* rev, const int* bond,
                                  const int* phys, const long long* toff, const long long* moff,
-                                 const T* tens, const T* msgs, T* zv, T* planes, long long plane_elems) {
-  __shared__ int dims[16], inner[16];
+                                 const T* tens, const T* msgs, T* zv, T* planes, long long plane_elems,
+                                 long long max_elems, int* bad) {
+  __shared__ int dims[kNaMaxLegs], inner[kNaMaxLegs];
   __shared__ T red[32];
   T* p0 = planes + (size_t)blockIdx.x * 2 * plane_elems;
   T* p1 = p0 + plane_elems;
   for (int u = blockIdx.x; u < nv; u += gridDim.x) {
     const int s0 = off[u], z = off[u + 1] - s0;
+    const long long n_ll = toff[u + 1] - toff[u];
+    // block-uniform checks (every thread reads the same values): a vertex the shared tables,
+    // the scratch planes or the one-layer sum cannot hold gets Z_u = NaN and a flag bit
+    const int why = (z < 0 || z > kNaMaxLegs) ? kBadTooManyLegs
+                    : (layers == 2 && (n_ll > max_elems || n_ll > plane_elems)) ? kBadTooLarge
+                    : (layers == 1 && phys[u] != 1) ? kBadPlainPhys : 0;
+    if (why) {
+      if (threadIdx.x == 0) {
+        T nanv = tzero<T>();
+        if constexpr (is_cplx<T>::value) nanv.x = nan("");
+        else nanv = (T)nan("");
+        zv[u] = nanv;
+        atomicOr(bad, why);
+      }
+      continue;
+    }
     if (threadIdx.x == 0) {
       int in = 1;
       for (int l = z - 1; l >= 0; --l) {
@@ -77,19 +105,8 @@ __global__ void na_vertex_kernel(int layers, int nv, const int* off, const int* 
     }
     __syncthreads();
     const T* A = tens + toff[u];
-    const int n = (int)(toff[u + 1] - toff[u]);
+    const int n = (int)n_ll;
     T acc = tzero<T>();
-    if (layers == 2 && n > plane_elems) {
-      // max_tensor_elems understated this vertex: no plane write, Z_u becomes NaN
-      if (threadIdx.x == 0) {
-        T bad = tzero<T>();
-        if constexpr (is_cplx<T>::value) bad.x = nan("");
-        else bad = (T)nan("");
-        zv[u] = bad;
-      }
-      __syncthreads();
-      continue;
-    }
     if (layers == 2) {
       const T* cur = A;
       T* nxt = p0;
@@ -148,9 +165,10 @@ __device__ __forceinline__ void na_log(T z, double& re, double& im) {
 
 // One block: total = sum_u log Z_u - sum_e log Z_e in FP64 (bethe_free_energy,
 // messagecache.jl:185-201); flags bit0 any Re Z_u < 0, bit1 any Re Z_e < 0, bit2 any Z_e == 0.
+// Bits 3-5 come from the vertex kernel's bad-vertex word.
 template <typename T>
 __global__ void na_sum_kernel(int nv, int nslots, const int* rev, const T* zv, const T* ze, double* total,
-                              int* flags) {
+                              int* flags, const int* bad) {
   __shared__ double sre[32], sim[32];
   __shared__ int sfl[32];
   double are = 0, aim = 0;
@@ -192,7 +210,7 @@ __global__ void na_sum_kernel(int nv, int nslots, const int* rev, const T* zv, c
     }
     total[0] = r;
     total[1] = i;
-    *flags = f;
+    *flags = f | *bad;
   }
 }
 
@@ -209,36 +227,55 @@ int run_static(cudaStream_t st, int sm_count, void* scratch, int layers, int64_t
                const int32_t* phys, const int64_t* toff, const int64_t* moff, const void* tens,
                const void* msgs, double* total, int32_t* flags, char* errbuf, int errlen) {
   const size_t es = sizeof(T);
+  // checked before any size arithmetic so that nothing below can wrap around
+  if (layers == 2 && max_tensor > (int64_t)(kStaticScratchBytes / (2 * es))) {
+    char msg[256];
+    snprintf(msg, sizeof(msg),
+             "max_tensor_elems %lld needs more than the static scratch of %zu bytes for one CTA's planes",
+             (long long)max_tensor, kStaticScratchBytes);
+    set_err(errbuf, errlen, msg);
+    return ITN_ERR_ARG;
+  }
   const size_t zv_bytes = ((size_t)nv * es + 255) & ~(size_t)255;
   const size_t ze_bytes = ((size_t)nslots * es + 255) & ~(size_t)255;
   const long long plane = (max_tensor + 31) & ~31LL;
   const size_t per_cta = layers == 2 ? 2 * (size_t)plane * es : 0;
-  if (zv_bytes + ze_bytes + (per_cta ? per_cta : 0) > kStaticScratchBytes) {
+  if (kNaHeaderBytes + zv_bytes + ze_bytes + per_cta > kStaticScratchBytes) {
     char msg[256];
     snprintf(msg, sizeof(msg),
              "network needs %zu bytes of scratch (vertex/edge scalars %zu, one CTA's planes %zu); "
              "the static scratch holds %zu",
-             zv_bytes + ze_bytes + per_cta, zv_bytes + ze_bytes, per_cta, kStaticScratchBytes);
+             kNaHeaderBytes + zv_bytes + ze_bytes + per_cta, zv_bytes + ze_bytes, per_cta, kStaticScratchBytes);
     set_err(errbuf, errlen, msg);
     return ITN_ERR_ARG;
   }
   int grid = (int)std::min<int64_t>(nv, (int64_t)sm_count * 2);
-  if (per_cta) grid = (int)std::min<size_t>(grid, (kStaticScratchBytes - zv_bytes - ze_bytes) / per_cta);
+  if (per_cta)
+    grid = (int)std::min<size_t>(grid, (kStaticScratchBytes - kNaHeaderBytes - zv_bytes - ze_bytes) / per_cta);
   grid = std::max(grid, 1);
   unsigned char* base = reinterpret_cast<unsigned char*>(scratch);
-  T* zv = reinterpret_cast<T*>(base);
-  T* ze = reinterpret_cast<T*>(base + zv_bytes);
-  T* planes = reinterpret_cast<T*>(base + zv_bytes + ze_bytes);
+  int* bad = reinterpret_cast<int*>(base);
+  T* zv = reinterpret_cast<T*>(base + kNaHeaderBytes);
+  T* ze = reinterpret_cast<T*>(base + kNaHeaderBytes + zv_bytes);
+  T* planes = reinterpret_cast<T*>(base + kNaHeaderBytes + zv_bytes + ze_bytes);
+  // the bad-vertex bits are the only scratch that must start at zero
+  cudaError_t ce = cudaMemsetAsync(bad, 0, sizeof(int), st);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    set_err(errbuf, errlen, cudaGetErrorString(ce));
+    return ITN_ERR_CUDA;
+  }
   if (nv > 0)
     na_vertex_kernel<T><<<grid, kNaThreads, 0, st>>>(layers, (int)nv, off, rev, bond, phys,
                                                     reinterpret_cast<const long long*>(toff),
                                                     reinterpret_cast<const long long*>(moff),
                                                     reinterpret_cast<const T*>(tens),
-                                                    reinterpret_cast<const T*>(msgs), zv, planes, plane);
+                                                    reinterpret_cast<const T*>(msgs), zv, planes, plane,
+                                                    (long long)max_tensor, bad);
   if (nslots > 0)
     na_edge_kernel<T><<<(int)((nslots * 32 + 255) / 256), 256, 0, st>>>(
         (int)nslots, rev, reinterpret_cast<const long long*>(moff), reinterpret_cast<const T*>(msgs), ze);
-  na_sum_kernel<T><<<1, 256, 0, st>>>((int)nv, (int)nslots, rev, zv, ze, total, flags);
+  na_sum_kernel<T><<<1, 256, 0, st>>>((int)nv, (int)nslots, rev, zv, ze, total, flags, bad);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_err(errbuf, errlen, cudaGetErrorString(e));

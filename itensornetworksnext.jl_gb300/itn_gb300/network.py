@@ -534,17 +534,37 @@ def vertex_scalar(factors, messages, vertex):
     return vertex_scalars(factors, messages, [vertex])[0]
 
 
-def edge_scalar(factors, messages, edge):
-    """<m(u->v), m(v->u)> (messagecache.jl:153-157)."""
-    flat, r = _scalars(factors, messages)
-    s = flat.slot[tuple(edge)]
-    es = flat.g.undirected_slots().tolist()
-    return r["ze"][es.index(min(s, int(flat.g.rev[s])))]
+def edge_scalar(cache: MessageCache, edge):
+    """edge_scalar(cache, edge) (messagecache.jl:153-157): contract_network of the two
+    messages of an edge, m(u->v) and m(v->u), over all their shared names."""
+    return edge_scalars(cache, [tuple(edge)])[0]
 
 
-def edge_scalars(factors, messages):
-    flat, r = _scalars(factors, messages)
-    return list(r["ze"])
+def edge_scalars(cache: MessageCache, edges=None):
+    """edge_scalars(cache[, edges]) (messagecache.jl:159-178): one scalar per edge of
+    ``edges`` (default: every edge of the cache), skipping repeats and reverses, in order.
+    All pairs are contracted in one device call: each pair becomes a two-vertex component
+    whose messages are the flattened pair, so its edge scalar is their full contraction."""
+    edges = [tuple(e) for e in (cache.keys() if edges is None else edges)]
+    seen, keep = set(), []
+    for e in edges:
+        r = (e[1], e[0])
+        if e in seen or r in seen:
+            continue
+        seen.add(e)
+        keep.append(e)
+    if not keep:
+        return []
+    a = [np.asarray(cache[e].data).ravel() for e in keep]
+    b = [np.asarray(cache[(e[1], e[0])].permute(cache[e].dimnames)).ravel() for e in keep]
+    dt = np.result_type(*[x.dtype for x in a + b], np.float64)
+    g = G.batched([G.from_edges(2, [(0, 1)], [x.size], phys=1, layers=1) for x in a])
+    mm = np.concatenate([np.concatenate([x, y]) for x, y in zip(a, b)]).astype(dt)
+    with BPEngine(g) as e:
+        e.set_tensors(np.ones(int(g.toff[-1]), dtype=dt))
+        e.set_messages(mm)
+        ze = e.logscalars()["ze"]
+    return list(ze)
 
 
 def region_scalar(factors, messages, region):

@@ -111,7 +111,7 @@ def test_vertex_region_scalars():
     assert np.isclose(N.region_scalar(tn, cache, [(0,)]), N.vertex_scalar(tn, cache, (0,)))
     assert np.isclose(N.region_scalar(tn, cache, [(1,), (2,)]),
                       np.prod(N.vertex_scalars(tn, cache, [(1,), (2,)])), rtol=1e-6)
-    assert np.isclose(N.edge_scalar(tn, cache, ((0,), (1,))), 2.0)
+    assert np.isclose(N.edge_scalar(cache, ((0,), (1,))), 2.0)
     assert abs(N.iterate_diff(cache, cache.copy())) <= 10 * np.finfo(float).eps
 
 
@@ -190,3 +190,36 @@ def test_contract_network_orders():
     r1 = N.contract_network([A, B, C, D], alg=N.Exact(order_alg=N.LeftAssociative()))
     r2 = N.contract_network([A, B, C, D], alg=N.Exact(order_alg=N.Greedy()))
     assert np.array_equal(r1.data, r2.data)
+
+
+def test_edge_scalars_of_a_norm_network_cache():
+    """edge_scalar(cache, edge) / edge_scalars(cache) (messagecache.jl:153-178): the full
+    contraction of the two messages of each edge, one value per undirected edge; the
+    messages of the two directions are stored with their names in different orders."""
+    rng = np.random.default_rng(21)
+    links = _grid_links(2, 3, 3)
+    verts = [(x, y) for x in range(2) for y in range(3)]
+    site = {v: N.Index(2) for v in verts}
+    tn = _random_tn(links, verts, np.complex128, rng, site)
+    nn = N.normnetwork(tn)
+    cache = N.message_environment("one", nn)
+    for e in cache.keys():
+        t = cache[e]
+        data = rng.standard_normal(t.data.shape) + 1j * rng.standard_normal(t.data.shape)
+        if e[0] > e[1]:  # reversed name order on one direction
+            cache[e] = N.ITensor(np.transpose(data), list(reversed(t.inds)))
+        else:
+            cache[e] = N.ITensor(data, t.inds)
+    got = N.edge_scalars(cache)
+    want = []
+    seen = set()
+    for e in cache.keys():
+        if (e[1], e[0]) in seen:
+            continue
+        seen.add(e)
+        a, b = cache[e], cache[(e[1], e[0])]
+        want.append(np.sum(a.data * b.permute(a.dimnames)))
+    assert len(got) == len(links) == len(want)
+    np.testing.assert_allclose(got, want, rtol=1e-12)
+    e0 = next(iter(cache.keys()))
+    assert np.isclose(N.edge_scalar(cache, e0), want[0], rtol=1e-12)

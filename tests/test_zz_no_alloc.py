@@ -31,17 +31,19 @@ def _dev(torch, arr):
     return torch.from_numpy(np.ascontiguousarray(arr)).cuda()
 
 
-def _static_logz(lib, torch, g, t, m, code):
+def _static_logz(lib, torch, g, t, m, code, max_tensor=None, phys=None):
     dev = dict(
         off=_dev(torch, g.off.astype(np.int32)), rev=_dev(torch, g.rev.astype(np.int32)),
-        bond=_dev(torch, g.bond.astype(np.int32)), phys=_dev(torch, g.phys.astype(np.int32)),
+        bond=_dev(torch, g.bond.astype(np.int32)),
+        phys=_dev(torch, (g.phys if phys is None else phys).astype(np.int32)),
         toff=_dev(torch, g.toff.astype(np.int64)), moff=_dev(torch, g.moff.astype(np.int64)),
         tens=_dev(torch, t), msgs=_dev(torch, m))
     total = torch.zeros(2, dtype=torch.float64, device="cuda")
     flags = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     err = ctypes.create_string_buffer(256)
     stream = torch.cuda.current_stream().cuda_stream
-    max_tensor = int(np.max(np.diff(g.toff)))
+    if max_tensor is None:
+        max_tensor = int(np.max(np.diff(g.toff)))
     results = []
     for _ in range(2):  # two calls in a row share the static scratch
         total.zero_()
@@ -56,7 +58,8 @@ def _static_logz(lib, torch, g, t, m, code):
     return results
 
 
-@pytest.mark.parametrize("dtype,tol", [(np.float64, 1e-10), (np.float32, 2e-4)])
+@pytest.mark.parametrize("dtype,tol", [(np.float64, 1e-10), (np.float32, 2e-4), (np.complex128, 1e-10),
+                                       (np.complex64, 2e-4)])
 def test_static_scratch_matches_logscalars(lib, dtype, tol):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(7)
@@ -72,7 +75,41 @@ def test_static_scratch_matches_logscalars(lib, dtype, tol):
     for total, flags in _static_logz(lib, torch, g, t, m, code):
         assert flags == int(ref["flags"][0])
         assert abs(total[0] - ref["totals"][0][0]) <= tol * abs(ref["totals"][0][0])
-        assert abs(total[1] - ref["totals"][0][1]) <= tol * max(1.0, abs(ref["totals"][0][1]))
+        # complex: the imaginary part of a sum of logs is defined modulo 2 pi
+        dim = np.angle(np.exp(1j * (total[1] - ref["totals"][0][1])))
+        assert abs(dim) <= tol * max(1.0, abs(ref["totals"][0][1]))
+
+
+def test_static_scratch_flags_vertices_it_cannot_contract(lib):
+    """A max_tensor_elems below the largest tensor (bit 3), a vertex with 17 legs (bit 4)
+    and a one-layer vertex with a physical index (bit 5) each give NaN and their flag bit,
+    and the call after them, with the right sizes, is exact again (the bits start at zero
+    on every call)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    g = G.square_lattice(4, 4, 2, periodic=True, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m = G.identity_messages(g)
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.set_messages(m)
+        ref = e.logscalars()["totals"][0][0]
+    for total, flags in _static_logz(lib, torch, g, t, m, L.F64, max_tensor=int(np.max(np.diff(g.toff))) - 1):
+        assert flags & 8 and np.isnan(total[0])
+    for total, flags in _static_logz(lib, torch, g, t, m, L.F64):
+        assert flags == 0 and abs(total[0] - ref) <= 1e-10 * abs(ref)
+    # a star: vertex 0 with 17 legs of dimension 2 (2 * 2^17 tensor entries)
+    star = G.from_edges(18, [(0, k) for k in range(1, 18)], 2, phys=2)
+    ts = G.random_tensors(star, rng, np.float64)
+    for total, flags in _static_logz(lib, torch, star, ts, G.identity_messages(star), L.F64):
+        assert flags & 16 and np.isnan(total[0])
+    # one-layer network handed a physical dimension of 2 on vertex 5
+    gp = G.square_lattice(4, 4, 2, periodic=True, phys=1, layers=1)
+    tp = G.random_tensors(gp, rng, np.float64)
+    phys = gp.phys.copy()
+    phys[5] = 2
+    for total, flags in _static_logz(lib, torch, gp, tp, G.identity_messages(gp), L.F64, phys=phys):
+        assert flags & 32 and np.isnan(total[0])
 
 
 def test_static_scratch_plain_network(lib):
