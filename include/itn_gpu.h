@@ -291,6 +291,16 @@ int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int
                                 const void *d_messages, double *d_total, int32_t *d_flags,
                                 char *errbuf, int32_t errbuf_len);
 
+/* Fault injection for tests, with no counterpart in the reference (it has no device code
+ * to fail).  ITN_FAULT_WAIT_NS: elapsed-time limit in ns of the tensor-core sweep's bounded
+ * waits on other items' messages (value <= 0 restores the default of 2 s); a wait that runs
+ * out makes the kernel stop early, release its resources and the call return
+ * ITN_ERR_TIMEOUT, with the device and the context still usable.  ITN_FAULT_ALLOC: the next
+ * `value` device allocations the library makes on the calling thread fail, so the calls
+ * making them return ITN_ERR_OOM (the host-side stand-in for exhausted device memory). */
+enum { ITN_FAULT_WAIT_NS = 1, ITN_FAULT_ALLOC = 2 };
+int32_t itn_inject_fault(itn_ctx *ctx, int32_t kind, int64_t value);
+
 /* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product
  * (M = 128 and M = 64, K = 64) against exact host arithmetic.  m128_ok / m64_ok report
  * success; max_err is the largest absolute error of the M = 128 product; lane_of_row

@@ -40,7 +40,6 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kBlk = 8192;                 // bytes of one 64 x 64 BF16 operand block
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
-constexpr uint32_t kMaxDepPolls = 1u << 22; // bounded waits on another item (64 ns apart)
 constexpr int kTmemCols = 64;
 // TMEM columns a CTA of `groups` groups allocates: 64 per group, rounded up to the power of
 // two that tcgen05.alloc requires
@@ -142,6 +141,7 @@ struct TcArgs {
   unsigned long long* tagged;  // persistent kernel: 4 buffers of tagged entries
   size_t tagged_stride;        // entries per tagged buffer (64 per slot)
   unsigned* epoch;             // persistent kernel: [0] epoch of the tags, [1] CTA ticket
+  unsigned long long wait_ns;  // give up a wait on another item's message after this long
 };
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -280,8 +280,8 @@ __device__ __forceinline__ void fetch_in(const TcArgs& a, uint32_t epoch, int it
   }
 }
 
-// Wait (bounded; giving up early once another group has raised the error flag) until
-// both entries carry the tag of sweep t.
+// Wait (bounded by a.wait_ns of elapsed time, read every 64 polls; giving up early once
+// another group has raised the error flag) until both entries carry the tag of sweep t.
 __device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int item, int t, int l0, int e0,
                                         unsigned long long& w0, unsigned long long& w1) {
   const uint32_t want = sweep_tag(epoch, t);
@@ -290,11 +290,13 @@ __device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int ite
   const unsigned long long* tb = a.tagged + (size_t)(t & 3) * a.tagged_stride;
   const unsigned long long* p0 = tb + 64 * a.rev[4 * u + l0] + e0;
   const unsigned long long* p1 = tb + 64 * a.rev[4 * u + l0 + 2] + e0;
-  for (uint32_t polls = 0; polls < kMaxDepPolls; ++polls) {
+  const uint64_t t0 = ptx::globaltimer();
+  for (uint32_t polls = 1;; ++polls) {
     if ((uint32_t)(w0 >> 32) != want) w0 = ld_tagged(p0);
     if ((uint32_t)(w1 >> 32) != want) w1 = ld_tagged(p1);
     if ((uint32_t)(w0 >> 32) == want && (uint32_t)(w1 >> 32) == want) return true;
     if (*reinterpret_cast<volatile int*>(a.err)) return false;
+    if ((polls & 63) == 0 && ptx::globaltimer() - t0 > a.wait_ns) break;
     __nanosleep(32);
   }
   atomicExch(a.err, 2);
@@ -344,6 +346,8 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   const uint32_t Aimg = sbase + L.img, Alo = 2 * O::blk;
   const uint32_t R = sbase + L.reg;
   uint32_t ph_load = 0, ph_mma = 0;
+  // tid 0: an image copy is in flight / an MMA wait gave up (the exit path waits for those)
+  bool ld_pend = false, mma_lost = false;
   bool ok = true;    // group-uniform: false once a bounded wait gave up
   bool fail = false; // this thread's waits (folded into `ok` once per item)
   constexpr uint32_t idesc128 = O::tf32 ? ptx::idesc_tf32_f32(128, 64) : ptx::idesc_bf16_f32(128, 64);
@@ -356,7 +360,10 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   unsigned long long w0 = 0, w1 = 0;
   // the operand image is static: its copy starts before the done flag is read
   const bool first = gid < n_items;
-  if (first && tid == 0) issue_image<OP>(sm + L.img, a.image, gid, bar_load);
+  if (first && tid == 0) {
+    issue_image<OP>(sm + L.img, a.image, gid, bar_load);
+    ld_pend = true;
+  }
   const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
   if (first && !skip) fetch_in(a, epoch, gid, 0, l0, e0, w0, w1);
   int t = (first && !skip) ? 0 : nsweeps, item = gid;
@@ -429,12 +436,13 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     // 2. first GEMM: rows (s, r) of the image times P^T -> TMEM cols 0..63
     if (tid == 0) {
       if (!ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls)) fail = true;
+      else ld_pend = false;
       ptx::tc_fence_after();
       mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc128, false);
       ptx::mma_commit(bar_mma);
     }
     ph_load ^= 1;
-    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
     ph_mma ^= 1;
     ptx::tc_fence_after();
     // 3. epilogue 1: accumulator row (s, r) -> row r of XT_s (BF16 hi [+ lo]).  Warps 0, 1
@@ -478,7 +486,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
       mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc64, false);
       ptx::mma_commit(bar_mma);
     }
-    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
     ph_mma ^= 1;
     if (warp >= 2) store_xt();
     ptx::fence_proxy_async_smem();
@@ -488,11 +496,14 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
       mma_k64<OP>(tmem, Aimg + O::blk, Aimg + Alo + O::blk, R, R + O::blk, idesc64, true);
       ptx::mma_commit(bar_mma);
     }
-    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = true;
+    if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
     ph_mma ^= 1;
     ptx::tc_fence_after();
     // the image's only readers are done: fetch the next item's image and incoming entries
-    if (tid == 0 && has_next) issue_image<OP>(sm + L.img, a.image, item2, bar_load);
+    if (tid == 0 && has_next) {
+      issue_image<OP>(sm + L.img, a.image, item2, bar_load);
+      ld_pend = true;
+    }
     if (has_next) fetch_in(a, epoch, item2, t2, l0, e0, w0, w1);
     // 5. epilogue 2 from registers.  Z = Z[(bh,bl)][(kh,kl)] (bra indices of legs H, Lg
     //    on rows, kets on columns) is read with the 16x32bx2 shape: thread (w, l) holds row
@@ -612,13 +623,13 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     item = item2;
     t = t2;
   }
-  if (!ok && tid == 0) {
-    // a wait gave up: let the copy / MMAs already issued finish (bounded) before the
-    // shared memory and TMEM are released
-    ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);
-    ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls);
+  if (tid == 0 && (ld_pend || mma_lost)) {
+    // a copy is still in flight (the next item's image, or the unused first image when the
+    // run had already converged) or an MMA wait gave up: let them finish (bounded) before
+    // the shared memory and TMEM are released.  Every other MMA was waited for in its item.
+    if (ld_pend) ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);
+    if (mma_lost) ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls);
   }
-  if (skip && first && tid == 0) ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls);  // unused image copy
   ptx::tc_fence_before();
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -1068,6 +1079,7 @@ struct TcEngine {
   bool configured = false;  // kernel attributes set and residency measured (once per engine)
   // persistent launches since the tagged buffers were last cleared (host-side upper bound)
   uint64_t epoch_uses = 0;
+  uint64_t wait_ns = kDefaultWaitNs;  // limit of a wait on another item's message
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -1274,6 +1286,7 @@ static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   a.tagged = e->d_tagged;
   a.tagged_stride = e->tagged_stride;
   a.epoch = e->d_epoch;
+  a.wait_ns = e->wait_ns;
   return a;
 }
 
@@ -1335,6 +1348,10 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
 }
 
 const int* tc_err_ptr(const TcEngine* e) { return e ? e->d_err : nullptr; }
+
+void tc_set_wait_limit(TcEngine* e, uint64_t ns) {
+  if (e) e->wait_ns = ns;
+}
 
 cudaError_t tc_note_launches(TcEngine* e, int n, cudaStream_t st) {
   // Tags carry a 20-bit epoch that the persistent kernel advances once per launch.  Before

@@ -45,6 +45,10 @@ constexpr int64_t kClassMax[kNumSubClasses] = {512, 256, 64};
 constexpr int kClassBlock[kNumSubClasses] = {64, 32, 32};
 constexpr int kSmallMinItemsPerSm = 16;
 
+// Device allocations that itn_inject_fault(ITN_FAULT_ALLOC) has told the calling thread to
+// fail (a host-side stand-in for running out of device memory).
+thread_local int64_t t_fail_allocs = 0;
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -53,6 +57,10 @@ struct DevBuf {
   }
   cudaError_t ensure(size_t n) {
     if (n <= bytes && p) return cudaSuccess;
+    if (t_fail_allocs > 0) {
+      --t_fail_allocs;
+      return cudaErrorMemoryAllocation;
+    }
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
@@ -223,6 +231,8 @@ struct itn_ctx {
 
   // tensor-core engine (bp_tc.cu), created on first use
   TcEngine* tc = nullptr;
+  // limit of the tensor-core sweep's waits on other items' messages (itn_inject_fault)
+  uint64_t wait_ns = kDefaultWaitNs;
 
   ~itn_ctx() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -447,6 +457,25 @@ int32_t itn_destroy(itn_ctx* c) {
 }
 
 const char* itn_last_error(const itn_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int32_t itn_inject_fault(itn_ctx* c, int32_t kind, int64_t value) {
+  if (!c) return ITN_ERR_ARG;
+  switch (kind) {
+    case ITN_FAULT_WAIT_NS:
+      c->wait_ns = value > 0 ? (uint64_t)value : kDefaultWaitNs;
+      if (c->tc) tc_set_wait_limit(c->tc, c->wait_ns);
+      // the limit is a kernel argument baked into the cached solve graphs
+      for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+      c->graphs.clear();
+      c->graph_launches.clear();
+      return ITN_OK;
+    case ITN_FAULT_ALLOC:
+      if (value < 0) return fail(c, ITN_ERR_ARG, "allocation failure count < 0");
+      t_fail_allocs = value;
+      return ITN_OK;
+  }
+  return fail(c, ITN_ERR_ARG, "unknown fault kind %d", kind);
+}
 
 int32_t itn_synchronize(itn_ctx* c) {
   if (!c) return ITN_ERR_ARG;
@@ -752,6 +781,8 @@ int32_t itn_tensors_upload(itn_ctx* c, int32_t dtype, const void* packed) {
   if (!packed && c->toff[c->nv] > 0) return fail(c, ITN_ERR_ARG, "null tensor pointer");
   if (int r = ensure_device(c)) return r;
   if (int r = set_dtype(c, dtype)) return r;
+  // a failed upload leaves no tensors behind (a failed allocation frees the old buffer)
+  c->have_tensors = false;
   const size_t bytes = (size_t)c->toff[c->nv] * dtype_size(dtype);
   CK(c->d_tens.ensure(bytes));
   if (bytes) CK(cudaMemcpyAsync(c->d_tens.p, packed, bytes, cudaMemcpyHostToDevice, c->stream));
@@ -1144,7 +1175,10 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
     if (o->schedule != ITN_SCHED_PARALLEL)
       return fail(c, ITN_ERR_UNSUPPORTED, "tensor-core precision modes run the parallel schedule");
     if (c->dtype != ITN_F32) return fail(c, ITN_ERR_UNSUPPORTED, "tensor-core precision modes need float32 storage");
-    if (!c->tc) c->tc = tc_create();
+    if (!c->tc) {
+      c->tc = tc_create();
+      tc_set_wait_limit(c->tc, c->wait_ns);
+    }
     const char* why = nullptr;
     cudaError_t e = tc_prepare(c->tc, c->layers, c->nv, c->off.data(), c->bond.data(), c->phys.data(),
                                c->d_off.as<int>(), c->d_rev.as<int>(), c->d_moff.as<long long>(),

@@ -39,6 +39,11 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
 // Device address of the engine's error flag, non-zero once a bounded wait inside the
 // tensor-core kernel gave up (reset by tc_prepare; null before the first prepare).
 const int* tc_err_ptr(const TcEngine* e);
+// Elapsed-time limit (ns) of a sweep kernel's wait on another item's message; a wait that
+// runs out sets the error flag (ITN_ERR_TIMEOUT for the caller).  Applies to launches
+// recorded after the call.
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;
+void tc_set_wait_limit(TcEngine* e, uint64_t ns);
 // Account for up to `n` persistent launches about to be enqueued (a solve graph holds at
 // most two); clears the tagged buffers and restarts the epoch on the stream before the
 // 20-bit epoch could wrap onto a stale entry.

@@ -50,6 +50,36 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Global nanosecond timer (used to bound waits by elapsed time).
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// try_wait with a suspend-time hint: a thread whose phase is not complete may sleep up to
+// hint_ns nanoseconds (it resumes early when the phase completes) instead of spinning.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the phase of the given parity, sleeping in try_wait between checks, and give up
+// once limit_ns nanoseconds have passed since the first failed check; returns false then.
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_try_wait_hint(bar, parity, 20000u)) return true;
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait_hint(bar, parity, 20000u)) return true;
+    if (globaltimer() - t0 > limit_ns) return false;
+  }
+}
+
 // ---- bulk (1-D) TMA copy global -> shared, completion via mbarrier tx bytes -----------
 __device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes,
                                          uint64_t* bar) {

@@ -20,6 +20,7 @@ F32, F64, C64, C128 = range(4)
 SCHED_PARALLEL, SCHED_SEQUENTIAL = 0, 1
 PREC_NATIVE, PREC_BF16, PREC_TF32, PREC_TF32X3 = 0, 1, 2, 3
 MSG_IDENTITY_NORMALIZED, MSG_IDENTITY, MSG_ONES = 0, 1, 2
+FAULT_WAIT_NS, FAULT_ALLOC = 1, 2
 
 DTYPE_CODE = {np.dtype(np.float32): F32, np.dtype(np.float64): F64,
               np.dtype(np.complex64): C64, np.dtype(np.complex128): C128}
@@ -33,7 +34,7 @@ EXPORTED = [
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
     "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest", "itn_bp_grad",
     "itn_sweep_vjp", "itn_logz_static_scratch", "itn_contraction_order", "itn_contract_network",
-    "itn_apply_gates", "itn_bp_solve",
+    "itn_apply_gates", "itn_bp_solve", "itn_inject_fault",
 ]
 
 
@@ -117,6 +118,7 @@ def _declare(lib):
                                         ctypes.POINTER(_I32), _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logz_static_scratch": (_I32, [_I32, _VP, _I32, _I32, _I64, _I64, _I64, _VP, _VP, _VP, _VP,
                                            _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_char_p, _I32]),
+        "itn_inject_fault": (_I32, [_VP, _I32, _I64]),
         "itn_apply_gates": (_I32, [_VP, _I32, _I64, _VP, _VP, _I64, _VP, _I64, _VP, _I64, _I32,
                                    ctypes.c_double, _I32, _VP, _I64, _VP, _I64, _VP,
                                    ctypes.POINTER(ctypes.c_double)]),

@@ -186,6 +186,13 @@ class BPEngine:
         self._check(self.lib.itn_sweep_vjp(self._ctx, int(bool(normalized)), L.ptr(a), L.ptr(out)))
         return out
 
+    def inject_fault(self, kind: str, value: int):
+        """Test hook (itn_inject_fault): ``"wait_ns"`` sets the elapsed-time limit of the
+        tensor-core sweep's waits on other items' messages (<= 0: the default); ``"alloc"``
+        makes the next ``value`` device allocations on this thread fail."""
+        k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC}[kind]
+        self._check(self.lib.itn_inject_fault(self._ctx, k, int(value)))
+
     def tc_selftest(self) -> dict:
         """Run the one-CTA tcgen05 self-test (exact BF16 products, M=64 lane map)."""
         a = ctypes.c_int32()
