@@ -293,12 +293,14 @@ int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int
 
 /* Fault injection for tests, with no counterpart in the reference (it has no device code
  * to fail).  ITN_FAULT_WAIT_NS: elapsed-time limit in ns of the tensor-core sweep's bounded
- * waits on other items' messages (value <= 0 restores the default of 2 s); a wait that runs
- * out makes the kernel stop early, release its resources and the call return
+ * waits on other items' messages (value <= 0 restores the default of 2 s).
+ * ITN_FAULT_STALL (value 1 / 0): in the persistent tensor-core sweeps, one such wait looks
+ * for a message that is never written, so it runs out after the limit; the kernel then stops
+ * early, waits for its own copies, releases its resources and the call returns
  * ITN_ERR_TIMEOUT, with the device and the context still usable.  ITN_FAULT_ALLOC: the next
  * `value` device allocations the library makes on the calling thread fail, so the calls
  * making them return ITN_ERR_OOM (the host-side stand-in for exhausted device memory). */
-enum { ITN_FAULT_WAIT_NS = 1, ITN_FAULT_ALLOC = 2 };
+enum { ITN_FAULT_WAIT_NS = 1, ITN_FAULT_ALLOC = 2, ITN_FAULT_STALL = 3 };
 int32_t itn_inject_fault(itn_ctx *ctx, int32_t kind, int64_t value);
 
 /* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product

@@ -142,6 +142,7 @@ struct TcArgs {
   size_t tagged_stride;        // entries per tagged buffer (64 per slot)
   unsigned* epoch;             // persistent kernel: [0] epoch of the tags, [1] CTA ticket
   unsigned long long wait_ns;  // give up a wait on another item's message after this long
+  int stall;                   // fault injection: group 0's wait in sweep 1 looks for a tag never written
 };
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -283,8 +284,10 @@ __device__ __forceinline__ void fetch_in(const TcArgs& a, uint32_t epoch, int it
 // Wait (bounded by a.wait_ns of elapsed time, read every 64 polls; giving up early once
 // another group has raised the error flag) until both entries carry the tag of sweep t.
 __device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int item, int t, int l0, int e0,
-                                        unsigned long long& w0, unsigned long long& w1) {
-  const uint32_t want = sweep_tag(epoch, t);
+                                        unsigned long long& w0, unsigned long long& w1, bool stall = false) {
+  // sweep index 4095 is never written (a persistent launch runs at most 4095 sweeps and the
+  // last one writes the plain output), so a stalled wait can only run out
+  const uint32_t want = sweep_tag(epoch, stall ? 4095 : t);
   if ((uint32_t)(w0 >> 32) == want && (uint32_t)(w1 >> 32) == want) return true;
   const int u = item >> 1;
   const unsigned long long* tb = a.tagged + (size_t)(t & 3) * a.tagged_stride;
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     const int s0 = 4 * u;
     // pair (A, B) builds P; pair (H, Lg) receives the outgoing messages
     const int pa = h ? 2 : 0, pb = pa + 1, H = h ? 0 : 2, Lg = H + 1;
-    if (!wait_in(a, epoch, item, t, l0, e0, w0, w1)) fail = true;
+    if (!wait_in(a, epoch, item, t, l0, e0, w0, w1, PERSIST && a.stall && gid == 0 && t == 1)) fail = true;
     msg[l0 * 64 + e0] = __uint_as_float((uint32_t)w0);
     msg[(l0 + 2) * 64 + e0] = __uint_as_float((uint32_t)w1);
     group_sync(bar_id);
@@ -1080,6 +1083,7 @@ struct TcEngine {
   // persistent launches since the tagged buffers were last cleared (host-side upper bound)
   uint64_t epoch_uses = 0;
   uint64_t wait_ns = kDefaultWaitNs;  // limit of a wait on another item's message
+  int stall = 0;                      // fault injection (TcArgs::stall)
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -1287,6 +1291,7 @@ static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   a.tagged_stride = e->tagged_stride;
   a.epoch = e->d_epoch;
   a.wait_ns = e->wait_ns;
+  a.stall = e->stall;
   return a;
 }
 
@@ -1351,6 +1356,10 @@ const int* tc_err_ptr(const TcEngine* e) { return e ? e->d_err : nullptr; }
 
 void tc_set_wait_limit(TcEngine* e, uint64_t ns) {
   if (e) e->wait_ns = ns;
+}
+
+void tc_set_stall(TcEngine* e, int on) {
+  if (e) e->stall = on ? 1 : 0;
 }
 
 cudaError_t tc_note_launches(TcEngine* e, int n, cudaStream_t st) {

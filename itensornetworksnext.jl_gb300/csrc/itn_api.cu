@@ -233,6 +233,7 @@ struct itn_ctx {
   TcEngine* tc = nullptr;
   // limit of the tensor-core sweep's waits on other items' messages (itn_inject_fault)
   uint64_t wait_ns = kDefaultWaitNs;
+  int stall = 0;  // itn_inject_fault(ITN_FAULT_STALL)
 
   ~itn_ctx() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -465,6 +466,13 @@ int32_t itn_inject_fault(itn_ctx* c, int32_t kind, int64_t value) {
       c->wait_ns = value > 0 ? (uint64_t)value : kDefaultWaitNs;
       if (c->tc) tc_set_wait_limit(c->tc, c->wait_ns);
       // the limit is a kernel argument baked into the cached solve graphs
+      for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+      c->graphs.clear();
+      c->graph_launches.clear();
+      return ITN_OK;
+    case ITN_FAULT_STALL:
+      c->stall = value != 0;
+      if (c->tc) tc_set_stall(c->tc, c->stall);
       for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
       c->graphs.clear();
       c->graph_launches.clear();
@@ -1178,6 +1186,7 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
     if (!c->tc) {
       c->tc = tc_create();
       tc_set_wait_limit(c->tc, c->wait_ns);
+      tc_set_stall(c->tc, c->stall);
     }
     const char* why = nullptr;
     cudaError_t e = tc_prepare(c->tc, c->layers, c->nv, c->off.data(), c->bond.data(), c->phys.data(),

@@ -44,6 +44,9 @@ const int* tc_err_ptr(const TcEngine* e);
 // recorded after the call.
 constexpr uint64_t kDefaultWaitNs = 2000000000ull;
 void tc_set_wait_limit(TcEngine* e, uint64_t ns);
+// Fault injection: in persistent launches recorded after the call, one wait (the first group's
+// item in the second sweep) looks for a tag that no producer writes, so it runs out.
+void tc_set_stall(TcEngine* e, int on);
 // Account for up to `n` persistent launches about to be enqueued (a solve graph holds at
 // most two); clears the tagged buffers and restarts the epoch on the stream before the
 // 20-bit epoch could wrap onto a stale entry.

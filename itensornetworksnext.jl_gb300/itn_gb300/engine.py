@@ -188,9 +188,10 @@ class BPEngine:
 
     def inject_fault(self, kind: str, value: int):
         """Test hook (itn_inject_fault): ``"wait_ns"`` sets the elapsed-time limit of the
-        tensor-core sweep's waits on other items' messages (<= 0: the default); ``"alloc"``
+        tensor-core sweep's waits on other items' messages (<= 0: the default); ``"stall"``
+        (1 / 0) makes one such wait look for a message that is never written; ``"alloc"``
         makes the next ``value`` device allocations on this thread fail."""
-        k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC}[kind]
+        k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC, "stall": L.FAULT_STALL}[kind]
         self._check(self.lib.itn_inject_fault(self._ctx, k, int(value)))
 
     def tc_selftest(self) -> dict:

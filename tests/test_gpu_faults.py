@@ -1,9 +1,9 @@
 """Failure detection without faulting the GPU.
 
-* A tensor-core sweep whose waits on other items' messages may last at most 1 ns gives up
-  on the first message that is not there yet: the kernel stops early, waits for its own
-  copies and products, frees its tensor memory and the call returns ITN_ERR_TIMEOUT.  The
-  same context then solves the network again with the default limit and matches a fresh
+* A persistent tensor-core sweep in which one wait looks for a message that nothing writes
+  (the stall fault), with the wait limit cut to 1 ms, gives up: every group stops early,
+  waits for its own copies, frees its tensor memory and the call returns ITN_ERR_TIMEOUT.
+  The same context then solves the network again without the fault and matches a fresh
   solve bit for bit (the GPU and the context stayed usable).
 * A device allocation failure forced on the host makes the call that allocates return
   ITN_ERR_OOM; the context recovers once allocations succeed again.
@@ -38,13 +38,15 @@ def test_tensor_core_wait_that_runs_out_reports_timeout():
         want = ref.messages()
     with BPEngine(g) as e:
         e.set_tensors(t)
-        e.inject_fault("wait_ns", 1)
+        e.inject_fault("wait_ns", 1_000_000)
+        e.inject_fault("stall", 1)
         e.init_messages()
         with pytest.raises(ItnError) as ei:
             e.run(maxiter=12, precision="bf16", split_sweeps=2)
         assert ei.value.status == L.ITN_ERR_TIMEOUT
         assert "bounded wait" in str(ei.value)
-        # back to the default limit: the same context solves the network again
+        # no fault, default limit: the same context solves the network again
+        e.inject_fault("stall", 0)
         e.inject_fault("wait_ns", 0)
         e.init_messages()
         r = e.run(maxiter=12, precision="bf16", split_sweeps=2)
