@@ -1334,6 +1334,274 @@ cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg
   ITN_DISPATCH(dtype, return launch_generic_t<T>(a, cfg, st));
 }
 
+// ---- FP32 sweep of a d = 2 lattice with four legs of dimension 8 per vertex -----------------
+// The plain FP32 message update (beliefpropagation.jl:242-257) on CUDA cores with the
+// register blocking of vertex_scalar_d8_kernel.  One CTA of 128 threads per half-vertex item
+// (vertex u, half h): the two "front" legs f0, f1 (0, 1 for h = 0; 2, 3 for h = 1) are
+// absorbed first and the two "back" legs g0, g1 receive the outgoing messages.  With
+// M_s[f][g] = A_s[p][q] (h = 0, f = p = (k0,k1), g = q = (k2,k3)) or A_s[q][p] (h = 1):
+//   pass 1, thread (s, g):  T_s[bf][g] = sum_{f0,f1} m_f0[bf0][f0] m_f1[bf1][f1] M_s[(f0,f1)][g]
+//           as X = m_f0 * M_s[:, g] (8x8x8) then T = X * m_f1^T (8x8x8);
+//   pass 2, thread (s, bf): out_g0[bg0][kg0] += sum_bg1 M_s[bf][(bg0,bg1)] sum_kg1 T_s[bf][(kg0,kg1)] m_g1[bg1][kg1]
+//                           out_g1[bg1][kg1] += sum_bg0 M_s[bf][(bg0,bg1)] sum_kg0 m_g0[bg0][kg0] T_s[bf][(kg0,kg1)]
+//           each as two 8x8x8 products in registers, then summed over the 128 threads by a
+//           butterfly reduce-scatter (64 values -> 2 per lane) and the 4 warps' shares.
+// 786,432 multiply-adds per vertex (the leave-one-out minimum; the algorithmic count of the
+// four updates is 1,048,576).  The site tensor is staged with rows of kD8Ld floats so that
+// row (LDS.128) and column (LDS.32) reads are both free of bank conflicts.
+constexpr int kD8Ld = 68;
+constexpr size_t kD8SmemFloats = 2 * 128 * kD8Ld + 256 + 2 * 4 * 64 + 8;
+
+// Sum of v[0..63] over the warp, scattered: lane l returns entries 2l and 2l + 1.
+__device__ __forceinline__ float2 warp_reduce_scatter64(float (&v)[64]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16, n = 32; o >= 1; o >>= 1, n >>= 1) {
+    const bool hi = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      const float keep = hi ? v[i + n] : v[i];
+      const float send = hi ? v[i] : v[i + n];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return make_float2(v[0], v[1]);
+}
+
+struct SweepD8Args {
+  const int* rev;
+  const float* tens;
+  const float* msg_in;
+  float* msg_out;
+  int nv;
+  int normalize;
+  double* slot_diff;
+  ConvState* conv;
+};
+
+// 8 consecutive floats of shared memory (16-byte aligned) / 8 floats `stride` apart
+__device__ __forceinline__ void lds8(const float* p, float (&x)[8]) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  const float4 b = *reinterpret_cast<const float4*>(p + 4);
+  x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+  x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+}
+__device__ __forceinline__ void lds8s(const float* p, int stride, float (&x)[8]) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = p[i * stride];
+}
+
+// Row i (8 entries over the second index pair member) of the 8x8 block of M_s:
+// M_s[(i, j)][c] for j = 0..7 (COLUMN: the thread's column c) or M_s[c][(i, j)] (ROW).
+// H = 0: M_s = A_s (row stride kD8Ld); H = 1: M_s = A_s^T.
+template <int H, bool COLUMN>
+__device__ __forceinline__ void m_block_row(const float* Ms, int c, int i, float (&x)[8]) {
+  // M_s[f][g] sits at f * mrow + g * mcol
+  constexpr int mrow = H ? 1 : kD8Ld, mcol = H ? kD8Ld : 1;
+  if constexpr (COLUMN) {
+    // M_s[(i, j)][c]: j steps by mrow
+    if constexpr (mrow == 1) lds8(Ms + i * 8 + c * mcol, x);
+    else lds8s(Ms + i * 8 * mrow + c * mcol, mrow, x);
+  } else {
+    // M_s[c][(i, j)]: j steps by mcol
+    if constexpr (mcol == 1) lds8(Ms + c * mrow + i * 8, x);
+    else lds8s(Ms + c * mrow + i * 8 * mcol, mcol, x);
+  }
+}
+
+template <int H>
+__device__ __forceinline__ void sweep_d8_item(const SweepD8Args& a, int u, const float* As, float* Ts,
+                                              const float* mt, float* red) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  constexpr int f0 = H ? 2 : 0, f1 = f0 + 1, g0 = H ? 0 : 2, g1 = g0 + 1;
+  const int s = t >> 6, c = t & 63;
+  const float* Ms = As + 64 * s * kD8Ld;
+  // ---- pass 1: thread (s, g = c) ----
+  {
+    float X[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) X[i] = 0.f;
+#pragma unroll
+    for (int k0 = 0; k0 < 8; ++k0) {
+      float col[8];
+      m_block_row<H, true>(Ms, c, k0, col);
+#pragma unroll
+      for (int b0 = 0; b0 < 8; ++b0) {
+        const float w = mt[64 * f0 + 8 * b0 + k0];
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) X[b0 * 8 + k1] = fmaf(w, col[k1], X[b0 * 8 + k1]);
+      }
+    }
+    float* Tc = Ts + 64 * s * kD8Ld + c;
+#pragma unroll
+    for (int b1 = 0; b1 < 8; ++b1) {
+      float mr[8];
+      lds8(mt + 64 * f1 + 8 * b1, mr);
+#pragma unroll
+      for (int b0 = 0; b0 < 8; ++b0) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) acc = fmaf(X[b0 * 8 + k1], mr[k1], acc);
+        Tc[(b0 * 8 + b1) * kD8Ld] = acc;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- pass 2: thread (s, bf = c); the bra row is M_s[c][.] ----
+  const float* Tr = Ts + (64 * s + c) * kD8Ld;
+  {
+    // out on leg g0: P[bg0][kg0] = sum_bg1 M[c][(bg0,bg1)] V[kg0][bg1],  V = T m_g1^T
+    float V[64];
+    {
+      float T[64];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float x[8];
+        lds8(Tr + 8 * i, x);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) T[8 * i + j] = x[j];
+      }
+#pragma unroll
+      for (int b1 = 0; b1 < 8; ++b1) {
+        float mr[8];
+        lds8(mt + 64 * g1 + 8 * b1, mr);
+#pragma unroll
+        for (int k0 = 0; k0 < 8; ++k0) {
+          float acc = 0.f;
+#pragma unroll
+          for (int k1 = 0; k1 < 8; ++k1) acc = fmaf(T[k0 * 8 + k1], mr[k1], acc);
+          V[k0 * 8 + b1] = acc;
+        }
+      }
+    }
+    float P[64];
+#pragma unroll
+    for (int b0 = 0; b0 < 8; ++b0) {
+      float mb[8];
+      m_block_row<H, false>(Ms, c, b0, mb);
+#pragma unroll
+      for (int k0 = 0; k0 < 8; ++k0) {
+        float acc = 0.f;
+#pragma unroll
+        for (int b1 = 0; b1 < 8; ++b1) acc = fmaf(mb[b1], V[k0 * 8 + b1], acc);
+        P[b0 * 8 + k0] = acc;
+      }
+    }
+    const float2 r = warp_reduce_scatter64(P);
+    *reinterpret_cast<float2*>(red + warp * 64 + 2 * lane) = r;
+  }
+  {
+    // out on leg g1: P[bg1][kg1] = sum_bg0 M[c][(bg0,bg1)] U[bg0][kg1],  U = m_g0 T
+    float T[64];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float x[8];
+      lds8(Tr + 8 * i, x);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) T[8 * i + j] = x[j];
+    }
+    float P[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) P[i] = 0.f;
+#pragma unroll
+    for (int b0 = 0; b0 < 8; ++b0) {
+      float mr[8];
+      lds8(mt + 64 * g0 + 8 * b0, mr);
+      float U[8];
+#pragma unroll
+      for (int k1 = 0; k1 < 8; ++k1) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k0 = 0; k0 < 8; ++k0) acc = fmaf(mr[k0], T[k0 * 8 + k1], acc);
+        U[k1] = acc;
+      }
+      float mb[8];
+      m_block_row<H, false>(Ms, c, b0, mb);
+#pragma unroll
+      for (int b1 = 0; b1 < 8; ++b1)
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) P[b1 * 8 + k1] = fmaf(mb[b1], U[k1], P[b1 * 8 + k1]);
+    }
+    const float2 r = warp_reduce_scatter64(P);
+    *reinterpret_cast<float2*>(red + 256 + warp * 64 + 2 * lane) = r;
+  }
+}
+
+__global__ void __launch_bounds__(128, 3) sweep_d8_kernel(SweepD8Args a) {
+  extern __shared__ __align__(16) float sd8[];
+  float* As = sd8;                   // A_s[p][q] at (64 s + p) * kD8Ld + q
+  float* Ts = As + 128 * kD8Ld;      // T_s[bf][g] at (64 s + bf) * kD8Ld + g
+  float* mt = Ts + 128 * kD8Ld;      // incoming messages m_l[b][k] at 64 l + 8 b + k
+  float* red = mt + 256;             // [2 outputs][4 warps][64]
+  float* sums = red + 2 * 4 * 64;    // [2 outputs][2 warps]
+  if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
+  const int u = blockIdx.x >> 1, h = blockIdx.x & 1;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  {
+    // the site tensor (8192 floats, 32 KB aligned) into padded rows; the 4 incoming messages
+    const float4* src = reinterpret_cast<const float4*>(a.tens + (size_t)u * 8192);
+    float4 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __ldg(src + t + 128 * i);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int j = t + 128 * i;
+      *reinterpret_cast<float4*>(As + (j >> 4) * kD8Ld + (j & 15) * 4) = v[i];
+    }
+    mt[t] = __ldg(a.msg_in + 64 * a.rev[4 * u + (t >> 6)] + (t & 63));
+    mt[t + 128] = __ldg(a.msg_in + 64 * a.rev[4 * u + 2 + (t >> 6)] + (t & 63));
+  }
+  __syncthreads();
+  if (h) sweep_d8_item<1>(a, u, As, Ts, mt, red);
+  else sweep_d8_item<0>(a, u, As, Ts, mt, red);
+  __syncthreads();
+  // ---- finish: threads 0..63 the message on leg g0, 64..127 the one on leg g1 ----
+  const int g0 = h ? 0 : 2;
+  const int o = t >> 6, e = t & 63;
+  const float* ro = red + 256 * o;
+  const float val = (ro[e] + ro[64 + e]) + (ro[128 + e] + ro[192 + e]);
+  float sum = val;
+#pragma unroll
+  for (int k = 16; k >= 1; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
+  if (lane == 0) sums[2 * o + (warp & 1)] = sum;
+  __syncthreads();
+  sum = sums[2 * o] + sums[2 * o + 1];
+  const bool scale = a.normalize && sum != 0.f;
+  const float v = scale ? val / sum : val;
+  const int slot = 4 * u + g0 + o;
+  a.msg_out[64 * slot + e] = v;
+  if (a.slot_diff) {
+    const double ov = a.msg_in[64 * slot + e];
+    double n1 = (double)v * v, n2 = ov * ov, dd = (double)v * ov;
+#pragma unroll
+    for (int k = 16; k >= 1; k >>= 1) {
+      n1 += __shfl_xor_sync(0xffffffffu, n1, k);
+      n2 += __shfl_xor_sync(0xffffffffu, n2, k);
+      dd += __shfl_xor_sync(0xffffffffu, dd, k);
+    }
+    double* ds = reinterpret_cast<double*>(red);  // red is free once every thread has read it
+    __syncthreads();
+    if (lane == 0) {
+      ds[3 * (2 * o + (warp & 1))] = n1;
+      ds[3 * (2 * o + (warp & 1)) + 1] = n2;
+      ds[3 * (2 * o + (warp & 1)) + 2] = dd;
+    }
+    __syncthreads();
+    if (e == 0) {
+      const double* p0 = ds + 6 * o;
+      const double N1 = p0[0] + p0[3], N2 = p0[1] + p0[4], DD = p0[2] + p0[5];
+      const double val2 = 1.0 - DD * DD / (N1 * N2);
+      a.slot_diff[slot] = val2;
+      if (a.conv) {
+        if (val2 != val2) atomicExch(&a.conv->nan_flag, 1);
+        else atomicMax(&a.conv->dmax, enc_double(val2));
+        __threadfence();
+      }
+    }
+  }
+  if (a.conv) conv_finish_cta(a.conv);
+}
+
 template <typename T>
 cudaError_t launch_vertex_scalars_d8_t(int nv, const int* rev, const long long* moff, const long long* toff,
                                        const void* tens, const void* msgs, void* zv, cudaStream_t st) {
@@ -1355,6 +1623,22 @@ cudaError_t launch_vertex_scalars_d8(int dtype, int nv, const int* rev, const lo
     case DT_C64: return launch_vertex_scalars_d8_t<c64>(nv, rev, moff, toff, tens, msgs, zv, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_sweep_d8(const int* rev, const float* tens, const float* msg_in, float* msg_out, int nv,
+                            int normalize, double* slot_diff, ConvState* conv, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  const size_t smem = kD8SmemFloats * sizeof(float);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(sweep_d8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(sweep_d8_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    configured = true;
+  }
+  SweepD8Args a{rev, tens, msg_in, msg_out, nv, normalize, slot_diff, conv};
+  sweep_d8_kernel<<<2 * nv, 128, smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,

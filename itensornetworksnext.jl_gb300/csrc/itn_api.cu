@@ -1015,6 +1015,10 @@ int autotune_sweep(itn_ctx* c) {
   return ITN_OK;
 }
 
+// FP32 parallel sweeps of a network whose vertices all have d = 2 and four legs of dimension
+// 8 run on the register-blocked kernel (sweep_d8_kernel) instead of the interpreter.
+bool use_sweep_d8(const itn_ctx* c) { return c->scal_d8 && c->dtype == ITN_F32; }
+
 int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   const bool use_tol = o->tol >= 0;
   const size_t nc = c->par_classes.size();
@@ -1091,6 +1095,10 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       tr.conv = conv(c);
       cudaError_t e = tc_sweep(c->tc, tr, c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
+    } else if (use_sweep_d8(c)) {
+      CK(launch_sweep_d8(c->d_rev.as<int>(), c->d_tens.as<float>(), c->d_msg[in].as<float>(),
+                         c->d_msg[out].as<float>(), (int)c->nv, o->normalize,
+                         use_tol ? c->d_slot_diff.as<double>() : nullptr, conv(c), c->stream));
     } else {
       for (size_t k = 0; k < p.a.size(); ++k) {
         CK(launch_generic(c->dtype, p.a[k][in], p.cfg[k][in], c->stream));
@@ -1224,7 +1232,7 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   const bool use_tol = o->tol >= 0;
   ParPlan pplan;
   std::vector<SeqLaunch> slaunch;
-  if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE) {
+  if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE && !use_sweep_d8(c)) {
     if (int r = autotune_sweep(c)) return r;
     if (int r = make_par_plan(c, o, pplan)) return r;
   } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {

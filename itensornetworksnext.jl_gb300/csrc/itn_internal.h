@@ -103,6 +103,12 @@ cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, co
 cudaError_t launch_vertex_scalars_d8(int dtype, int nv, const int* rev, const long long* moff,
                                      const long long* toff, const void* tens, const void* msgs, void* zv,
                                      cudaStream_t st);
+// One FP32 parallel sweep of a two-layer network whose vertices all have d = 2 and four legs
+// of dimension 8 (vertex u's legs are slots 4u..4u+3, its tensor 8192 entries at 8192 u,
+// slot s's message 64 entries at 64 s), CUDA cores; slot_diff / conv as in GenericArgs
+// (the sweep also steps the outer loop when conv is given).
+cudaError_t launch_sweep_d8(const int* rev, const float* tens, const float* msg_in, float* msg_out, int nv,
+                            int normalize, double* slot_diff, ConvState* conv, cudaStream_t st);
 cudaError_t launch_logsum(int dtype, const void* zv, const void* ze, int nv, int ne,
                           const int* net_voff, const int* net_vlist, const int* net_eoff,
                           const int* net_elist, int n_nets, double* logzv, double* logze,
