@@ -39,6 +39,8 @@ SWEEPS = 30
 SPLIT_SWEEPS = 3
 SEED = 32
 METRIC = "BP message updates/s (32x32, D=8) mixed vs plain FP32; grad time @1e-6 err"
+# FP32 FMA rate of a GB300 at its maximum clock: 152 SMs x 128 lanes x 2 flops x 2.07 GHz
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 UNIT = "message updates/s"
 
 
@@ -406,7 +408,11 @@ def run_gpu(args):
                    "updates_per_step": upd_per_step,
                    "l2": "flushed between steps (256 MB write); the 33.5 MB of FP32 site tensors stay L2-resident within a step"},
         "fp32_plain": {"value": fp32_value, "ms_per_step": ms_fp32,
-                       "speedup_of_value": value / fp32_value},
+                       "speedup_of_value": value / fp32_value,
+                       "kernel": "sweep_d8_kernel (FP32 CUDA cores, register-blocked, one CTA per half vertex)",
+                       "achieved_tflops_alg": fps / (ms_fp32 / SWEEPS * 1e-3) / 1e12,
+                       "fp32_peak_tflops": FP32_PEAK_TFLOPS,
+                       "frac_of_fp32_peak": fps / (ms_fp32 / SWEEPS * 1e-3) / 1e12 / FP32_PEAK_TFLOPS},
         "logz_rel_err_vs_fp64": err,
         "logzv_max_abs_err_vs_fp64": site_err,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

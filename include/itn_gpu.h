@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define ITN_ABI_VERSION 1
+#define ITN_ABI_VERSION 2
 
 enum {
   ITN_OK = 0,
@@ -231,19 +231,30 @@ int32_t itn_apply_gates(itn_ctx *ctx, int32_t dtype, int64_t n_gates, const itn_
                         int32_t *out_bond, double *device_ms);
 
 /* Gradient of the Bethe log-norm (bethe_free_energy, messagecache.jl:185-201) with
- * respect to every site tensor, for the converged messages currently held.  No
- * counterpart in the reference (it has no AD); this is the backward rule the Julia
- * shim's ChainRulesCore.rrule(bethe_free_energy ∘ beliefpropagation) calls.
- * The direct term dlogZ_u/dA_u is always computed; with adjoint != 0 the implicit
- * (adjoint BP) correction lambda^T dF/dA is added, lambda solving
- * lambda = dL/dm + J^T lambda by fixed-point iteration until the relative change is
- * below tol (ITN_ERR_TIMEOUT after maxiter).  normalized: the messages come from
- * SimpleMessageUpdate(normalize = true).  Real dtypes, norm networks (layers = 2). */
+ * respect to every site tensor.  No counterpart in the reference (it has no AD); this is
+ * the backward rule the Julia shim's ChainRulesCore.rrule(bp_logz) calls.
+ * sweeps == 0 (implicit mode), for the converged messages currently held: the direct term
+ * dlogZ_u/dA_u is always computed; with adjoint != 0 the implicit (adjoint BP) correction
+ * lambda^T dF/dA is added, lambda solving lambda = dL/dm + J^T lambda by fixed-point
+ * iteration until the relative change is below tol (ITN_ERR_TIMEOUT after maxiter).
+ * sweeps > 0 (unrolled mode): runs `sweeps` parallel sweeps (beliefpropagation.jl:155-210)
+ * from the current messages, leaves their result as the current messages, and returns the
+ * exact gradient of the log-norm of that result, differentiating through every sweep in
+ * reverse: lambda_T = dL/dm_T, lambda_{t-1} = J(m_{t-1})^T lambda_t, gradient = direct term
+ * + sum_t lambda_t^T dF/dA(m_{t-1}).  The messages of every `checkpoint`-th sweep are kept
+ * (checkpoint <= 1: every sweep) and the others recomputed from the nearest kept sweep in
+ * the backward pass: device memory for about sweeps / checkpoint + checkpoint message sets
+ * instead of sweeps, at the cost of one more forward pass; the result does not depend on
+ * checkpoint (the recomputed sweeps are bit-identical).  adjoint, maxiter and tol are not
+ * used in this mode.  normalized: the sweeps are SimpleMessageUpdate(normalize = true).
+ * Real dtypes, norm networks (layers = 2). */
 typedef struct {
   int32_t adjoint;
   int32_t maxiter;
   double tol;
   int32_t normalized;
+  int32_t sweeps;      /* > 0: unrolled mode over this many sweeps */
+  int32_t checkpoint;  /* unrolled mode: keep the messages of every checkpoint-th sweep */
   int32_t reserved0;
 } itn_grad_opts;
 

@@ -52,6 +52,9 @@ thread_local int64_t t_fail_allocs = 0;
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;  // owns p: never copied
+  DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() {
     if (p) cudaFree(p);
   }
@@ -197,6 +200,7 @@ struct itn_ctx {
   DevBuf d_slot_dst, d_slot_eidx;
   // gradient work buffers
   DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_cot, d_adj;
+  DevBuf d_ckpt, d_seg;  // unrolled gradient: kept sweep states, recomputed segment
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
   // data
@@ -1519,6 +1523,140 @@ int apply_jt(itn_ctx* c, const void* m, const void* lam, void* cot, int normaliz
   return ITN_OK;
 }
 
+// One parallel sweep in -> out of the native CUDA-core kernel over every vertex (the
+// forward map of the unrolled gradient; no convergence bookkeeping).
+int sweep_native(itn_ctx* c, const void* in, void* out, int normalized) {
+  GenericArgs a;
+  LaunchCfg cfg;
+  if (int r = plan_generic(c, a, cfg, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, in, out)) return r;
+  a.normalize = normalized;
+  CK(launch_generic(c->dtype, a, cfg, c->stream));
+  return ITN_OK;
+}
+
+// grad += lambda^T dF/dA at messages m (the tangent plane of the all-legs contraction with
+// mu = the projection of lambda through the normalisation); needs adjoint_prepare(m).
+int add_lambda_dfda(itn_ctx* c, const void* m, const void* lam, int normalized) {
+  const int ns = (int)c->nslots, nd = (int)c->items_dump.size() / 2;
+  CK(launch_grad_mu(c->dtype, c->d_moff.as<long long>(), ns, lam, c->d_F.p, c->d_S.p, c->d_mu.p, normalized,
+                    nullptr, c->stream));
+  GenericArgs a;
+  LaunchCfg cfg;
+  if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
+  DualArgs d;
+  memset(&d, 0, sizeof(d));
+  d.grad_out = c->d_grad.p;
+  d.zv = c->d_zv.p;
+  d.tan_in = c->d_mu.p;
+  d.dump_tangent = 1;
+  for (int tr = 0; tr < 2; ++tr) {
+    d.transpose = tr;
+    CK(launch_dual(c->dtype, a, d, cfg, c->stream));
+  }
+  return ITN_OK;
+}
+
+// The direct term dlogZ_u/dA_u = (T_u(m) + T_u(m^T)) / Z_u into d_grad (zeroed first);
+// computes the scalars of m.
+int grad_direct(itn_ctx* c, const void* m) {
+  const size_t tb = (size_t)c->toff[c->nv] * dtype_size(c->dtype);
+  if (int r = compute_scalars(c, m)) return r;
+  CK(c->d_grad.ensure(std::max<size_t>(tb, 16)));
+  CK(cudaMemsetAsync(c->d_grad.p, 0, tb, c->stream));
+  const int nd = (int)c->items_dump.size() / 2;
+  GenericArgs a;
+  LaunchCfg cfg;
+  if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
+  DualArgs d;
+  memset(&d, 0, sizeof(d));
+  d.grad_out = c->d_grad.p;
+  d.zv = c->d_zv.p;
+  for (int tr = 0; tr < 2; ++tr) {
+    d.transpose = tr;
+    CK(launch_dual(c->dtype, a, d, cfg, c->stream));
+  }
+  return ITN_OK;
+}
+
+// Unrolled gradient (itn_grad_opts.sweeps > 0): T = sweeps parallel sweeps m_t = F(m_{t-1})
+// from the current messages, then the reverse pass
+//   lambda_T = dL/dm_T,  grad = dL/dA|m_T + sum_{t=T..1} lambda_t^T dF/dA(m_{t-1}),
+//   lambda_{t-1} = J(m_{t-1})^T lambda_t.
+// Sweep states m_s with s % k == 0 (k = checkpoint) are kept; the others of a segment
+// [c0 + 1, c0 + k - 1] are recomputed from m_{c0} when the reverse pass enters it.
+int grad_unrolled(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_result* res) {
+  const int T = o->sweeps, k = std::max(1, o->checkpoint);
+  const size_t es = dtype_size(c->dtype);
+  const size_t tb = (size_t)c->toff[c->nv] * es, mb = (size_t)c->moff[c->nslots] * es;
+  const size_t mbs = std::max<size_t>((mb + 255) & ~(size_t)255, 256);
+  const int ns = (int)c->nslots;
+  const int nck = (T - 1) / k + 1;  // kept states m_0, m_k, ... (indices < T)
+  CK(c->d_ckpt.ensure((size_t)nck * mbs));
+  CK(c->d_seg.ensure((size_t)(k + 1) * mbs));  // a segment's k - 1 states + two forward buffers
+  unsigned char* ck = static_cast<unsigned char*>(c->d_ckpt.p);
+  unsigned char* seg = static_cast<unsigned char*>(c->d_seg.p);
+  auto ckpt = [&](int s) { return (void*)(ck + (size_t)(s / k) * mbs); };
+  auto segp = [&](int j) { return (void*)(seg + (size_t)j * mbs); };  // m_{c0 + 1 + j}
+  void* fwd[2] = {segp(k - 1), segp(k)};  // forward scratch (past the segment slots)
+  void* cur_msg = c->d_msg[c->cur].p;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  // forward
+  if (mb) CK(cudaMemcpyAsync(ckpt(0), cur_msg, mb, cudaMemcpyDeviceToDevice, c->stream));
+  const void* prev = ckpt(0);
+  for (int t = 1; t <= T; ++t) {
+    void* out = (t < T && t % k == 0) ? ckpt(t) : fwd[t & 1];
+    if (t == T) out = cur_msg;  // the context ends holding m_T
+    if (int r = sweep_native(c, prev, out, o->normalized)) return r;
+    prev = out;
+  }
+  // direct term and lambda_T at m_T
+  if (int r = grad_direct(c, cur_msg)) return r;
+  CK(c->d_g.ensure(std::max<size_t>(mb, 16)));
+  CK(c->d_lam.ensure(std::max<size_t>(mb, 16)));
+  if (int r = adjoint_prepare(c, cur_msg, o->normalized)) return r;
+  CK(launch_grad_g(c->dtype, c->d_moff.as<long long>(), c->d_rev.as<int>(), c->d_slot_dst.as<int>(),
+                   c->d_slot_eidx.as<int>(), ns, c->d_U.p, cur_msg, c->d_zv.p, c->d_ze.p, c->d_lam.p, c->stream));
+  // reverse pass
+  int seg_base = -1;  // segment currently recomputed: states m_{seg_base + 1 ..}
+  for (int t = T; t >= 1; --t) {
+    const int s = t - 1;
+    const void* ms;
+    if (s % k == 0) {
+      ms = ckpt(s);
+    } else {
+      const int c0 = s - s % k;
+      if (seg_base != c0) {
+        const void* p = ckpt(c0);
+        for (int j = 0; j + 1 < k && c0 + 1 + j < T; ++j) {
+          if (int r = sweep_native(c, p, segp(j), o->normalized)) return r;
+          p = segp(j);
+        }
+        seg_base = c0;
+      }
+      ms = segp(s - c0 - 1);
+    }
+    if (int r = adjoint_prepare(c, ms, o->normalized)) return r;
+    if (int r = add_lambda_dfda(c, ms, c->d_lam.p, o->normalized)) return r;
+    if (t > 1) {
+      if (int r = apply_jt(c, ms, c->d_lam.p, c->d_cot.p, o->normalized)) return r;
+      // lambda_{t-1} is in d_cot: exchange the two buffers (pointers, not contents)
+      std::swap(c->d_lam.p, c->d_cot.p);
+      std::swap(c->d_lam.bytes, c->d_cot.bytes);
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  if (tb) CK(cudaMemcpyAsync(grad, c->d_grad.p, tb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (res) {
+    res->adjoint_iterations = T;
+    res->adjoint_residual = 0.0;
+    res->device_ms = ms;
+  }
+  return ITN_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1549,8 +1687,10 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     return fail(c, ITN_ERR_UNSUPPORTED, "the gradient is implemented for real site tensors");
   if (c->layers != 2) return fail(c, ITN_ERR_UNSUPPORTED, "the gradient is implemented for norm networks");
   if (int r = ensure_device(c)) return r;
-  itn_grad_opts def = {1, 200, 1e-10, 1, 0};
+  itn_grad_opts def = {1, 200, 1e-10, 1, 0, 1, 0};
   if (!o) o = &def;
+  if (o->sweeps < 0) return fail(c, ITN_ERR_ARG, "sweeps < 0");
+  if (o->sweeps > 0) return grad_unrolled(c, o, grad, res);
   const int dt = c->dtype;
   const size_t es = dtype_size(dt);
   const size_t tb = (size_t)c->toff[c->nv] * es, mb = (size_t)c->moff[c->nslots] * es;

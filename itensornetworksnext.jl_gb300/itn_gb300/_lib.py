@@ -66,7 +66,8 @@ class BpOpts(ctypes.Structure):
 
 class GradOpts(ctypes.Structure):
     _fields_ = [("adjoint", ctypes.c_int32), ("maxiter", ctypes.c_int32), ("tol", ctypes.c_double),
-                ("normalized", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
+                ("normalized", ctypes.c_int32), ("sweeps", ctypes.c_int32), ("checkpoint", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32)]
 
 
 class GradResult(ctypes.Structure):

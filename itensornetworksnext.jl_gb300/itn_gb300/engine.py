@@ -169,10 +169,14 @@ class BPEngine:
                                               ctypes.byref(out)))
         return out.value
 
-    def grad(self, *, adjoint=True, maxiter=200, tol=1e-10, normalized=True):
-        """Gradient of bethe_free_energy w.r.t. every site tensor at the current
-        (converged) messages; returns (packed gradient, info dict)."""
-        o = L.GradOpts(int(bool(adjoint)), int(maxiter), float(tol), int(bool(normalized)), 0)
+    def grad(self, *, adjoint=True, maxiter=200, tol=1e-10, normalized=True, sweeps=0, checkpoint=1):
+        """Gradient of bethe_free_energy w.r.t. every site tensor; returns (packed gradient,
+        info dict).  sweeps == 0: at the current (converged) messages, with the implicit
+        adjoint correction when ``adjoint``.  sweeps > 0: runs that many parallel sweeps
+        from the current messages and differentiates through them exactly, keeping every
+        ``checkpoint``-th sweep's messages (the others are recomputed)."""
+        o = L.GradOpts(int(bool(adjoint)), int(maxiter), float(tol), int(bool(normalized)), int(sweeps),
+                       int(checkpoint), 0)
         r = L.GradResult()
         out = np.empty(int(self.graph.toff[-1]), dtype=self.dtype)
         self._check(self.lib.itn_bp_grad(self._ctx, ctypes.byref(o), L.ptr(out), ctypes.byref(r)))

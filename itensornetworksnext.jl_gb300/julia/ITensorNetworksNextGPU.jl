@@ -1,25 +1,39 @@
 # ITensorNetworksNextGPU.jl -- Julia side of the drop-in: GPU strategies for
 # ITensorNetworksNext.jl that call libitn_gpu.so through `ccall`.
 #
-# Plug-in points used (paths inside ITensorNetworksNext.jl):
-#   * MessageUpdateAlgorithm + message_update!(alg, cache, factors, edge)
-#       src/beliefpropagation/beliefpropagation.jl:214-235 (strategy interface)
-#   * AI.solve specialised on BeliefPropagationAlgorithm whose sweep uses GPUMessageUpdate,
-#     so `beliefpropagation(factors, messages; ...)` (beliefpropagation.jl:69-92) keeps its
-#     signature and returns a MessageCache
-#   * bethe_free_energy(factors, messages) (src/beliefpropagation/messagecache.jl:185-201)
-#   * ChainRulesCore.rrule for the converged BP log-norm (no reference counterpart)
+# Plug-in points of the reference used here (paths inside ITensorNetworksNext.jl):
+#   * `GPUMessageUpdate <: MessageUpdateAlgorithm` with a `message_update!(alg, cache,
+#     factors, edge)` method (src/beliefpropagation/beliefpropagation.jl:214-235): the
+#     per-edge strategy, one device update per call (itn_message_update).
+#   * `AI.solve` specialised on `BeliefPropagationAlgorithm` whose sweep algorithm carries a
+#     `GPUMessageUpdate` (beliefpropagation.jl:96-210): `beliefpropagation(factors, messages;
+#     edges, stopping_criterion, message_update_algorithm = GPUMessageUpdate())`
+#     (beliefpropagation.jl:69-92) keeps its signature, goes down in one call (itn_bp_run)
+#     and returns a `MessageCache`.
+#   * `GPUExact` with `contract_network(::GPUExact, tn)` (src/contract_network.jl:12-17, the
+#     method table the unknown-algorithm fallback guards): exact contraction by pairwise GPU
+#     contractions (itn_contract_network).
+#   * `bethe_free_energy(factors, ::DeviceMessageCache)` (src/beliefpropagation/
+#     messagecache.jl:185): the log-norm of messages that stayed on the device after the
+#     solve (itn_logscalars, FP64 log-scalars, no re-upload).
+#   * `ChainRulesCore.rrule(::typeof(bp_logz), nn, messages)`: the converged BP log-norm and
+#     its gradient (no reference counterpart: the reference has no AD); the tangent of the
+#     NormNetwork is a structural tangent of its ket tensors, each in its own index order.
 #
-# Not exercised in this repository: no Julia toolchain is available where it was built.
+# Not exercised here: no Julia toolchain exists where this repository is built and tested.
+# tests/c/julia_shim_replay.c replays every ccall below (argument lists, struct layouts,
+# packing and index orders) against the library from C.
 module ITensorNetworksNextGPU
 
 using ITensorNetworksNext: ITensorNetworksNext, MessageUpdateAlgorithm, MessageCache,
-    NormNetwork, messagecache, linknames, sitenames, kettensor, braname
+    NormNetwork, linknames, sitenames, kettensor, conj_bratensor, braname
 using ITensorNetworksNext.AlgorithmsInterfaceExtensions: StopWhenConverged
 using AlgorithmsInterface: AlgorithmsInterface as AI
-using Graphs: vertices, edges, src, dst, neighbors
-using ITensorBase: dimnames, unnamed
-using ChainRulesCore: ChainRulesCore, NoTangent
+using Graphs: vertices, src, dst, neighbors
+using ITensorBase: dimnames, unnamed, inds, name
+using ChainRulesCore: ChainRulesCore, NoTangent, Tangent
+
+const INN = ITensorNetworksNext
 
 const libitn = get(ENV, "ITN_GPU_LIB",
     joinpath(@__DIR__, "..", "lib", "libitn_gpu.so"))
@@ -39,7 +53,10 @@ eltype_code(::Type{Float32}) = Int32(0)
 eltype_code(::Type{Float64}) = Int32(1)
 eltype_code(::Type{ComplexF32}) = Int32(2)
 eltype_code(::Type{ComplexF64}) = Int32(3)
+eltype_code(::Type{T}) where {T} =
+    throw(ArgumentError("no GPU arithmetic for element type $T (use SimpleMessageUpdate)"))
 
+# C layouts of itn_bp_opts / itn_bp_result / itn_grad_opts / itn_grad_result
 struct ItnBpOpts
     schedule::Int32
     maxiter::Int32
@@ -66,6 +83,8 @@ struct ItnGradOpts
     maxiter::Int32
     tol::Float64
     normalized::Int32
+    sweeps::Int32
+    checkpoint::Int32
     reserved0::Int32
 end
 
@@ -76,30 +95,42 @@ struct ItnGradResult
     device_ms::Float64
 end
 
-# ---- the strategy -----------------------------------------------------------------------
-"""
-    GPUMessageUpdate(; precision = :native, split_sweeps = 0, device = 0, schedule = :parallel)
+precision_code(p::Symbol) = p === :native ? Int32(0) : p === :bf16 ? Int32(1) :
+    p === :tf32 ? Int32(2) : p === :tf32x3 ? Int32(3) : throw(ArgumentError("unknown precision $p"))
 
-Message-update strategy that runs the whole BP solve on the GPU. `precision = :bf16`
-uses the tcgen05 tensor-core sweep (Float32 networks, 4 legs of dimension 8) with
-`split_sweeps` final hi/lo sweeps.
+# ---- the message-update strategy ------------------------------------------------------------
+"""
+    GPUMessageUpdate(; normalize = true, precision = :native, split_sweeps = 0,
+                       schedule = :sequential, device = 0)
+
+`MessageUpdateAlgorithm` whose updates run on the GPU.  Through `beliefpropagation` the whole
+solve is one device call: `schedule = :sequential` follows the `edges` order exactly (the
+reference's Gauss-Seidel sweep), `:parallel` updates every edge from the previous sweep's
+messages (Jacobi; `edges` only fixes the edge set).  `precision = :bf16` / `:tf32` run the
+tcgen05 tensor-core sweep on Float32 networks whose vertices have four legs of dimension 8 and
+a site index of dimension 2, with `split_sweeps` final hi/lo sweeps; `:tf32x3` runs every
+sweep with TF32 hi/lo operands.
 """
 Base.@kwdef struct GPUMessageUpdate <: MessageUpdateAlgorithm
+    normalize::Bool = true
     precision::Symbol = :native
     split_sweeps::Int = 0
+    schedule::Symbol = :sequential
     device::Int = 0
-    schedule::Symbol = :parallel
 end
 
-# A flattened norm network on the device.
+# A flattened norm network on the device: CSR graph (one leg per neighbour), ket tensors
+# uploaded with their own strides (permuted to the canonical [site, legs...] on the device).
 mutable struct DeviceNetwork{V}
     ctx::Ptr{Cvoid}
     verts::Vector{V}
-    slot::Dict{Pair{V, V}, Int}   # directed edge -> CSR slot
+    slot::Dict{Pair{V, V}, Int}          # directed edge -> CSR slot
     off::Vector{Int64}
     bond::Vector{Int32}
     moff::Vector{Int64}
     elt::DataType
+    # per vertex: canonical axis names (site name or nothing, then the link of each leg)
+    canon::Vector{Vector{Any}}
 end
 
 function destroy!(d::DeviceNetwork)
@@ -108,9 +139,6 @@ function destroy!(d::DeviceNetwork)
     return nothing
 end
 
-# Build the CSR description (one leg per neighbour; all shared link names of a pair
-# fuse into that leg, abstracttensornetwork.jl:52-73) and upload the ket tensors with
-# their own strides (permuted to [site, legs...] on the device).
 function DeviceNetwork(nn::NormNetwork; device::Integer = 0)
     ctxr = Ref{Ptr{Cvoid}}(C_NULL)
     st = ccall((:itn_create, libitn), Int32, (Ptr{Ptr{Cvoid}}, Int32, Int32), ctxr, device, 0)
@@ -121,6 +149,7 @@ function DeviceNetwork(nn::NormNetwork; device::Integer = 0)
     off = Int64[0]; nbr = Int64[]; bond = Int32[]; phys = Int32[]
     slot = Dict{Pair{eltype(verts), eltype(verts)}, Int}()
     ptrs = Ptr{Cvoid}[]; strides = Int64[]
+    canon = Vector{Vector{Any}}()
     elt = eltype(unnamed(kettensor(nn, first(verts))))
     keep = Any[]
     for v in verts
@@ -130,20 +159,22 @@ function DeviceNetwork(nn::NormNetwork; device::Integer = 0)
         st_of = Dict(n => stride(data, i) for (i, n) in enumerate(names))
         sz_of = Dict(n => size(data, i) for (i, n) in enumerate(names))
         sites = sitenames(nn.ket, v)
-        # fused site axis: a single site name is required for a strided upload
         length(sites) <= 1 || throw(ArgumentError("vertex $v has several site indices"))
         push!(phys, isempty(sites) ? 1 : sz_of[only(sites)])
         push!(strides, isempty(sites) ? 0 : st_of[only(sites)])
+        cv = Any[isempty(sites) ? nothing : only(sites)]
         for w in neighbors(nn, v)
             ln = collect(linknames(nn.ket, v => w))
             length(ln) == 1 || throw(ArgumentError("edge $v => $w carries $(length(ln)) links; fuse them first"))
             slot[v => w] = length(nbr)
             push!(nbr, vidx[w]); push!(bond, sz_of[only(ln)]); push!(strides, st_of[only(ln)])
+            push!(cv, only(ln))
         end
         push!(off, length(nbr))
         push!(ptrs, pointer(data)); push!(keep, data)
+        push!(canon, cv)
     end
-    GC.@preserve keep off nbr bond phys begin
+    GC.@preserve keep off nbr bond phys ptrs strides begin
         check(ctx, ccall((:itn_graph_upload, libitn), Int32,
             (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int32}, Ptr{Int64}, Ptr{Int32}, Int32, Ptr{Int32}),
             ctx, length(verts), off, nbr, bond, C_NULL, phys, 2, C_NULL))
@@ -151,111 +182,303 @@ function DeviceNetwork(nn::NormNetwork; device::Integer = 0)
             (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Int64}), ctx, eltype_code(elt), ptrs, strides))
     end
     moff = cumsum(vcat(Int64(0), Int64.(bond) .^ 2))
-    d = DeviceNetwork(ctx, verts, slot, off, bond, moff, elt)
+    d = DeviceNetwork(ctx, verts, slot, off, bond, moff, elt, canon)
     finalizer(destroy!, d)
     return d
 end
 
-# Messages: D x D operator with (bra, ket) names; packed as m[bra][ket] row-major.
-function upload_messages!(d::DeviceNetwork, nn::NormNetwork, cache)
+# Messages: D x D operator with (bra, ket) names, packed as m[bra][ket] row-major
+# (the C layout): column-major M[bra, ket] is written out transposed.
+function pack_messages(d::DeviceNetwork, nn::NormNetwork, cache)
     packed = Vector{d.elt}(undef, d.moff[end])
     for ((a, b), s) in d.slot
         m = cache[a => b]
         ket = only(linknames(nn.ket, a => b))
-        bra = braname(nn, ket)
-        M = unnamed(permutedims(m, (bra, ket)))   # rows bra, columns ket
+        M = unnamed(permutedims(m, (braname(nn, ket), ket)))   # rows bra, columns ket
         packed[(d.moff[s + 1] + 1):d.moff[s + 2]] .= vec(permutedims(M, (2, 1)))
     end
-    check(d.ctx, ccall((:itn_messages_upload, libitn), Int32, (Ptr{Cvoid}, Int32, Ptr{Cvoid}),
-        d.ctx, eltype_code(d.elt), packed))
+    return packed
+end
+
+function upload_messages!(d::DeviceNetwork, nn::NormNetwork, cache)
+    packed = pack_messages(d, nn, cache)
+    GC.@preserve packed check(d.ctx, ccall((:itn_messages_upload, libitn), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}), d.ctx, eltype_code(d.elt), packed))
     return d
+end
+
+function message_block(d::DeviceNetwork, packed, s)
+    D = Int(d.bond[s + 1])
+    return permutedims(reshape(packed[(d.moff[s + 1] + 1):d.moff[s + 2]], D, D), (2, 1))  # M[bra, ket]
+end
+
+function store_message!(cache, nn::NormNetwork, edge::Pair, M)
+    ket = only(linknames(nn.ket, edge))
+    copyto!(unnamed(permutedims(cache[edge], (braname(nn, ket), ket))), M)
+    return cache
 end
 
 function download_messages!(cache, d::DeviceNetwork, nn::NormNetwork)
     packed = Vector{d.elt}(undef, d.moff[end])
-    check(d.ctx, ccall((:itn_messages_download, libitn), Int32, (Ptr{Cvoid}, Int32, Ptr{Cvoid}),
-        d.ctx, eltype_code(d.elt), packed))
+    GC.@preserve packed check(d.ctx, ccall((:itn_messages_download, libitn), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}), d.ctx, eltype_code(d.elt), packed))
     for ((a, b), s) in d.slot
-        D = Int(d.bond[s + 1])
-        M = permutedims(reshape(packed[(d.moff[s + 1] + 1):d.moff[s + 2]], D, D), (2, 1))
-        ket = only(linknames(nn.ket, a => b))
-        copyto!(unnamed(permutedims(cache[a => b], (braname(nn, ket), ket))), M)
+        store_message!(cache, nn, a => b, message_block(d, packed, s))
     end
     return cache
 end
 
-precision_code(p::Symbol) = p === :native ? Int32(0) : p === :bf16 ? Int32(1) :
-    p === :tf32 ? Int32(2) : p === :tf32x3 ? Int32(3) : throw(ArgumentError("unknown precision $p"))
+# One device context per (norm network, device) for the per-edge strategy, so that a
+# sequence of message_update! calls on the same factors uploads the tensors once.
+const EDGE_CONTEXTS = WeakKeyDict{Any, DeviceNetwork}()
 
-# The whole solve in one call: beliefpropagation(nn, messages; edges, stopping_criterion,
-# message_update_algorithm = GPUMessageUpdate(...)) dispatches here through AI.solve.
-function gpu_beliefpropagation(nn::NormNetwork, messages, alg::GPUMessageUpdate;
-        maxiter = nothing, tol = nothing, edges = nothing)
-    isnothing(maxiter) && isnothing(tol) &&
-        throw(ArgumentError("At least one of `maxiter` or `tol` must be specified."))
+"""
+    message_update!(alg::GPUMessageUpdate, cache, factors::NormNetwork, edge)
+
+The reference's strategy entry point (beliefpropagation.jl:214-257): recompute the message
+on `edge` from its incoming neighbours on the GPU (itn_message_update), normalised by its
+sum when `alg.normalize`, and write it into `cache`.
+"""
+function INN.message_update!(alg::GPUMessageUpdate, cache, factors::NormNetwork, edge)
+    d = get!(() -> DeviceNetwork(factors; device = alg.device), EDGE_CONTEXTS, factors)
+    upload_messages!(d, factors, cache)
+    e = src(edge) => dst(edge)
+    s = d.slot[e]
+    check(d.ctx, ccall((:itn_message_update, libitn), Int32, (Ptr{Cvoid}, Int64, Int32),
+        d.ctx, s, Int32(alg.normalize)))
+    packed = Vector{d.elt}(undef, d.moff[end])
+    GC.@preserve packed check(d.ctx, ccall((:itn_messages_download, libitn), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}), d.ctx, eltype_code(d.elt), packed))
+    store_message!(cache, factors, e, message_block(d, packed, s))
+    return cache
+end
+
+# (maxiter, tol) of the reference's stopping criteria (beliefpropagation.jl:16-55):
+# AI.StopAfterIteration, StopWhenConverged and their `|` combination.
+gpu_stopping(c::StopWhenConverged) = (nothing, c.tol)
+function gpu_stopping(c::AI.StopAfterIteration)
+    n = hasproperty(c, :max_iterations) ? c.max_iterations : getfield(c, 1)
+    return (Int(n), nothing)
+end
+function gpu_stopping(c::AI.StopWhenAny)
+    maxiter = nothing; tol = nothing
+    for x in c.criteria
+        m, t = gpu_stopping(x)
+        isnothing(m) || (maxiter = m)
+        isnothing(t) || (tol = t)
+    end
+    return (maxiter, tol)
+end
+gpu_stopping(c) = throw(ArgumentError("stopping criterion $c is not supported by GPUMessageUpdate"))
+
+"""
+    DeviceMessageCache
+
+A `MessageCache` together with the device context that holds the same messages (and the
+network's tensors), as returned by [`gpu_solve`](@ref); `bethe_free_energy(factors, ::DeviceMessageCache)`
+reads the messages where they are.
+"""
+struct DeviceMessageCache{C}
+    cache::C
+    dev::DeviceNetwork
+end
+
+const SweepGPU = INN.BeliefPropagationSweepAlgorithm{<:GPUMessageUpdate}
+
+# The whole solve as one device call; returns the messages on the host and keeps them on the
+# device (DeviceMessageCache).
+function gpu_solve(problem::INN.BeliefPropagationProblem{<:NormNetwork},
+                   algorithm::INN.BeliefPropagationAlgorithm{<:Any, <:SweepGPU}, iterate)
+    nn = problem.factors
+    alg = algorithm.subalgorithm.message_update_algorithm
+    maxiter, tol = gpu_stopping(algorithm.stopping_criterion)
     d = DeviceNetwork(nn; device = alg.device)
-    cache = MessageCache(messages)
+    cache = copy(MessageCache(iterate))
     upload_messages!(d, nn, cache)
     seq = alg.schedule === :sequential
-    eslots = seq ? Int64[d.slot[src(e) => dst(e)] for e in something(edges, collect(keys(cache)))] : Int64[]
+    eslots = seq ? Int64[d.slot[src(e) => dst(e)] for e in algorithm.edges] : Int64[]
     res = Ref{ItnBpResult}()
     GC.@preserve eslots begin
         opts = ItnBpOpts(seq ? 1 : 0, isnothing(maxiter) ? -1 : maxiter,
-            isnothing(tol) ? -1.0 : tol, 1, precision_code(alg.precision), alg.split_sweeps, 0,
-            seq ? pointer(eslots) : C_NULL, length(eslots))
+            isnothing(tol) ? -1.0 : tol, Int32(alg.normalize), precision_code(alg.precision),
+            alg.split_sweeps, 0, seq ? pointer(eslots) : C_NULL, length(eslots))
         check(d.ctx, ccall((:itn_bp_run, libitn), Int32,
             (Ptr{Cvoid}, Ref{ItnBpOpts}, Ref{ItnBpResult}), d.ctx, opts, res))
     end
     download_messages!(cache, d, nn)
-    destroy!(d)
-    return cache
+    return DeviceMessageCache(cache, d)
 end
 
-# bethe_free_energy(nn, messages) on the device (FP64 log-scalars).
-function gpu_bethe_free_energy(nn::NormNetwork, cache; device = 0)
-    d = DeviceNetwork(nn; device)
-    upload_messages!(d, nn, cache)
+"""
+    AI.solve(problem::BeliefPropagationProblem{<:NormNetwork}, algorithm; iterate)
+
+Specialisation for a sweep algorithm that carries a `GPUMessageUpdate`: the outer loop
+(StopAfterIteration(maxiter) | StopWhenConverged(tol), iteration 0 skipped, delta < tol),
+every sweep and the convergence test run on the device in one itn_bp_run call; returns the
+`MessageCache`, as `beliefpropagation` promises.
+"""
+function AI.solve(problem::INN.BeliefPropagationProblem{<:NormNetwork},
+                  algorithm::INN.BeliefPropagationAlgorithm{<:Any, <:SweepGPU}; iterate, kwargs...)
+    return gpu_solve(problem, algorithm, iterate).cache
+end
+
+"""
+    bethe_free_energy(factors::NormNetwork, messages::DeviceMessageCache)
+
+messagecache.jl:185-201 on the device: FP64 log-scalars, complex promotion when a real part is
+negative, -Inf when an edge scalar is zero.
+"""
+function INN.bethe_free_energy(nn::NormNetwork, messages::DeviceMessageCache)
+    d = messages.dev
     tot = zeros(Float64, 2); flags = zeros(Int32, 1)
-    check(d.ctx, ccall((:itn_logscalars, libitn), Int32,
+    GC.@preserve tot flags check(d.ctx, ccall((:itn_logscalars, libitn), Int32,
         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
         d.ctx, C_NULL, C_NULL, C_NULL, C_NULL, tot, flags))
-    destroy!(d)
     (flags[1] & 4) != 0 && return -Inf
     cplx = d.elt <: Complex || (flags[1] & 3) != 0
     return cplx ? complex(tot[1], tot[2]) : tot[1]
 end
 
+# ---- contract_network ------------------------------------------------------------------------
 """
-    bp_logz(nn; maxiter, tol, alg = GPUMessageUpdate()) -> log Z_BP
+    GPUExact(; order = nothing, order_alg = :greedy, precision = :native, device = 0)
 
-Converged BP log-norm of `nn`; differentiable through the rrule below.
+`contract_network` algorithm (the counterpart of `Exact`, contract_network.jl:7-10) that
+contracts pairwise on the GPU.  `order` is an explicit list of steps in the
+itn_contraction_order format or `nothing`; `order_alg` is `:greedy` or `:left`
+(LeftAssociative); `precision = :bf16` uses tcgen05 BF16 hi/lo products on Float32 data,
+`:tf32x3` TF32 hi/lo products (FP32 accuracy on the tensor cores).
 """
-function bp_logz(nn::NormNetwork, messages; alg = GPUMessageUpdate(), kwargs...)
-    cache = gpu_beliefpropagation(nn, messages, alg; kwargs...)
-    return gpu_bethe_free_energy(nn, cache; device = alg.device)
+Base.@kwdef struct GPUExact
+    order::Union{Nothing, Vector{Int32}} = nothing
+    order_alg::Symbol = :greedy
+    precision::Symbol = :native
+    device::Int = 0
 end
 
-# rrule: the pullback of the converged log-norm w.r.t. every ket tensor comes from the
-# implicit (adjoint BP) gradient, itn_bp_grad.
-function ChainRulesCore.rrule(::typeof(bp_logz), nn::NormNetwork, messages; alg = GPUMessageUpdate(), kwargs...)
-    cache = gpu_beliefpropagation(nn, messages, alg; kwargs...)
-    d = DeviceNetwork(nn; device = alg.device)
-    upload_messages!(d, nn, cache)
-    y = gpu_bethe_free_energy(nn, cache; device = alg.device)
+network_tensors(tn::AbstractVector) = collect(tn)
+network_tensors(tn::NormNetwork) =
+    reduce(vcat, [[kettensor(tn, v), conj_bratensor(tn, v)] for v in vertices(tn)])
+network_tensors(tn) = [tn[k] for k in keys(tn)]
+
+"""
+    contract_network(alg::GPUExact, tn)
+
+Exact contraction of a vector of ITensors, an `ITensorNetwork` or a `NormNetwork` by pairwise
+GPU contractions (itn_contract_network).  Column-major Julia arrays are handed over as
+row-major arrays of the reversed axis order; the result comes back the same way.
+"""
+function INN.contract_network(alg::GPUExact, tn)
+    ts = network_tensors(tn)
+    T = promote_type(map(t -> eltype(unnamed(t)), ts)...)
+    code = Dict{Any, Int64}()
+    index_of = Dict{Any, Any}()
+    ranks = Int32[]; labels = Int64[]; dims = Int64[]; datas = Any[]
+    for t in ts
+        names = dimnames(t)
+        for (n, i) in zip(names, inds(t))
+            index_of[n] = i
+        end
+        a = convert(Array{T}, unnamed(t))
+        push!(datas, a)
+        push!(ranks, length(names))
+        for k in length(names):-1:1                    # column-major = reversed row-major
+            push!(labels, get!(code, names[k], length(code)))
+            push!(dims, size(a, k))
+        end
+    end
+    ptrs = Ptr{Cvoid}[pointer(a) for a in datas]
+    out_rank = Ref{Int32}(0)
+    # the result holds the open indices (labels that occur once)
+    count = Dict{Int64, Int}()
+    for l in labels
+        count[l] = get(count, l, 0) + 1
+    end
+    cap = prod((dims[k] for k in eachindex(labels) if count[labels[k]] == 1); init = Int64(1))
+    out = Vector{T}(undef, cap)
+    out_labels = zeros(Int64, 48); out_dims = zeros(Int64, 48)
+    steps = isnothing(alg.order) ? C_NULL : alg.order
+    order_code = !isnothing(alg.order) ? Int32(2) : alg.order_alg === :left ? Int32(1) : Int32(0)
+    ctxr = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:itn_create, libitn), Int32, (Ptr{Ptr{Cvoid}}, Int32, Int32), ctxr, alg.device, 0)
+    st == ITN_OK || error("itn_create failed with status $st")
+    try
+        GC.@preserve datas ptrs ranks labels dims out out_labels out_dims steps begin
+            check(ctxr[], ccall((:itn_contract_network, libitn), Int32,
+                (Ptr{Cvoid}, Int32, Int32, Ptr{Int32}, Ptr{Int64}, Ptr{Int64}, Ptr{Ptr{Cvoid}}, Int32,
+                 Ptr{Int32}, Int32, Ptr{Cvoid}, Int64, Ref{Int32}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}),
+                ctxr[], eltype_code(T), length(ts), ranks, labels, dims, ptrs, order_code, steps,
+                precision_code(alg.precision), out, cap, out_rank, out_labels, out_dims, C_NULL))
+        end
+    finally
+        ccall((:itn_destroy, libitn), Int32, (Ptr{Cvoid},), ctxr[])
+    end
+    r = Int(out_rank[])
+    name_of = Dict(c => n for (n, c) in code)
+    names = [name_of[out_labels[k]] for k in r:-1:1]    # back to column-major order
+    shape = Tuple(Int(out_dims[k]) for k in r:-1:1)
+    data = reshape(out[1:prod(shape; init = 1)], shape)
+    return data[(index_of[n] for n in names)...]
+end
+
+# ---- the converged log-norm and its gradient ----------------------------------------------------
+"""
+    bp_logz(nn, messages; alg = GPUMessageUpdate(schedule = :parallel), edges, maxiter, tol)
+
+Converged BP log-norm of `nn` (beliefpropagation followed by bethe_free_energy), on the GPU;
+differentiable through the rrule below.
+"""
+function bp_logz(nn::NormNetwork, messages; alg = GPUMessageUpdate(; schedule = :parallel),
+                 edges = collect(keys(MessageCache(messages))), maxiter = nothing, tol = nothing)
+    problem = INN.BeliefPropagationProblem(nn)
+    sub = INN.BeliefPropagationSweepAlgorithm(; message_update_algorithm = alg,
+        stopping_criterion = AI.StopAfterIteration(length(edges)))
+    crit = INN.select_beliefpropagation_stopping_criterion((; maxiter, tol))
+    algorithm = INN.BeliefPropagationAlgorithm(; edges, subalgorithm = sub, stopping_criterion = crit)
+    dc = gpu_solve(problem, algorithm, messages)
+    y = INN.bethe_free_energy(nn, dc)
+    return y, dc
+end
+
+# The packed canonical gradient (per vertex row-major [site, legs in CSR order]) as an array
+# in the ket tensor's own (column-major) index order.
+function unpack_gradient(d::DeviceNetwork, nn::NormNetwork, g::Vector, k::Int, toff::Int)
+    v = d.verts[k]
+    A = kettensor(nn, v)
+    names = dimnames(A)
+    data = unnamed(A)
+    cnames = [n for n in d.canon[k] if !isnothing(n)]
+    cdims = Tuple(size(data, findfirst(==(n), collect(names))) for n in cnames)
+    n = prod(cdims; init = 1)
+    # row-major [c1, c2, ...] = column-major [..., c2, c1]
+    blk = reshape(g[(toff + 1):(toff + n)], reverse(cdims))
+    pos = [length(cnames) + 1 - findfirst(==(nm), cnames) for nm in names]
+    return permutedims(blk, pos), toff + n
+end
+
+function ChainRulesCore.rrule(::typeof(bp_logz), nn::NormNetwork, messages; kwargs...)
+    y, dc = bp_logz(nn, messages; kwargs...)
+    d = dc.dev
     function bp_logz_pullback(ȳ)
-        n = d.off  # tensor sizes follow the upload order
+        ȳ = ChainRulesCore.unthunk(ȳ)
         total = sum(length(unnamed(kettensor(nn, v))) for v in d.verts)
         g = Vector{d.elt}(undef, total)
         res = Ref{ItnGradResult}()
-        check(d.ctx, ccall((:itn_bp_grad, libitn), Int32,
+        GC.@preserve g check(d.ctx, ccall((:itn_bp_grad, libitn), Int32,
             (Ptr{Cvoid}, Ref{ItnGradOpts}, Ptr{Cvoid}, Ref{ItnGradResult}),
-            d.ctx, ItnGradOpts(1, 200, 1e-10, 1, 0), g, res))
-        destroy!(d)
-        # g is in canonical [site, legs...] row-major order per vertex; the caller maps it
-        # back onto each ket tensor's index order (the inverse of the upload strides).
-        return NoTangent(), ȳ .* g, NoTangent()
+            d.ctx, ItnGradOpts(1, 200, 1e-10, 1, 0, 1, 0), g, res))
+        # d log Z / d A_v for every ket tensor, each in its own index order: the tangent of
+        # the NormNetwork's ket network (its bra is a function of the ket)
+        toff = 0
+        ket_tangents = Dict{eltype(d.verts), Any}()
+        for k in eachindex(d.verts)
+            arr, toff = unpack_gradient(d, nn, g, k, toff)
+            ket_tangents[d.verts[k]] = ȳ .* arr
+        end
+        nn_tangent = Tangent{typeof(nn)}(; ket = ket_tangents)
+        return NoTangent(), nn_tangent, NoTangent()
     end
-    return y, bp_logz_pullback
+    return (y, dc), bp_logz_pullback
 end
 
 # ---- gate application (src/apply/apply_operators.jl:209-283) -------------------------------

@@ -36,7 +36,7 @@ def test_python_binding_covers_header(lib_built):
 def test_abi_version_and_status_strings(lib_built):
     from itn_gb300 import _lib as L
     lib = L.load(lib_built)
-    assert lib.itn_abi_version() == 1
+    assert lib.itn_abi_version() == 2
     assert lib.itn_status_string(0) == b"ok"
     assert lib.itn_status_string(1) == b"invalid argument"
 
