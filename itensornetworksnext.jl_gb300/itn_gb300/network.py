@@ -187,6 +187,53 @@ def normnetwork(tn: ITensorNetwork, braname=None):
     return NormNetwork(tn, braname)
 
 
+class _NormView:
+    """A read-only view of one layer of a NormNetwork with its graph structure
+    (KetView / BraView, src/normnetworkview.jl:6-58)."""
+
+    def __init__(self, parent: NormNetwork):
+        self.parent = parent
+
+    def vertices(self):
+        return self.parent.vertices()
+
+    def edges(self):
+        return self.parent.edges()
+
+    def is_vertex_assigned(self, v):
+        return v in self.parent.ket.tensors
+
+    def issettable(self):
+        return False
+
+    def isinsertable(self):
+        return False
+
+    def __setitem__(self, v, t):
+        raise TypeError(f"{type(self).__name__} is a read-only view of a NormNetwork")
+
+
+class KetView(_NormView):
+    """The ket layer: view[v] is kettensor(nn, v) itself."""
+
+    def __getitem__(self, v):
+        return self.parent.kettensor(v)
+
+    def linknames(self, u, v):
+        return self.parent.ket.linknames(u, v)
+
+
+class BraView(_NormView):
+    """The bra layer: view[v] is bratensor(nn, v) (link names mapped by braname, data
+    conjugated)."""
+
+    def __getitem__(self, v):
+        return self.parent.bratensor(v)
+
+    def linknames(self, u, v):
+        return [self.parent.bra(n) for n in self.parent.ket.linknames(u, v)]
+
+
 # ---- message caches -----------------------------------------------------------------------------
 class MessageCache:
     """Directed edge (u, v) -> message ITensor (src/beliefpropagation/messagecache.jl:15-52)."""

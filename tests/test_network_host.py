@@ -151,3 +151,30 @@ def test_message_cache_basics():
     assert dst[((1, 1), (1, 2))] == ""
     assert dst[((1, 2), (2, 2))] == "(1, 2) => (2, 2)"
     assert dst[((2, 2), (2, 3))] == "(2, 2) => (2, 3)"
+
+
+def test_ket_and_bra_views():
+    """test_normnetwork.jl:106-134: the views share the graph, the ket view exposes the ket
+    tensors themselves and the bra view the bra tensors; both are read-only."""
+    rng = np.random.default_rng(4)
+    links = {(0, 1): N.Index(2), (1, 2): N.Index(3)}
+    site = {v: N.Index(2) for v in range(3)}
+    ts = {}
+    for v in range(3):
+        inds = [site[v]] + [i for (a, b), i in links.items() if v in (a, b)]
+        shape = tuple(i.dim for i in inds)
+        ts[v] = N.ITensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape), inds)
+    tn = N.ITensorNetwork(ts)
+    nn = N.NormNetwork(tn)
+    kv, bv = N.KetView(nn), N.BraView(nn)
+    assert set(kv.vertices()) == set(bv.vertices()) == set(tn.vertices())
+    assert set(kv.edges()) == set(bv.edges()) == set(tn.edges())
+    for v in tn.vertices():
+        assert kv[v] is nn.kettensor(v)
+        assert bv[v].inds == nn.bratensor(v).inds
+        np.testing.assert_array_equal(bv[v].data, np.conj(tn[v].data))
+    assert kv.is_vertex_assigned(1) and bv.is_vertex_assigned(1)
+    assert not kv.issettable() and not kv.isinsertable() and not bv.issettable() and not bv.isinsertable()
+    assert bv.linknames(0, 1) == [nn.bra(n) for n in kv.linknames(0, 1)]
+    with pytest.raises(TypeError):
+        kv[0] = tn[0]
