@@ -176,8 +176,9 @@ int32_t itn_contraction_order(int32_t n_tensors, const int32_t *ranks, const int
  * contraction by pairwise GPU contractions (device permute + GEMM).  tensors[t] are host
  * row-major arrays in the order of their labels.  alg 0 = Greedy, 1 = LeftAssociative,
  * 2 = explicit `steps` (the itn_contraction_order format).  precision: ITN_PREC_NATIVE
- * (dtype arithmetic on CUDA cores) or ITN_PREC_BF16 (float32 data, tcgen05 GEMM with BF16
- * hi/lo split operands).  The result (row-major in the order of out_labels, at most 48
+ * (dtype arithmetic on CUDA cores), ITN_PREC_BF16 (float32 data, tcgen05 GEMM with BF16
+ * hi/lo split operands, ~16 significant bits) or ITN_PREC_TF32X3 (float32 data, tcgen05 GEMM
+ * with TF32 hi/lo split operands: the accuracy of FP32 arithmetic).  The result (row-major in the order of out_labels, at most 48
  * indices) is copied to `out` if out_capacity elements suffice; device_ms (may be NULL)
  * receives the device time of the pairwise steps. */
 int32_t itn_contract_network(itn_ctx *ctx, int32_t dtype, int32_t n_tensors, const int32_t *ranks,

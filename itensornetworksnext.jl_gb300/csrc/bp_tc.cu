@@ -1354,6 +1354,8 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
 
 const int* tc_err_ptr(const TcEngine* e) { return e ? e->d_err : nullptr; }
 
+bool tc_tf32_ok() { return g_probe.ran && g_probe.tf32_ok; }
+
 void tc_set_wait_limit(TcEngine* e, uint64_t ns) {
   if (e) e->wait_ns = ns;
 }

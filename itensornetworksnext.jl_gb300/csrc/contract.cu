@@ -7,7 +7,7 @@
 // permutes its two operands into GEMM form -- A as [free_A, shared], B as [shared, free_B]
 // (row-major) -- with a strided permute kernel and multiplies them with a tiled GEMM:
 //   * CUDA cores for float / double / complex (64 x 64 tiles, 4 x 4 register blocking);
-//   * tcgen05 for float in BF16 split precision (hi/lo operands, 3 MMAs per product,
+//   * tcgen05 for float in BF16 or TF32 split precision (hi/lo operands, 3 MMAs per product,
 //     FP32 accumulation in TMEM) -- contract_gemm_tc in this file.
 // The result carries the labels free_A ++ free_B.
 #include <cuda_runtime.h>
@@ -205,24 +205,58 @@ cudaError_t contract_gemm(int dtype, const void* A, const void* B, void* C, long
 }
 
 
-// ---- tcgen05 GEMM, BF16 hi/lo split (float32 in, float32 out) --------------------------------
-// Operands are packed into K-major core-matrix tiles: A tile (mt, kt) = 128 rows x 64 k,
-// B tile (nt, kt) = 64 columns of B (as rows) x 64 k; each tile holds its hi part followed by
-// its lo part.  One CTA computes a 128 x 64 block of C with D in 64 TMEM columns, streaming K
-// through a two-stage bulk-TMA pipeline.
+// ---- tcgen05 GEMM with hi/lo split operands (float32 in, float32 out) --------------------------
+// Two operand modes: BF16 hi/lo (x = hi + lo, both BF16: ~16 significant bits, kind::f16) and
+// TF32 hi/lo (hi = the TF32 rounding of x, lo = the TF32 rounding of x - hi: ~21 bits, the
+// accuracy of FP32 arithmetic, kind::tf32).  Each product is hi*hi + lo*hi + hi*lo (3 MMAs).
+// Operands are packed into K-major core-matrix tiles (cores of 8 rows x 16 bytes): A tile
+// (mt, kt) = 128 rows x 64 k, B tile (nt, kt) = 64 columns of B (as rows) x 64 k; each tile
+// holds its hi part followed by its lo part.  One CTA computes a 128 x 64 block of C with D in
+// 64 TMEM columns, streaming K through a two-stage bulk-TMA pipeline.
 namespace {
 
-constexpr int kTcBlk = 8192;                      // 64 x 64 BF16 block
-constexpr uint32_t kTcATile = 4 * kTcBlk;          // 128 rows: 2 blocks hi + 2 blocks lo
-constexpr uint32_t kTcBTile = 2 * kTcBlk;          // 64 rows: 1 block hi + 1 block lo
+template <int MODE> struct GemmMode;  // 0: BF16 hi/lo, 1: TF32 hi/lo
+template <> struct GemmMode<0> {
+  static constexpr uint32_t blk = 8192;   // 64 x 64 block
+  static constexpr uint32_t sbo = 1024;   // bytes between 8-row core groups
+  static constexpr int ksteps = 4;        // MMAs per K = 64
+};
+template <> struct GemmMode<1> {
+  static constexpr uint32_t blk = 16384;
+  static constexpr uint32_t sbo = 2048;
+  static constexpr int ksteps = 8;
+};
+template <int MODE> constexpr uint32_t a_tile() { return 4 * GemmMode<MODE>::blk; }  // 2 blocks hi + 2 lo
+template <int MODE> constexpr uint32_t b_tile() { return 2 * GemmMode<MODE>::blk; }  // 1 block hi + 1 lo
 constexpr uint32_t kTcPolls = 1u << 26;
 
+// byte offset of element (r, k) inside a 64 x 64 block of the mode
+template <int MODE>
 __host__ __device__ __forceinline__ uint32_t cblk_off(int r, int k) {
-  return (uint32_t)((((r >> 3) << 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+  if constexpr (MODE == 1)
+    return (uint32_t)((((r >> 3) << 4) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+  else
+    return (uint32_t)((((r >> 3) << 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
+// hi and lo parts of x, stored at the element's offset in the hi and lo planes
+template <int MODE>
+__device__ __forceinline__ void put_split(unsigned char* hi, unsigned char* lo, uint32_t o, float x) {
+  if constexpr (MODE == 1) {
+    const uint32_t h = ptx::to_tf32(x);
+    *reinterpret_cast<uint32_t*>(hi + o) = h;
+    *reinterpret_cast<uint32_t*>(lo + o) = ptx::to_tf32(x - __uint_as_float(h));
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    *reinterpret_cast<__nv_bfloat16*>(hi + o) = h;
+    *reinterpret_cast<__nv_bfloat16*>(lo + o) = __float2bfloat16_rn(x - __bfloat162float(h));
+  }
+}
+
+template <int MODE>
 __global__ void pack_a_kernel(const float* __restrict__ A, long long M, long long K, long long kt_n,
                               unsigned char* __restrict__ out, long long tiles) {
+  constexpr uint32_t blk = GemmMode<MODE>::blk;
   // one thread per (tile, row, k): element A[m][k]
   const long long total = tiles * 128 * 64;
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total; j += (long long)gridDim.x * blockDim.x) {
@@ -231,17 +265,16 @@ __global__ void pack_a_kernel(const float* __restrict__ A, long long M, long lon
     const long long mt = t / kt_n, kt = t % kt_n;
     const long long m = mt * 128 + r, kk = kt * 64 + k;
     const float x = (m < M && kk < K) ? A[m * K + kk] : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-    unsigned char* base = out + t * kTcATile;
-    const uint32_t o = (r >> 6) * kTcBlk + cblk_off(r & 63, k);
-    *reinterpret_cast<__nv_bfloat16*>(base + o) = h;
-    *reinterpret_cast<__nv_bfloat16*>(base + 2 * kTcBlk + o) = l;
+    unsigned char* base = out + t * a_tile<MODE>();
+    const uint32_t o = (r >> 6) * blk + cblk_off<MODE>(r & 63, k);
+    put_split<MODE>(base, base + 2 * blk, o, x);
   }
 }
 
+template <int MODE>
 __global__ void pack_b_kernel(const float* __restrict__ B, long long K, long long N, long long kt_n,
                               unsigned char* __restrict__ out, long long tiles) {
+  constexpr uint32_t blk = GemmMode<MODE>::blk;
   const long long total = tiles * 64 * 64;
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total; j += (long long)gridDim.x * blockDim.x) {
     const long long t = j >> 12;
@@ -249,21 +282,26 @@ __global__ void pack_b_kernel(const float* __restrict__ B, long long K, long lon
     const long long nt = t / kt_n, kt = t % kt_n;
     const long long n = nt * 64 + r, kk = kt * 64 + k;
     const float x = (n < N && kk < K) ? B[kk * N + n] : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-    unsigned char* base = out + t * kTcBTile;
-    *reinterpret_cast<__nv_bfloat16*>(base + cblk_off(r, k)) = h;
-    *reinterpret_cast<__nv_bfloat16*>(base + kTcBlk + cblk_off(r, k)) = l;
+    unsigned char* base = out + t * b_tile<MODE>();
+    put_split<MODE>(base, base + blk, cblk_off<MODE>(r, k), x);
   }
 }
 
+// The tensor core sums each K = 64 tile into TMEM; after every tile the 128 threads read the
+// tile's partial products and add them to FP32 registers (one row of 64 columns per thread),
+// so that the long sum over K runs in round-to-nearest FP32 on the CUDA cores.  Loads of tile
+// kt + 1 overlap the MMAs of tile kt (two smem stages); the readout of tile kt precedes the
+// MMAs of tile kt + 1, which overwrite the same 64 TMEM columns.
+template <int MODE>
 __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __restrict__ Ap,
                                                       const unsigned char* __restrict__ Bp, float* __restrict__ C,
                                                       long long M, long long N, long long kt_n, long long nt_n,
                                                       int* err) {
+  using G = GemmMode<MODE>;
+  constexpr uint32_t kA = a_tile<MODE>(), kB = b_tile<MODE>();
   extern __shared__ __align__(1024) unsigned char sm[];
   // stage s: A tile at s * (A + B), B tile after it
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * (kTcATile + kTcBTile));  // load[2], mma[2]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * (kA + kB));  // load[2], mma
   uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bar + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long mt = blockIdx.x / nt_n, nt = blockIdx.x % nt_n;
@@ -272,73 +310,100 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __res
     ptx::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < 4; ++i) ptx::mbar_init(bar + i, 1);
+    for (int i = 0; i < 3; ++i) ptx::mbar_init(bar + i, 1);
     ptx::fence_mbar_init();
   }
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *taddr_s;
-  bool ok = true;
-  if (tid == 0) {
-    const uint32_t sb = ptx::smem_u32(sm);
-    constexpr uint32_t idesc = ptx::idesc_bf16_f32(128, 64);
-    uint32_t ph_load[2] = {0, 0}, ph_mma[2] = {0, 0};
-    auto load = [&](long long kt, int s) {
-      unsigned char* dst = sm + s * (kTcATile + kTcBTile);
-      ptx::mbar_arrive_expect_tx(bar + s, kTcATile + kTcBTile);
-      ptx::bulk_g2s(dst, Ap + (mt * kt_n + kt) * kTcATile, kTcATile, bar + s);
-      ptx::bulk_g2s(dst + kTcATile, Bp + (nt * kt_n + kt) * kTcBTile, kTcBTile, bar + s);
-    };
-    load(0, 0);
-    for (long long kt = 0; kt < kt_n && ok; ++kt) {
-      const int s = (int)(kt & 1);
-      if (kt + 1 < kt_n) {
-        const int s2 = (int)((kt + 1) & 1);
-        if (kt + 1 >= 2) {  // stage s2 was last read by the MMAs of step kt - 1
-          ok = ptx::mbar_wait_bounded(bar + 2 + s2, ph_mma[s2], kTcPolls);
-          ph_mma[s2] ^= 1;
-        }
-        if (ok) load(kt + 1, s2);
-      }
-      if (ok) ok = ptx::mbar_wait_bounded(bar + s, ph_load[s], kTcPolls);
-      ph_load[s] ^= 1;
-      if (!ok) break;
-      ptx::tc_fence_after();
-      const uint32_t a = sb + s * (kTcATile + kTcBTile), b = a + kTcATile;
+  const uint32_t sb = ptx::smem_u32(sm);
+  constexpr uint32_t idesc = MODE == 1 ? ptx::idesc_tf32_f32(128, 64) : ptx::idesc_bf16_f32(128, 64);
+  auto load = [&](long long kt, int s) {
+    unsigned char* dst = sm + s * (kA + kB);
+    ptx::mbar_arrive_expect_tx(bar + s, kA + kB);
+    ptx::bulk_g2s(dst, Ap + (mt * kt_n + kt) * kA, kA, bar + s);
+    ptx::bulk_g2s(dst + kA, Bp + (nt * kt_n + kt) * kB, kB, bar + s);
+  };
+  auto mma = [&](uint32_t a, uint32_t b, uint32_t acc) {
+    const uint64_t ad = ptx::smem_desc(a, 128, G::sbo), bd = ptx::smem_desc(b, 128, G::sbo);
+    if constexpr (MODE == 1) ptx::mma_tf32(tmem, ad, bd, idesc, acc);
+    else ptx::mma_bf16(tmem, ad, bd, idesc, acc);
+  };
+  uint32_t ph_load[2] = {0, 0}, ph_mma = 0;
+  bool ld_pend[2] = {false, false};  // tid 0: copies in flight per stage
+  float acc[64];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint32_t ko = (uint32_t)(2 * j) * 128;
-        const uint32_t acc = (kt > 0 || j > 0) ? 1u : 0u;
-        ptx::mma_bf16(tmem, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc, acc);
-        ptx::mma_bf16(tmem, ptx::smem_desc(a + 2 * kTcBlk + ko, 128, 1024), ptx::smem_desc(b + ko, 128, 1024), idesc, 1);
-        ptx::mma_bf16(tmem, ptx::smem_desc(a + ko, 128, 1024), ptx::smem_desc(b + kTcBlk + ko, 128, 1024), idesc, 1);
-      }
-      ptx::mma_commit(bar + 2 + s);
-    }
-    if (ok) {
-      // the last commit covers every MMA issued before it
-      const int sl = (int)((kt_n - 1) & 1);
-      ok = ptx::mbar_wait_bounded(bar + 2 + sl, ph_mma[sl], kTcPolls);
-    }
-    if (!ok) atomicExch(err, 1);
+  for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+  if (tid == 0) {
+    load(0, 0);
+    ld_pend[0] = true;
   }
-  ok = __syncthreads_and(tid == 0 ? ok : true);
-  ptx::tc_fence_after();
-  if (ok) {
-    const int row = warp * 32 + lane;
-    const long long m = mt * 128 + row;
+  bool ok = true, mma_lost = false;
+  for (long long kt = 0; kt < kt_n; ++kt) {
+    const int s = (int)(kt & 1);
+    bool mine = true;
+    if (tid == 0) {
+      // stage s ^ 1 was last read by the MMAs of tile kt - 1, which completed before the
+      // readout below
+      if (kt + 1 < kt_n) {
+        load(kt + 1, s ^ 1);
+        ld_pend[s ^ 1] = true;
+      }
+      mine = ptx::mbar_wait_bounded(bar + s, ph_load[s], kTcPolls);
+      if (mine) ld_pend[s] = false;
+      ph_load[s] ^= 1;
+      if (mine) {
+        ptx::tc_fence_after();
+        const uint32_t a = sb + s * (kA + kB), b = a + kA;
+#pragma unroll
+        for (int j = 0; j < G::ksteps; ++j) {
+          const uint32_t ko = (uint32_t)(2 * j) * 128;  // two core columns per MMA
+          mma(a + ko, b + ko, j > 0 ? 1u : 0u);
+          mma(a + 2 * G::blk + ko, b + ko, 1);
+          mma(a + ko, b + G::blk + ko, 1);
+        }
+        ptx::mma_commit(bar + 2);
+      }
+    }
+    if (!__syncthreads_and(mine)) {
+      ok = false;
+      break;
+    }
+    if (!__syncthreads_and(ptx::mbar_wait_bounded(bar + 2, ph_mma, kTcPolls))) {
+      ok = false;
+      mma_lost = true;
+      break;
+    }
+    ph_mma ^= 1;
+    ptx::tc_fence_after();
 #pragma unroll
     for (int cb = 0; cb < 4; ++cb) {
       float v[16];
       ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cb * 16, v);
       ptx::tmem_wait_ld();
-      if (m < M) {
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const long long n = nt * 64 + cb * 16 + e;
-          if (n < N) C[m * N + n] = v[e];
-        }
+      for (int e = 0; e < 16; ++e) acc[cb * 16 + e] += v[e];
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok && tid == 0) {
+    atomicExch(err, 1);
+    // let copies still in flight land before the shared memory is released (bounded)
+    for (int st = 0; st < 2; ++st)
+      if (ld_pend[st]) ptx::mbar_wait_bounded(bar + st, ph_load[st], kTcPolls);
+    // and MMAs whose completion was not seen, before the tensor memory is released
+    if (mma_lost) ptx::mbar_wait_bounded(bar + 2, ph_mma, kTcPolls);
+  }
+  if (ok) {
+    const int row = warp * 32 + lane;
+    const long long m = mt * 128 + row;
+    if (m < M) {
+#pragma unroll
+      for (int e = 0; e < 64; ++e) {
+        const long long n = nt * 64 + e;
+        if (n < N) C[m * N + n] = acc[e];
       }
     }
   }
@@ -352,22 +417,16 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __res
 
 int* g_tc_err = nullptr;
 
-}  // namespace
-
-cudaError_t contract_gemm_tc(const float* A, const float* B, float* C, long long M, long long N, long long K,
-                             cudaStream_t st) {
-  if (M == 0 || N == 0) return cudaSuccess;
-  int m128 = 0, m64 = 0;
-  cudaError_t e = tc_run_probe(st, &m128, &m64, nullptr, nullptr);
-  if (e != cudaSuccess) return e;
-  if (!m128) return cudaErrorNotSupported;
-  if (K == 0) return cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st);
+template <int MODE>
+cudaError_t gemm_tc_run(const float* A, const float* B, float* C, long long M, long long N, long long K,
+                        cudaStream_t st) {
+  constexpr uint32_t kA = a_tile<MODE>(), kB = b_tile<MODE>();
   const long long mt_n = (M + 127) / 128, nt_n = (N + 63) / 64, kt_n = (K + 63) / 64;
   if (mt_n * nt_n > 0x7fffffffLL) return cudaErrorInvalidValue;
   unsigned char *Ap = nullptr, *Bp = nullptr;
-  e = cudaMallocAsync(&Ap, (size_t)(mt_n * kt_n) * kTcATile, st);
+  cudaError_t e = cudaMallocAsync(&Ap, (size_t)(mt_n * kt_n) * kA, st);
   if (e != cudaSuccess) return e;
-  e = cudaMallocAsync(&Bp, (size_t)(nt_n * kt_n) * kTcBTile, st);
+  e = cudaMallocAsync(&Bp, (size_t)(nt_n * kt_n) * kB, st);
   if (e != cudaSuccess) {
     cudaFreeAsync(Ap, st);
     return e;
@@ -378,15 +437,30 @@ cudaError_t contract_gemm_tc(const float* A, const float* B, float* C, long long
     cudaMemsetAsync(g_tc_err, 0, sizeof(int), st);
   }
   const long long at = mt_n * kt_n, bt = nt_n * kt_n;
-  pack_a_kernel<<<(int)std::min<long long>((at * 8192 + 255) / 256, 1 << 20), 256, 0, st>>>(A, M, K, kt_n, Ap, at);
-  pack_b_kernel<<<(int)std::min<long long>((bt * 4096 + 255) / 256, 1 << 20), 256, 0, st>>>(B, K, N, kt_n, Bp, bt);
-  const size_t smem = 2 * (kTcATile + kTcBTile) + 64;
-  cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  gemm_tc_kernel<<<(unsigned)(mt_n * nt_n), 128, smem, st>>>(Ap, Bp, C, M, N, kt_n, nt_n, g_tc_err);
+  pack_a_kernel<MODE><<<(int)std::min<long long>((at * 8192 + 255) / 256, 1 << 20), 256, 0, st>>>(A, M, K, kt_n, Ap,
+                                                                                                  at);
+  pack_b_kernel<MODE><<<(int)std::min<long long>((bt * 4096 + 255) / 256, 1 << 20), 256, 0, st>>>(B, K, N, kt_n, Bp,
+                                                                                                  bt);
+  const size_t smem = 2 * (kA + kB) + 64;
+  cudaFuncSetAttribute(gemm_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gemm_tc_kernel<MODE><<<(unsigned)(mt_n * nt_n), 128, smem, st>>>(Ap, Bp, C, M, N, kt_n, nt_n, g_tc_err);
   e = cudaGetLastError();
   cudaFreeAsync(Ap, st);
   cudaFreeAsync(Bp, st);
   return e;
+}
+
+}  // namespace
+
+cudaError_t contract_gemm_tc(const float* A, const float* B, float* C, long long M, long long N, long long K,
+                             cudaStream_t st, bool tf32) {
+  if (M == 0 || N == 0) return cudaSuccess;
+  int m128 = 0, m64 = 0;
+  cudaError_t e = tc_run_probe(st, &m128, &m64, nullptr, nullptr);
+  if (e != cudaSuccess) return e;
+  if (!m128 || (tf32 && !tc_tf32_ok())) return cudaErrorNotSupported;
+  if (K == 0) return cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st);
+  return tf32 ? gemm_tc_run<1>(A, B, C, M, N, K, st) : gemm_tc_run<0>(A, B, C, M, N, K, st);
 }
 
 }  // namespace itn

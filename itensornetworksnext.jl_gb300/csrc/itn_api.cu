@@ -2103,8 +2103,10 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
                              int64_t* out_labels, int64_t* out_dims, double* device_ms) {
   if (!c) return ITN_ERR_ARG;
   if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
-  if (precision != ITN_PREC_NATIVE && !(precision == ITN_PREC_BF16 && dtype == ITN_F32))
-    return fail(c, ITN_ERR_UNSUPPORTED, "contract_network precision %d needs float32 data (BF16 split)", precision);
+  if (precision != ITN_PREC_NATIVE &&
+      !((precision == ITN_PREC_BF16 || precision == ITN_PREC_TF32X3) && dtype == ITN_F32))
+    return fail(c, ITN_ERR_UNSUPPORTED,
+                "contract_network precision %d needs float32 data (BF16 split or TF32 split)", precision);
   if (!tensors || !out_rank) return fail(c, ITN_ERR_ARG, "null pointer");
   if (alg != 0 && alg != 1 && alg != 2) return fail(c, ITN_ERR_ARG, "unknown order algorithm %d", alg);
   if (int r = ensure_device(c)) return r;
@@ -2199,9 +2201,9 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
     }
     if (e == cudaSuccess) e = cudaMallocAsync(&tc, std::max<size_t>((size_t)M * N * es, 16), c->stream);
     if (e == cudaSuccess) {
-      if (precision == ITN_PREC_BF16)
+      if (precision == ITN_PREC_BF16 || precision == ITN_PREC_TF32X3)
         e = contract_gemm_tc(reinterpret_cast<const float*>(ta), reinterpret_cast<const float*>(tb),
-                             reinterpret_cast<float*>(tc), M, N, K, c->stream);
+                             reinterpret_cast<float*>(tc), M, N, K, c->stream, precision == ITN_PREC_TF32X3);
       else
         e = contract_gemm(dtype, ta, tb, tc, M, N, K, c->stream);
     }

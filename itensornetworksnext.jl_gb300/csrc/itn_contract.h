@@ -23,9 +23,10 @@ cudaError_t contract_permute(int dtype, const void* in, void* out, const std::ve
 cudaError_t contract_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K,
                           cudaStream_t st);
 
-// Float32 C[M,N] = A[M,K] B[K,N] on tcgen05 with BF16 hi/lo split operands (3 MMAs per
-// product).  Returns cudaErrorNotSupported when the tensor-core self-test has not passed.
+// Float32 C[M,N] = A[M,K] B[K,N] on tcgen05 with hi/lo split operands (3 MMAs per product):
+// BF16 hi/lo, or TF32 hi/lo when `tf32` (FP32 accuracy).  Returns cudaErrorNotSupported when
+// the tensor-core self-test has not passed.
 cudaError_t contract_gemm_tc(const float* A, const float* B, float* C, long long M, long long N, long long K,
-                             cudaStream_t st);
+                             cudaStream_t st, bool tf32);
 
 }  // namespace itn

@@ -54,5 +54,7 @@ cudaError_t tc_note_launches(TcEngine* e, int n, cudaStream_t st);
 // One-CTA tcgen05 self-test (cached per process): M=128 product exact, M=64
 // accumulator lane map found.  lane_of_row may be null (64 entries otherwise).
 cudaError_t tc_run_probe(cudaStream_t st, int* m128_ok, int* m64_ok, double* max_err, int* lane_of_row);
+// The probe's exact TF32 product (kind::tf32) passed (false before the probe has run).
+bool tc_tf32_ok();
 
 }  // namespace itn

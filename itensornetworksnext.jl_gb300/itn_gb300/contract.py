@@ -16,7 +16,7 @@ from . import _lib as L
 from .graphs import Graph
 
 _ALG = {"greedy": 0, "left": 1}
-_PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16}
+_PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16, "tf32x3": L.PREC_TF32X3}
 
 
 class Context:

@@ -94,3 +94,38 @@ def test_bf16_split_tensor_core_gemm():
     z = contract_norm_network(g, t, precision="bf16")
     zr = C.contract_norm(g, t.astype(np.float64))
     assert abs(z - zr) <= 1e-4 * abs(zr)
+
+
+def test_tf32_split_tensor_core_gemm_has_fp32_accuracy():
+    """TF32 hi/lo operands (3 kind::tf32 MMAs per product, partial sums promoted to FP32
+    registers after every K = 64 tile).  One pairwise step is as accurate as FP32 arithmetic:
+    within 4x the FP32 CUDA-core GEMM's error (plus 2e-7) on small and large shapes and
+    magnitudes down to 1e-18.  Measured on a GB300: 300 x 1031 x 130 tf32x3 6.7e-7, FP32 CUDA
+    cores 1.5e-6, BF16 split 4.9e-6 (without the per-tile promotion the tensor core's own
+    sum over K = 1031 gave 7.8e-6); 4 x 4 x 4 1.4e-7 vs 4.9e-8.  Chained steps: the tensor
+    core's sums within a tile are not rounded like FP32 additions and their errors add up over
+    a contraction's steps -- 3.6e-6 on the 32 steps of a 4x4 D=2 norm network against
+    3.6e-8 for FP32 CUDA cores -- so that case is bounded at 1e-5, ten times below the BF16
+    split bound of 1e-4."""
+    rng = np.random.default_rng(10)
+    for (m, k, n), scale in [((300, 1031, 130), 1.0), ((4, 4, 4), 1.0), ((16, 8, 16), 1e-10),
+                             ((64, 64, 64), 1e-18), ((200, 300, 100), 1.0)]:
+        A = (rng.standard_normal((m, k)) * scale).astype(np.float32)
+        B = (rng.standard_normal((k, n)) * scale).astype(np.float32)
+        ref = A.astype(np.float64) @ B.astype(np.float64)
+        top = np.max(np.abs(ref))
+        out, lab = contract_network([A, B], [["m", "k"], ["k", "n"]], precision="tf32x3")
+        fp32, _ = contract_network([A, B], [["m", "k"], ["k", "n"]])
+        err, err32 = (float(np.max(np.abs(x - ref))) / top for x in (out, fp32))
+        print(f"gemm {m}x{k}x{n} (scale {scale:g}) vs FP64: tf32x3 {err:.2e}, fp32 CUDA cores {err32:.2e}")
+        assert lab == ["m", "n"]
+        assert err <= 4 * err32 + 2e-7 and err <= 1e-6
+    # a norm network in FP32 through the tensor cores (32 chained steps)
+    g = G.square_lattice(4, 4, 2, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float32, G.peps_scale(g))
+    z = contract_norm_network(g, t, precision="tf32x3")
+    z32 = contract_norm_network(g, t)
+    zr = C.contract_norm(g, t.astype(np.float64))
+    e, e32 = abs(z - zr) / abs(zr), abs(z32 - zr) / abs(zr)
+    print(f"4x4 D=2 norm network (every step stored in FP32): tf32x3 {e:.2e}, fp32 CUDA cores {e32:.2e}")
+    assert e <= 1e-5
