@@ -33,6 +33,35 @@ def shard_networks(sizes, rank: int, world: int):
     return int(bounds[rank]), int(bounds[rank + 1])
 
 
+def shard_batch(graphs, rank: int, world: int):
+    """This rank's share of a batch of independent networks: (lo, hi, batched graph of
+    graphs[lo:hi]), the split balanced by vertex count (shard_networks)."""
+    from .graphs import batched
+    lo, hi = shard_networks([g.nv for g in graphs], rank, world)
+    return lo, hi, (batched(graphs[lo:hi]) if hi > lo else None)
+
+
+def solve_shard(graphs, tensors, rank: int, world: int, *, maxiter: int, device: int = 0, dtype=None):
+    """Solve this rank's networks on its GPU: ``tensors[k]`` is network k's packed site
+    tensors.  Runs `maxiter` parallel sweeps from the normalised identity on the batched
+    shard (one BPEngine, every network of the shard in each sweep launch) and returns
+    ({network index: Bethe log-norm}, device ms of the sweeps, message updates done)."""
+    from .engine import BPEngine
+    lo, hi, g = shard_batch(graphs, rank, world)
+    if g is None:
+        return {}, 0.0, 0
+    t = np.concatenate([np.asarray(tensors[k]) for k in range(lo, hi)])
+    if dtype is not None:
+        t = t.astype(dtype)
+    with BPEngine(g, device=device) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        r = e.run(maxiter=maxiter)
+        logz = e.bethe_free_energy(None)
+    vals = logz if isinstance(logz, list) else [logz]
+    return {lo + i: v for i, v in enumerate(vals)}, r.device_ms, maxiter * g.nslots
+
+
 def _tensor(x, device):
     import torch
     return torch.tensor([float(x)], dtype=torch.float64, device=device)
@@ -57,13 +86,13 @@ def sum_over_ranks(x: float, group=None, device="cpu") -> float:
 
 
 def gather_logz(local: dict, n_total: int, group=None, device="cpu"):
-    """Per-network log-norms from every rank into one array (rank-local dict {net: value});
-    networks no rank reports stay NaN."""
+    """Per-network log-norms from every rank into one array (rank-local dict {net: value},
+    real part for complex log-norms); networks no rank reports stay NaN."""
     import torch
     import torch.distributed as dist
     buf = torch.full((n_total,), float("nan"), dtype=torch.float64, device=device)
     for k, v in local.items():
-        buf[k] = float(v)
+        buf[k] = float(np.real(v))
     if dist.is_available() and dist.is_initialized():
         # NaN-aware merge: every entry is finite on exactly one rank
         mask = torch.isnan(buf)
