@@ -577,6 +577,46 @@ def bench_batched(device, pg=None, rank=0, world=1, steps=3):
             "logz_finite": bool(np.all(np.isfinite(gathered)))}
 
 
+def run_case(name, device=0):
+    """Small runs of one kernel family each, for ncu captures (profiles/*.md give the
+    commands): d8 = FP32 32x32 D=8 sweeps (sweep_d8_kernel); mixed = the 30-sweep mixed solve
+    (bp_tc_kernel, tc_image_kernel); grad = the 12x12 D=6 FP32 gradient (bp2_dual_kernel,
+    adj_update_kernel); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
+    contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel)."""
+    from itn_gb300 import BPEngine
+    from itn_gb300 import graphs as G
+    if name in ("d8", "mixed"):
+        g, t = workload()
+        with BPEngine(g, device=device) as e:
+            e.set_tensors(t.astype(np.float32))
+            for _ in range(2):
+                e.init_messages()
+                r = e.run(maxiter=4) if name == "d8" else e.run(maxiter=SWEEPS, precision="bf16",
+                                                                split_sweeps=SPLIT_SWEEPS)
+            print(name, "device ms", r.device_ms)
+    elif name == "grad":
+        g = G.square_lattice(12, 12, 6, periodic=False, phys=2)
+        t = G.random_tensors(g, np.random.default_rng(5), np.float64, G.peps_scale(g)).astype(np.float32)
+        with BPEngine(g, device=device) as e:
+            e.set_tensors(t)
+            e.init_messages()
+            e.run(maxiter=200, tol=1e-12)
+            print("grad", e.grad(adjoint=True, tol=1e-6)[1])
+    elif name == "gate":
+        print("gate", bench_apply_layer(device)["device_ms"])
+    elif name == "contract":
+        from itn_gb300.contract import contract_network
+        rng = np.random.default_rng(3)
+        A = rng.standard_normal((2048, 2048)).astype(np.float32)
+        B = rng.standard_normal((2048, 2048)).astype(np.float32)
+        for prec in ("native", "bf16", "tf32x3"):
+            _, _, ms = contract_network([A, B], [["m", "k"], ["k", "n"]], precision=prec, return_time=True)
+            print("contract", prec, "device ms", ms)
+    else:
+        raise SystemExit(f"unknown case {name}")
+    return 0
+
+
 def bench_16x16(device):
     """16x16 open PEPS, d=2, D=4, N(0,1)/sqrt(d D^4): 50 parallel sweeps or tol 1e-10, FP32
     and FP64; plus the BP error of a 6x6 D=3 network against its exact contraction."""
@@ -687,6 +727,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract"],
+                    help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
                     help="skip the secondary configurations (gradient, batched, 16x16, exact 6x6)")
@@ -697,6 +739,8 @@ def main():
         return run_reference(args)
     import __graft_entry__
     __graft_entry__.build()
+    if args.case:
+        return run_case(args.case)
     return run_gpu(args)
 
 

@@ -27,6 +27,7 @@
 #include "itn_tc.h"
 #include "itn_contract.h"
 #include "itn_apply.h"
+#include <nvtx3/nvToolsExt.h>
 
 using namespace itn;
 
@@ -48,6 +49,16 @@ constexpr int kSmallMinItemsPerSm = 16;
 // Device allocations that itn_inject_fault(ITN_FAULT_ALLOC) has told the calling thread to
 // fail (a host-side stand-in for running out of device memory).
 thread_local int64_t t_fail_allocs = 0;
+
+// NVTX range for the lifetime of a scope: every C entry point opens one named after itself,
+// and a solve opens one per chunk of sweeps (tools such as Nsight Systems show them; without
+// a tool attached the calls return at once).
+struct NvtxScope {
+  explicit NvtxScope(const char* name) { nvtxRangePushA(name); }
+  ~NvtxScope() { nvtxRangePop(); }
+  NvtxScope(const NvtxScope&) = delete;
+  NvtxScope& operator=(const NvtxScope&) = delete;
+};
 
 struct DevBuf {
   void* p = nullptr;
@@ -1295,6 +1306,9 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
       c->graph_launches[key] = rec_launches;
     }
     if (o->precision != ITN_PREC_NATIVE) CK(tc_note_launches(c->tc, 2, c->stream));
+    char rng[96];
+    snprintf(rng, sizeof(rng), "bp sweeps %lld-%lld", (long long)issued + 1, (long long)(issued + n));
+    NvtxScope nvtx_chunk(rng);
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(cudaGraphLaunch(exec, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
@@ -1358,10 +1372,12 @@ int bp_run_finish(itn_ctx* c, itn_bp_result* res) {
 extern "C" {
 
 int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
+  NvtxScope nvtx_("itn_bp_run");
   return bp_run_impl(c, o, res, false);
 }
 
 int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
+  NvtxScope nvtx_("itn_message_update");
   if (int r = check_ready(c, true)) return r;
   if (slot < 0 || slot >= c->nslots) return fail(c, ITN_ERR_ARG, "slot out of range");
   if (int r = ensure_device(c)) return r;
@@ -1379,6 +1395,7 @@ int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
 }
 
 int32_t itn_iterate_diff(itn_ctx* c, int32_t dtype, const void* m1, const void* m2, double* out) {
+  NvtxScope nvtx_("itn_iterate_diff");
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "no network uploaded");
   if (!m1 || !m2 || !out) return fail(c, ITN_ERR_ARG, "null pointer");
@@ -1662,6 +1679,7 @@ int grad_unrolled(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_resul
 extern "C" {
 
 int32_t itn_sweep_vjp(itn_ctx* c, int32_t normalized, const void* cot_out, void* cot_in) {
+  NvtxScope nvtx_("itn_sweep_vjp");
   if (int r = check_ready(c, true)) return r;
   if (!cot_out || !cot_in) return fail(c, ITN_ERR_ARG, "null cotangent pointer");
   if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
@@ -1681,6 +1699,7 @@ int32_t itn_sweep_vjp(itn_ctx* c, int32_t normalized, const void* cot_out, void*
 }
 
 int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_result* res) {
+  NvtxScope nvtx_("itn_bp_grad");
   if (int r = check_ready(c, true)) return r;
   if (!grad) return fail(c, ITN_ERR_ARG, "null gradient pointer");
   if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
@@ -1820,6 +1839,7 @@ extern "C" {
 
 int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* logze,
                        double* totals, int32_t* flags) {
+  NvtxScope nvtx_("itn_logscalars");
   if (int r = check_ready(c, true)) return r;
   if (int r = ensure_device(c)) return r;
   const size_t es = dtype_size(c->dtype);
@@ -1853,6 +1873,7 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
 int32_t itn_bp_solve(itn_ctx* c, int32_t dtype, const void* tensors, const void* messages_in,
                      const itn_bp_opts* o, itn_bp_result* res, void* messages_out, double* totals,
                      int32_t* flags) {
+  NvtxScope nvtx_("itn_bp_solve");
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
   if (!o) return fail(c, ITN_ERR_ARG, "null options");
@@ -1966,6 +1987,7 @@ int32_t itn_apply_gates(itn_ctx* c, int32_t dtype, int64_t n_gates, const itn_ga
                         int64_t n_op_elems, int32_t max_rank, double cutoff, int32_t normalize, void* out_sites,
                         int64_t out_capacity, double* out_s, int64_t s_capacity, int32_t* out_bond,
                         double* device_ms) {
+  NvtxScope nvtx_("itn_apply_gates");
   if (!c) return ITN_ERR_ARG;
   if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
   if (n_gates < 0) return fail(c, ITN_ERR_ARG, "negative gate count");
@@ -2101,6 +2123,7 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
                              const int64_t* dims, const void* const* tensors, int32_t alg, const int32_t* steps_in,
                              int32_t precision, void* out, int64_t out_capacity, int32_t* out_rank,
                              int64_t* out_labels, int64_t* out_dims, double* device_ms) {
+  NvtxScope nvtx_("itn_contract_network");
   if (!c) return ITN_ERR_ARG;
   if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
   if (precision != ITN_PREC_NATIVE &&
