@@ -582,7 +582,8 @@ def run_case(name, device=0):
     commands): d8 = FP32 32x32 D=8 sweeps (sweep_d8_kernel); mixed = the 30-sweep mixed solve
     (bp_tc_kernel, tc_image_kernel); grad = the 12x12 D=6 FP32 gradient (bp2_dual_kernel,
     adj_update_kernel); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
-    contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel)."""
+    contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel); batched = the
+    256-network complex64 batch (sweep_z3_kernel)."""
     from itn_gb300 import BPEngine
     from itn_gb300 import graphs as G
     if name in ("d8", "mixed"):
@@ -604,6 +605,8 @@ def run_case(name, device=0):
             print("grad", e.grad(adjoint=True, tol=1e-6)[1])
     elif name == "gate":
         print("gate", bench_apply_layer(device)["device_ms"])
+    elif name == "batched":
+        print("batched", bench_batched(device))
     elif name == "contract":
         from itn_gb300.contract import contract_network
         rng = np.random.default_rng(3)
@@ -727,7 +730,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
-    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract"],
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",

@@ -27,8 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
-SOURCES = ["itn_api.cu", "bp_generic.cu", "bp_tc.cu", "noalloc.cu", "contract.cu", "apply_gates.cu"]
-HEADERS = ["itn_common.cuh", "itn_internal.h", "itn_tc.h", "tc_ptx.cuh", "itn_conv.cuh", "itn_contract.h", "itn_apply.h"]
+SOURCES = ["itn_api.cu", "bp_generic.cu", "bp_tc.cu", "bp_z3.cu", "noalloc.cu", "contract.cu", "apply_gates.cu"]
+HEADERS = ["itn_common.cuh", "itn_internal.h", "itn_tc.h", "tc_ptx.cuh", "itn_conv.cuh", "itn_contract.h", "itn_apply.h", "itn_z3.h"]
 
 
 def nvcc() -> str:

@@ -27,6 +27,7 @@
 #include "itn_tc.h"
 #include "itn_contract.h"
 #include "itn_apply.h"
+#include "itn_z3.h"
 #include <nvtx3/nvToolsExt.h>
 
 using namespace itn;
@@ -183,6 +184,14 @@ struct itn_ctx {
   int64_t max_tensor = 1;
   std::vector<int> eslots;  // undirected edges: slot < rev[slot]
   bool scal_d8 = false;     // every vertex: two layers, d = 2, four legs of dimension 8
+  // every vertex: two layers, three legs of dimension <= 8, at most 1024 tensor entries
+  // (the grouped sweep of bp_z3.cu); items_z3 sorted by tensor size, largest first
+  bool z3 = false;
+  std::vector<int> items_z3;
+  std::vector<double> z3_work;      // per item: entries x (D0 + D1 + D2), the sweep's cost share
+  DevBuf d_items_z3;
+  std::array<int, 4> z3_budget{{0, 0, 0, 0}};  // autotuned shared memory per CTA (bytes), per dtype
+  std::array<int, 4> z3_mult{{0, 0, 0, 0}};    // autotuned CTAs per resident CTA slot
   // Parallel-sweep items in size classes (items_par is sorted by tensor size, largest
   // first), in launch order: contiguous item ranges with their own staging limits and CTA
   // size; a single class uses the whole network's limits and the tuned CTA size.
@@ -737,6 +746,26 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
     for (int64_t q = c->off[u]; q < c->off[u + 1] && c->scal_d8; ++q)
       if (c->bond[q] != 8) c->scal_d8 = false;
   }
+  c->z3 = layers == 2 && nv > 0;
+  c->items_z3.clear();
+  c->z3_work.clear();
+  for (int64_t u = 0; u < nv && c->z3; ++u) {
+    if (c->off[u + 1] - c->off[u] != 3 || c->toff[u + 1] - c->toff[u] > kZ3MaxTensor) c->z3 = false;
+    for (int64_t q = c->off[u]; q < c->off[u + 1] && c->z3; ++q)
+      if (c->bond[q] > kZ3MaxBond) c->z3 = false;
+  }
+  if (c->z3) {
+    c->items_z3.resize(nv);
+    for (int64_t u = 0; u < nv; ++u) c->items_z3[u] = (int)u;
+    std::stable_sort(c->items_z3.begin(), c->items_z3.end(), [&](int a, int b) {
+      return c->toff[a + 1] - c->toff[a] > c->toff[b + 1] - c->toff[b];
+    });
+    for (int u : c->items_z3)
+      c->z3_work.push_back((double)(c->toff[u + 1] - c->toff[u]) *
+                           (c->bond[c->off[u]] + c->bond[c->off[u] + 1] + c->bond[c->off[u] + 2]));
+  }
+  c->z3_budget = {0, 0, 0, 0};
+  c->z3_mult = {0, 0, 0, 0};
   c->tuned_block.assign(4, 0);
   if (c->prog_host.empty()) c->prog_host.push_back(0);
   c->prog_dirty = true;
@@ -751,7 +780,8 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       (r = upload_vec(c, c->d_net_eoff, eoff, c->stream)) || (r = upload_vec(c, c->d_net_elist, elist, c->stream)) ||
       (r = upload_vec(c, c->d_items_par, c->items_par, c->stream)) ||
       (r = upload_vec(c, c->d_items_scal, c->items_scal, c->stream)) ||
-      (r = upload_vec(c, c->d_items_dump, c->items_dump, c->stream)) || (r = sync_programs(c)))
+      (r = upload_vec(c, c->d_items_dump, c->items_dump, c->stream)) ||
+      (r = upload_vec(c, c->d_items_z3, c->items_z3, c->stream)) || (r = sync_programs(c)))
     return r;
   {
     std::vector<int> epos(ns, -1);
@@ -1034,6 +1064,117 @@ int autotune_sweep(itn_ctx* c) {
 // 8 run on the register-blocked kernel (sweep_d8_kernel) instead of the interpreter.
 bool use_sweep_d8(const itn_ctx* c) { return c->scal_d8 && c->dtype == ITN_F32; }
 
+// Networks whose vertices all have three legs run the grouped sweep (bp_z3.cu).
+bool use_sweep_z3(const itn_ctx* c) { return c->z3 && !use_sweep_d8(c); }
+
+// Launch shape of the grouped sweep for a shared-memory budget per CTA and a CTA multiplier:
+// size classes by the largest tensor (at most 1024, 512, ... entries), warps per CTA of a
+// class = slices of its largest vertex that fit the budget (at most 8), CTAs shared among
+// the classes in proportion to their work, the total `mult` x the CTAs resident at once.
+int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult, const void* in, void* out,
+            int normalize, double* slot_diff, ConvState* cv) {
+  memset(&a, 0, sizeof(a));
+  a.off = c->d_off.as<int>();
+  a.rev = c->d_rev.as<int>();
+  a.bond = c->d_bond.as<int>();
+  a.toff = c->d_toff.as<long long>();
+  a.moff = c->d_moff.as<long long>();
+  a.tens = c->d_tens.p;
+  a.msg_in = in;
+  a.msg_out = out;
+  a.items = c->d_items_z3.as<int>();
+  a.normalize = normalize;
+  a.slot_diff = slot_diff;
+  a.conv = cv;
+  const size_t es = dtype_size(c->dtype);
+  const int n = (int)c->items_z3.size();
+  auto size_of = [&](int i) { const int u = c->items_z3[i]; return (int)(c->toff[u + 1] - c->toff[u]); };
+  // classes: items whose tensors have (limit / 2, limit] entries, limit = 1024, 512, ...
+  std::vector<std::pair<int, int>> ranges;
+  int i = 0, limit = kZ3MaxTensor;
+  while (i < n) {
+    while (limit / 2 >= size_of(i) && limit > 8 && (int)ranges.size() + 1 < kZ3MaxClasses) limit /= 2;
+    int j = i;
+    while (j < n && (size_of(j) > limit / 2 || limit <= 8 || (int)ranges.size() + 1 == kZ3MaxClasses)) ++j;
+    ranges.push_back({i, j});
+    i = j;
+  }
+  smem = (size_t)budget;
+  for (auto& rg : ranges) smem = std::max(smem, (size_t)(3 * size_of(rg.first) + 448) * es);
+  smem = std::min(smem, kZ3MaxSmem);
+  const int per_sm = std::max(1, z3_blocks_per_sm(c->dtype, smem));
+  const int total = std::max(1, c->sm_count * per_sm * std::max(mult, 1));
+  double wsum = 0;
+  for (double w : c->z3_work) wsum += w;
+  int start = 0;
+  a.n_classes = (int)ranges.size();
+  for (size_t k = 0; k < ranges.size(); ++k) {
+    Z3Class& cl = a.cls[k];
+    cl.first = ranges[k].first;
+    cl.count = ranges[k].second - ranges[k].first;
+    cl.nmax = size_of(cl.first);
+    cl.slice = 3 * cl.nmax + 448;
+    // vertices in flight per CTA: as many slices as the budget holds (at most 8, a power of
+    // two); the CTA's 8 warps are shared among them (wpi warps per vertex)
+    const int fit = (int)std::max<size_t>(1, std::min<size_t>(kZ3Threads / 32, smem / ((size_t)cl.slice * es)));
+    cl.groups = 1;
+    while (cl.groups * 2 <= fit) cl.groups *= 2;
+    cl.wpi = (kZ3Threads / 32) / cl.groups;
+    double w = 0;
+    for (int q = cl.first; q < cl.first + cl.count; ++q) w += c->z3_work[q];
+    const int need = (cl.count + cl.groups - 1) / cl.groups;
+    cl.ctas = std::max(1, std::min(need, (int)std::lround(total * w / std::max(wsum, 1.0))));
+    cl.cta_start = start;
+    start += cl.ctas;
+  }
+  grid = start;
+  return ITN_OK;
+}
+
+// Autotuner of the grouped sweep: time one sweep per (shared-memory budget, CTA multiplier)
+// candidate on the current messages (best of three after a warm-up launch) and keep the
+// fastest shape for this dtype.
+int autotune_z3(itn_ctx* c) {
+  const int dt = c->dtype;
+  if (c->z3_budget[dt] > 0) return ITN_OK;
+  const int budgets[4] = {24 << 10, 48 << 10, 96 << 10, 200 << 10};
+  const int mults[2] = {1, 2};
+  float best = 1e30f;
+  int bb = budgets[1], bm = 1;
+  for (int budget : budgets)
+    for (int mult : mults) {
+      Z3Args a;
+      int grid = 0;
+      size_t smem = 0;
+      if (int r = plan_z3(c, a, grid, smem, budget, mult, c->d_msg[c->cur].p, c->d_msg[c->cur ^ 1].p, 1, nullptr,
+                          nullptr))
+        return r;
+      float ms = 1e30f;
+      for (int rep = 0; rep < 4; ++rep) {
+        float t = 0.f;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        CK(launch_sweep_z3(dt, a, grid, smem, c->stream));
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+        if (rep > 0) ms = std::min(ms, t);
+      }
+      if (getenv("ITN_DEBUG"))
+        fprintf(stderr, "[itn] z3 autotune: budget %d KB mult %d grid %d smem %zu: %.4f ms\n", budget >> 10, mult,
+                grid, smem, ms);
+      if (ms < best) {
+        best = ms;
+        bb = budget;
+        bm = mult;
+      }
+    }
+  c->z3_budget[dt] = bb;
+  c->z3_mult[dt] = bm;
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+  return ITN_OK;
+}
+
 int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   const bool use_tol = o->tol >= 0;
   const size_t nc = c->par_classes.size();
@@ -1110,6 +1251,14 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       tr.conv = conv(c);
       cudaError_t e = tc_sweep(c->tc, tr, c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core sweep");
+    } else if (use_sweep_z3(c)) {
+      Z3Args za;
+      int grid = 0;
+      size_t smem = 0;
+      if (int r = plan_z3(c, za, grid, smem, c->z3_budget[c->dtype], c->z3_mult[c->dtype], c->d_msg[in].p,
+                          c->d_msg[out].p, o->normalize, use_tol ? c->d_slot_diff.as<double>() : nullptr, conv(c)))
+        return r;
+      CK(launch_sweep_z3(c->dtype, za, grid, smem, c->stream));
     } else if (use_sweep_d8(c)) {
       CK(launch_sweep_d8(c->d_rev.as<int>(), c->d_tens.as<float>(), c->d_msg[in].as<float>(),
                          c->d_msg[out].as<float>(), (int)c->nv, o->normalize,
@@ -1247,7 +1396,9 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   const bool use_tol = o->tol >= 0;
   ParPlan pplan;
   std::vector<SeqLaunch> slaunch;
-  if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE && !use_sweep_d8(c)) {
+  if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE && use_sweep_z3(c)) {
+    if (int r = autotune_z3(c)) return r;
+  } else if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE && !use_sweep_d8(c)) {
     if (int r = autotune_sweep(c)) return r;
     if (int r = make_par_plan(c, o, pplan)) return r;
   } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {
