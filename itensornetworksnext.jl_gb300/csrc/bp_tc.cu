@@ -17,9 +17,10 @@
 // accumulation is FP32 in TMEM.  The split variant adds the hi*lo and lo*hi products
 // (x = hi + lo, both BF16) for ~16 significant bits.
 //
-// Per CTA (128 threads = 4 warps, one TMEM lane quarter each): one vertex at a time;
-// thread 0 issues the bulk TMA copy of the vertex's pre-tiled BF16 operand image and
-// the MMAs; all threads build the Kronecker operands and run the epilogues.
+// Per group (128 threads = 4 warps, one TMEM lane quarter each): one half-vertex item at a
+// time; thread 0 issues the bulk TMA copy of the vertex's pre-tiled operand image, one
+// elected lane of warp 0 the MMAs; all threads build the Kronecker operands and run the
+// epilogues.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdio.h>
@@ -313,7 +314,12 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   static_assert(tmem_cols_for(GROUPS) <= 512, "at most 512 TMEM columns per CTA");
   extern __shared__ __align__(1024) unsigned char sm_all[];
   constexpr TcSmem L = tc_smem<OP>();
-  const int g = GROUPS > 1 ? (int)(threadIdx.x >> 7) : 0;
+  // The group, the warp and the TMEM base are broadcast from lane 0 so that the compiler can
+  // treat them, and the operand descriptors derived from them, as warp-uniform.  The MMAs of a
+  // GEMM are issued by one elected lane of warp 0 with the whole warp converged; against the
+  // same MMAs issued from a `tid == 0` branch this measured 9% (BF16) to 28% (TF32 hi/lo)
+  // faster per sweep, and it freed the BF16 kernel's spilled registers.
+  const int g = GROUPS > 1 ? __shfl_sync(0xffffffffu, (int)(threadIdx.x >> 7), 0) : 0;
   const uint32_t bar_id = 1 + g;
   unsigned char* sm = sm_all + g * L.stride;
   uint64_t* bar_load = reinterpret_cast<uint64_t*>(sm + L.bars);
@@ -323,12 +329,21 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   float* outs = reinterpret_cast<float*>(sm + L.outs);  // [64] message on the pair's first leg
   float* part = reinterpret_cast<float*>(sm + L.part);  // [4 warps][64] partials, second leg
   unsigned char* reg = sm + L.reg;
-  const int tid = threadIdx.x & (kThreads - 1), warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x & (kThreads - 1), lane = tid & 31;
+  const int warp = __shfl_sync(0xffffffffu, tid >> 5, 0);
   const int n_items = 2 * a.nv;
-  // groups are numbered across CTAs first, so the groups with one item more than the
-  // others are spread over all SMs
+  // Groups are numbered across CTAs first.  Fixed schedule: group gid runs items gid,
+  // gid + ngroups, ... of every sweep.  Round-robin schedule (persistent launches of 4 or
+  // fewer groups per CTA): the work is the sequence of tickets k = t * n_items + item over all
+  // sweeps t of the launch, and group gid runs tickets gid, gid + ngroups, ..., so every group
+  // gets the same number of items (+- 1) over the launch instead of one more than others in
+  // every sweep.  An item waits only for items of lower tickets, and each group runs its
+  // tickets in increasing order, so the lowest unfinished ticket can always proceed.  With 8
+  // groups per SM the fixed schedule measured faster (groups with fewer items leave the SM to
+  // the others), with 4 (BF16 split) the round-robin one (0.59 vs 0.63 ms per 30 sweeps).
   const int gid = g * gridDim.x + blockIdx.x, ngroups = gridDim.x * GROUPS;
   const int nsweeps = PERSIST ? a.nsweeps : 1;
+  constexpr bool rr = PERSIST && GROUPS <= 4;
   const uint32_t epoch = PERSIST ? a.epoch[0] : 0u;
 
   if (threadIdx.x < 32) {
@@ -343,7 +358,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
-  const uint32_t tmem = *taddr_s + (uint32_t)(kTmemCols * g);
+  const uint32_t tmem = __shfl_sync(0xffffffffu, *taddr_s, 0) + (uint32_t)(kTmemCols * g);
   const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
   const uint32_t sbase = ptx::smem_u32(sm);
   const uint32_t Aimg = sbase + L.img, Alo = 2 * O::blk;
@@ -362,19 +377,24 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   const int l0 = tid >> 6, e0 = tid & 63;
   unsigned long long w0 = 0, w1 = 0;
   // the operand image is static: its copy starts before the done flag is read
-  const bool first = gid < n_items;
+  const bool first = gid < (rr ? n_items * nsweeps : n_items);
+  int t = rr ? gid / n_items : 0, item = gid - t * n_items;
   if (first && tid == 0) {
-    issue_image<OP>(sm + L.img, a.image, gid, bar_load);
+    issue_image<OP>(sm + L.img, a.image, item, bar_load);
     ld_pend = true;
   }
   const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
-  if (first && !skip) fetch_in(a, epoch, gid, 0, l0, e0, w0, w1);
-  int t = (first && !skip) ? 0 : nsweeps, item = gid;
+  if (first && !skip) fetch_in(a, epoch, item, t, l0, e0, w0, w1);
+  if (!first || skip) t = nsweeps;
   while (t < nsweeps) {
-    // the item after this one: the next of this group in the sweep, else the first of
-    // the next sweep
+    // this group's next item
     int item2 = item + ngroups, t2 = t;
-    if (item2 >= n_items) {
+    if (rr) {
+      while (item2 >= n_items) {
+        item2 -= n_items;
+        ++t2;
+      }
+    } else if (item2 >= n_items) {
       item2 = gid;
       ++t2;
     }
@@ -437,12 +457,15 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     ptx::fence_proxy_async_smem();
     group_sync(bar_id);
     // 2. first GEMM: rows (s, r) of the image times P^T -> TMEM cols 0..63
-    if (tid == 0) {
+    if (warp == 0) {
       if (!ptx::mbar_wait_bounded(bar_load, ph_load, kMaxPolls)) fail = true;
       else ld_pend = false;
       ptx::tc_fence_after();
-      mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc128, false);
-      ptx::mma_commit(bar_mma);
+      if (ptx::elect_one()) {
+        mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc128, false);
+        ptx::mma_commit(bar_mma);
+      }
+      __syncwarp();
     }
     ph_load ^= 1;
     if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
@@ -484,20 +507,26 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     group_sync(bar_id);
     // 4. second GEMM, Z = image (rows of the other pair, K = (s, this pair)) x XT^T with
     //    M = 64, in two K halves: s = 0 from XT0, then s = 1 from XT1 in the same buffer
-    if (tid == 0) {
+    if (warp == 0) {
       ptx::tc_fence_after();
-      mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc64, false);
-      ptx::mma_commit(bar_mma);
+      if (ptx::elect_one()) {
+        mma_k64<OP>(tmem, Aimg, Aimg + Alo, R, R + O::blk, idesc64, false);
+        ptx::mma_commit(bar_mma);
+      }
+      __syncwarp();
     }
     if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
     ph_mma ^= 1;
     if (warp >= 2) store_xt();
     ptx::fence_proxy_async_smem();
     group_sync(bar_id);
-    if (tid == 0) {
+    if (warp == 0) {
       ptx::tc_fence_after();
-      mma_k64<OP>(tmem, Aimg + O::blk, Aimg + Alo + O::blk, R, R + O::blk, idesc64, true);
-      ptx::mma_commit(bar_mma);
+      if (ptx::elect_one()) {
+        mma_k64<OP>(tmem, Aimg + O::blk, Aimg + Alo + O::blk, R, R + O::blk, idesc64, true);
+        ptx::mma_commit(bar_mma);
+      }
+      __syncwarp();
     }
     if (!ptx::mbar_wait_bounded(bar_mma, ph_mma, kMaxPolls)) fail = mma_lost = true;
     ph_mma ^= 1;

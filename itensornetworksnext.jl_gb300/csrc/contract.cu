@@ -303,7 +303,10 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __res
   // stage s: A tile at s * (A + B), B tile after it
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * (kA + kB));  // load[2], mma
   uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bar + 4);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // the warp index and TMEM base are broadcast from lane 0 so that the compiler treats them as
+  // warp-uniform; warp 0 issues the MMAs from one elected lane (faster than a tid == 0 branch)
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int warp = __shfl_sync(0xffffffffu, tid >> 5, 0);
   const long long mt = blockIdx.x / nt_n, nt = blockIdx.x % nt_n;
   if (warp == 0) {
     ptx::tmem_alloc(taddr_s, 64);
@@ -316,7 +319,7 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __res
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
-  const uint32_t tmem = *taddr_s;
+  const uint32_t tmem = __shfl_sync(0xffffffffu, *taddr_s, 0);
   const uint32_t sb = ptx::smem_u32(sm);
   constexpr uint32_t idesc = MODE == 1 ? ptx::idesc_tf32_f32(128, 64) : ptx::idesc_bf16_f32(128, 64);
   auto load = [&](long long kt, int s) {
@@ -343,27 +346,31 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const unsigned char* __res
   for (long long kt = 0; kt < kt_n; ++kt) {
     const int s = (int)(kt & 1);
     bool mine = true;
-    if (tid == 0) {
+    if (warp == 0) {
       // stage s ^ 1 was last read by the MMAs of tile kt - 1, which completed before the
       // readout below
-      if (kt + 1 < kt_n) {
+      if (lane == 0 && kt + 1 < kt_n) {
         load(kt + 1, s ^ 1);
         ld_pend[s ^ 1] = true;
       }
       mine = ptx::mbar_wait_bounded(bar + s, ph_load[s], kTcPolls);
       if (mine) ld_pend[s] = false;
       ph_load[s] ^= 1;
+      mine = __all_sync(0xffffffffu, mine);  // the elected block below needs the whole warp
       if (mine) {
         ptx::tc_fence_after();
         const uint32_t a = sb + s * (kA + kB), b = a + kA;
+        if (ptx::elect_one()) {
 #pragma unroll
-        for (int j = 0; j < G::ksteps; ++j) {
-          const uint32_t ko = (uint32_t)(2 * j) * 128;  // two core columns per MMA
-          mma(a + ko, b + ko, j > 0 ? 1u : 0u);
-          mma(a + 2 * G::blk + ko, b + ko, 1);
-          mma(a + ko, b + G::blk + ko, 1);
+          for (int j = 0; j < G::ksteps; ++j) {
+            const uint32_t ko = (uint32_t)(2 * j) * 128;  // two core columns per MMA
+            mma(a + ko, b + ko, j > 0 ? 1u : 0u);
+            mma(a + 2 * G::blk + ko, b + ko, 1);
+            mma(a + ko, b + G::blk + ko, 1);
+          }
+          ptx::mma_commit(bar + 2);
         }
-        ptx::mma_commit(bar + 2);
+        __syncwarp();
       }
     }
     if (!__syncthreads_and(mine)) {
