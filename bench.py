@@ -583,7 +583,8 @@ def run_case(name, device=0):
     (bp_tc_kernel, tc_image_kernel); grad = the 12x12 D=6 FP32 gradient (bp2_dual_kernel,
     adj_update_kernel); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
     contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel); batched = the
-    256-network complex64 batch (sweep_z3_kernel)."""
+    256-network complex64 batch (sweep_z3_kernel); exact6 = the exact FP64 contraction of the
+    6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>)."""
     from itn_gb300 import BPEngine
     from itn_gb300 import graphs as G
     if name in ("d8", "mixed"):
@@ -616,6 +617,13 @@ def run_case(name, device=0):
             for _ in range(2):  # the first call of a precision includes one-time set-up (self-test, module load)
                 _, _, ms = contract_network([A, B], [["m", "k"], ["k", "n"]], precision=prec, return_time=True)
             print("contract", prec, "device ms", ms)
+    elif name == "exact6":
+        from itn_gb300.contract import contract_network, norm_network_tensors
+        g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
+        t6 = G.random_tensors(g6, np.random.default_rng(63), np.float64, G.peps_scale(g6))
+        ts, ls = norm_network_tensors(g6, t6)
+        z, _, ms = contract_network(ts, ls, return_time=True)
+        print("exact6 log z", float(np.log(z[()])), "device ms", ms)
     else:
         raise SystemExit(f"unknown case {name}")
     return 0
@@ -731,7 +739,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
-    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched"],
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",

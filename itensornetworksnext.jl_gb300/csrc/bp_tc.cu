@@ -96,6 +96,26 @@ __device__ __forceinline__ void split_bf16(float x, float& hi, float& lo) {
   lo = x - hi;
 }
 
+
+// Row r (8 floats) of an 8 x 8 FP32 matrix in shared memory (16-byte aligned), as two 16-byte
+// accesses; rows 4..7 take their second half first, so eight threads reading rows 0..7 hit
+// eight different groups of four banks in each access.
+__device__ __forceinline__ void row8(const float* m, int r, float (&v)[8]) {
+  const int sw = (r >> 2) & 1;
+  const float4* p = reinterpret_cast<const float4*>(m + 8 * r);
+  const float4 x = p[sw], y = p[sw ^ 1];
+  const float4 lo = sw ? y : x, hi = sw ? x : y;
+  v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
+  v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
+}
+__device__ __forceinline__ void store_row8(float* m, int r, const float (&v)[8]) {
+  const int sw = (r >> 2) & 1;
+  float4* p = reinterpret_cast<float4*>(m + 8 * r);
+  const float4 lo = make_float4(v[0], v[1], v[2], v[3]), hi = make_float4(v[4], v[5], v[6], v[7]);
+  p[sw] = sw ? hi : lo;
+  p[sw ^ 1] = sw ? lo : hi;
+}
+
 struct TcSmem {
   // offsets in bytes from a group's shared-memory slice; stride = slice size
   uint32_t img, reg, msg, outs, part, bars, taddr, total, stride;
@@ -413,14 +433,14 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     //    128-byte core, so the 16-byte stores are free of bank conflicts
     {
       const int bi = tid & 7, bo = (tid >> 3) & 7, kq = (tid >> 6) * 4;
-      const float* ma = msg + pa * 64;
       float mb[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) mb[k] = msg[pb * 64 + bi * 8 + k];
+      row8(msg + pb * 64, bi, mb);
+      const float4 wa = *reinterpret_cast<const float4*>(msg + pa * 64 + bo * 8 + kq);
+      const float wj[4] = {wa.x, wa.y, wa.z, wa.w};
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int ko = kq + j;
-        const float w = ma[bo * 8 + ko];
+        const float w = wj[j];
         const uint32_t off = op_off<OP>(bo * 8 + bi, ko * 8);
         if constexpr (O::tf32) {
           // 8 K-entries = two 16-byte core rows (and the same in the lo plane when split:
@@ -546,16 +566,16 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     {
       const int hf = lane >> 4, bh = 2 * warp + ((lane >> 3) & 1), bl = lane & 7;
       float th[4], tl[8], ml[8], mh[4];
+      row8(msg + Lg * 64, bl, ml);
+      const float4 hv = *reinterpret_cast<const float4*>(msg + H * 64 + bh * 8 + 4 * hf);
+      mh[0] = hv.x;
+      mh[1] = hv.y;
+      mh[2] = hv.z;
+      mh[3] = hv.w;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        tl[k] = 0.f;
-        ml[k] = msg[Lg * 64 + bl * 8 + k];
-      }
+      for (int k = 0; k < 8; ++k) tl[k] = 0.f;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        th[q] = 0.f;
-        mh[q] = msg[H * 64 + bh * 8 + 4 * hf + q];
-      }
+      for (int q = 0; q < 4; ++q) th[q] = 0.f;
 #pragma unroll
       for (int qc = 0; qc < 2; ++qc) {  // columns 16 qc + j (+ 32 hf): kh = 4 hf + 2 qc + (j >> 3)
         float z[16];
@@ -581,14 +601,8 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
         tl[k] += __shfl_xor_sync(0xffffffffu, tl[k], 16);
         tl[k] += __shfl_xor_sync(0xffffffffu, tl[k], 8);
       }
-      if (bl == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) outs[bh * 8 + 4 * hf + q] = th[q];
-      }
-      if (lane < 8) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) part[warp * 64 + bl * 8 + k] = tl[k];
-      }
+      if (bl == 0) *reinterpret_cast<float4*>(outs + bh * 8 + 4 * hf) = make_float4(th[0], th[1], th[2], th[3]);
+      if (lane < 8) store_row8(part + warp * 64, bl, tl);
     }
     ptx::tc_fence_before();
     // one consensus per item on the bounded waits, folded into the barrier the final
