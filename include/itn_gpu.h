@@ -143,6 +143,18 @@ int32_t itn_bp_solve(itn_ctx *ctx, int32_t dtype, const void *tensors, const voi
                      const itn_bp_opts *opts, itn_bp_result *result, void *messages_out,
                      double *totals, int32_t *flags);
 
+/* itn_bp_solve in two halves, for callers that solve many networks back to back (a serving
+ * loop): itn_bp_solve_submit queues the uploads, the solve, the log-norm (when `logz` is
+ * non-zero) and the download of the final messages into messages_out, and returns without
+ * waiting (a solve with a tolerance still waits for its convergence checks);
+ * itn_bp_solve_wait waits for that work and returns the result, totals and flags as
+ * itn_bp_solve does.  Between the two the host buffers must stay valid and unchanged, and every
+ * other call on the context returns ITN_ERR_STATE.  Each context has its own stream, so with two
+ * contexts on one device the uploads of one network overlap the solve of the other. */
+int32_t itn_bp_solve_submit(itn_ctx *ctx, int32_t dtype, const void *tensors, const void *messages_in,
+                            const itn_bp_opts *opts, void *messages_out, int32_t logz);
+int32_t itn_bp_solve_wait(itn_ctx *ctx, itn_bp_result *result, double *totals, int32_t *flags);
+
 /* message_update!(SimpleMessageUpdate(normalize), cache, factors, edge)
  * (src/beliefpropagation/beliefpropagation.jl:242-257) for the directed slot. */
 int32_t itn_message_update(itn_ctx *ctx, int64_t slot, int32_t normalize);

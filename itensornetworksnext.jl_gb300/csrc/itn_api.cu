@@ -243,6 +243,13 @@ struct itn_ctx {
     int launches = 0;
     float ms_before = 0.f;
   } pending;
+  // a solve queued by itn_bp_solve_submit and not yet completed by itn_bp_solve_wait: it owns
+  // the stream's results and the pinned staging until then
+  struct {
+    bool active = false;
+    bool logz = false;
+    itn_bp_result res{};  // the result of a solve that completed inside the submit call
+  } submitted;
 
   // convergence state (device): dmax, nan, done, at, iters, delta, counter
   DevBuf d_slot_diff, d_state;
@@ -401,6 +408,13 @@ int plan_generic(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items,
 
 ConvState* conv(itn_ctx* c) { return c->d_state.as<ConvState>(); }
 
+// Calls that use a context's stream or staging are refused while a submitted solve is pending.
+int not_busy(itn_ctx* c) {
+  if (c && c->submitted.active)
+    return fail(c, ITN_ERR_STATE, "a solve submitted with itn_bp_solve_submit is pending: call itn_bp_solve_wait first");
+  return ITN_OK;
+}
+
 int check_ready(itn_ctx* c, bool need_msgs) {
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "no network uploaded");
@@ -484,6 +498,7 @@ int32_t itn_destroy(itn_ctx* c) {
 const char* itn_last_error(const itn_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 int32_t itn_inject_fault(itn_ctx* c, int32_t kind, int64_t value) {
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   switch (kind) {
     case ITN_FAULT_WAIT_NS:
@@ -518,6 +533,7 @@ int32_t itn_synchronize(itn_ctx* c) {
 int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const int64_t* csr_nbr,
                          const int32_t* bond, const int64_t* rev, const int32_t* phys,
                          int32_t layers, const int32_t* net_id) {
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (int r = ensure_device(c)) return r;
   if (nv < 0 || nv > (1LL << 30)) return fail(c, ITN_ERR_ARG, "nv out of range");
@@ -829,6 +845,7 @@ static int set_dtype(itn_ctx* c, int32_t dtype) {
 }
 
 int32_t itn_tensors_upload(itn_ctx* c, int32_t dtype, const void* packed) {
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
   if (!packed && c->toff[c->nv] > 0) return fail(c, ITN_ERR_ARG, "null tensor pointer");
@@ -850,6 +867,7 @@ int32_t itn_tensors_upload(itn_ctx* c, int32_t dtype, const void* packed) {
 
 int32_t itn_tensors_upload_strided(itn_ctx* c, int32_t dtype, const void* const* site_ptrs,
                                    const int64_t* strides) {
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
   if (!site_ptrs || !strides) return fail(c, ITN_ERR_ARG, "null pointer");
@@ -900,6 +918,7 @@ int32_t itn_tensors_upload_strided(itn_ctx* c, int32_t dtype, const void* const*
 }
 
 int32_t itn_tensors_download(itn_ctx* c, int32_t dtype, void* packed) {
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, false)) return r;
   if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "dtype differs from the uploaded tensors");
   const size_t bytes = (size_t)c->toff[c->nv] * dtype_size(dtype);
@@ -909,6 +928,7 @@ int32_t itn_tensors_download(itn_ctx* c, int32_t dtype, void* packed) {
 }
 
 int32_t itn_messages_upload(itn_ctx* c, int32_t dtype, const void* packed) {
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, false)) return r;
   if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "message dtype must equal the tensor dtype");
   const size_t bytes = (size_t)c->moff[c->nslots] * dtype_size(dtype);
@@ -921,6 +941,7 @@ int32_t itn_messages_upload(itn_ctx* c, int32_t dtype, const void* packed) {
 }
 
 int32_t itn_messages_download(itn_ctx* c, int32_t dtype, void* packed) {
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, true)) return r;
   if (dtype != c->dtype) return fail(c, ITN_ERR_ARG, "dtype differs from the uploaded data");
   const size_t bytes = (size_t)c->moff[c->nslots] * dtype_size(dtype);
@@ -931,6 +952,7 @@ int32_t itn_messages_download(itn_ctx* c, int32_t dtype, void* packed) {
 }
 
 int32_t itn_messages_init(itn_ctx* c, int32_t kind) {
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, false)) return r;
   if (kind < 0 || kind > 2) return fail(c, ITN_ERR_ARG, "unknown message init kind");
   c->cur = 0;
@@ -1524,11 +1546,13 @@ extern "C" {
 
 int32_t itn_bp_run(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res) {
   NvtxScope nvtx_("itn_bp_run");
+  if (int r_ = not_busy(c)) return r_;
   return bp_run_impl(c, o, res, false);
 }
 
 int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
   NvtxScope nvtx_("itn_message_update");
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, true)) return r;
   if (slot < 0 || slot >= c->nslots) return fail(c, ITN_ERR_ARG, "slot out of range");
   if (int r = ensure_device(c)) return r;
@@ -1547,6 +1571,7 @@ int32_t itn_message_update(itn_ctx* c, int64_t slot, int32_t normalize) {
 
 int32_t itn_iterate_diff(itn_ctx* c, int32_t dtype, const void* m1, const void* m2, double* out) {
   NvtxScope nvtx_("itn_iterate_diff");
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "no network uploaded");
   if (!m1 || !m2 || !out) return fail(c, ITN_ERR_ARG, "null pointer");
@@ -1831,6 +1856,7 @@ extern "C" {
 
 int32_t itn_sweep_vjp(itn_ctx* c, int32_t normalized, const void* cot_out, void* cot_in) {
   NvtxScope nvtx_("itn_sweep_vjp");
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, true)) return r;
   if (!cot_out || !cot_in) return fail(c, ITN_ERR_ARG, "null cotangent pointer");
   if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
@@ -1851,6 +1877,7 @@ int32_t itn_sweep_vjp(itn_ctx* c, int32_t normalized, const void* cot_out, void*
 
 int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_result* res) {
   NvtxScope nvtx_("itn_bp_grad");
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, true)) return r;
   if (!grad) return fail(c, ITN_ERR_ARG, "null gradient pointer");
   if (c->dtype != ITN_F32 && c->dtype != ITN_F64)
@@ -1949,6 +1976,7 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
 
 int32_t itn_tc_selftest(itn_ctx* c, int32_t* m128_ok, int32_t* m64_ok, double* max_err,
                         int32_t* lane_of_row) {
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (int r = ensure_device(c)) return r;
   int a = 0, b = 0, lr[64];
@@ -1991,6 +2019,7 @@ extern "C" {
 int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* logze,
                        double* totals, int32_t* flags) {
   NvtxScope nvtx_("itn_logscalars");
+  if (int r_ = not_busy(c)) return r_;
   if (int r = check_ready(c, true)) return r;
   if (int r = ensure_device(c)) return r;
   const size_t es = dtype_size(c->dtype);
@@ -2021,11 +2050,11 @@ int32_t itn_logscalars(itn_ctx* c, void* zv, void* ze, double* logzv, double* lo
   return ITN_OK;
 }
 
-int32_t itn_bp_solve(itn_ctx* c, int32_t dtype, const void* tensors, const void* messages_in,
-                     const itn_bp_opts* o, itn_bp_result* res, void* messages_out, double* totals,
-                     int32_t* flags) {
-  NvtxScope nvtx_("itn_bp_solve");
+int32_t itn_bp_solve_submit(itn_ctx* c, int32_t dtype, const void* tensors, const void* messages_in,
+                            const itn_bp_opts* o, void* messages_out, int32_t logz) {
+  NvtxScope nvtx_("itn_bp_solve_submit");
   if (!c) return ITN_ERR_ARG;
+  if (int r = not_busy(c)) return r;
   if (!c->have_graph) return fail(c, ITN_ERR_STATE, "upload the network first");
   if (!o) return fail(c, ITN_ERR_ARG, "null options");
   const size_t tb = (size_t)c->toff[c->nv] * (dtype >= ITN_F32 && dtype <= ITN_C128 ? dtype_size(dtype) : 0);
@@ -2047,23 +2076,47 @@ int32_t itn_bp_solve(itn_ctx* c, int32_t dtype, const void* tensors, const void*
   // afterwards would move it under those copies)
   if (int r = ensure_pinned(c, kPinLogzAt + 20 * (size_t)c->n_nets + 16)) return r;
   // the solve (its last synchronisation deferred when it has no tolerance)
-  if (int r = bp_run_impl(c, o, res, true)) return r;
-  // log-norm and the messages, then one wait for everything
+  c->submitted.res = itn_bp_result{};
+  if (int r = bp_run_impl(c, o, &c->submitted.res, true)) return r;
+  // log-norm and the messages, queued behind the solve
   unsigned char* h = static_cast<unsigned char*>(c->h_pin) + kPinLogzAt;
-  double* h_tot = reinterpret_cast<double*>(h);
-  int32_t* h_fl = reinterpret_cast<int32_t*>(h + 16 * (size_t)c->n_nets);
-  if (totals || flags) {
+  if (logz) {
     if (int r = enqueue_logscalars(c)) return r;
-    CK(cudaMemcpyAsync(h_tot, c->d_tot.p, 16 * (size_t)c->n_nets, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(h_fl, c->d_flags.p, 4 * (size_t)c->n_nets, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h, c->d_tot.p, 16 * (size_t)c->n_nets, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h + 16 * (size_t)c->n_nets, c->d_flags.p, 4 * (size_t)c->n_nets, cudaMemcpyDeviceToHost,
+                       c->stream));
   }
   if (messages_out && mb)
     CK(cudaMemcpyAsync(messages_out, c->d_msg[c->cur].p, mb, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  if (int r = bp_run_finish(c, res)) return r;
-  if (totals) memcpy(totals, h_tot, 16 * (size_t)c->n_nets);
-  if (flags) memcpy(flags, h_fl, 4 * (size_t)c->n_nets);
+  c->submitted.active = true;
+  c->submitted.logz = logz != 0;
   return ITN_OK;
+}
+
+int32_t itn_bp_solve_wait(itn_ctx* c, itn_bp_result* res, double* totals, int32_t* flags) {
+  NvtxScope nvtx_("itn_bp_solve_wait");
+  if (!c) return ITN_ERR_ARG;
+  if (!c->submitted.active) return fail(c, ITN_ERR_STATE, "no solve was submitted");
+  c->submitted.active = false;
+  CK(cudaStreamSynchronize(c->stream));
+  // a run without a tolerance completes here; one with a tolerance already did in the submit
+  if (res && !c->pending.active) *res = c->submitted.res;
+  if (int r = bp_run_finish(c, res)) return r;
+  if ((totals || flags) && !c->submitted.logz)
+    return fail(c, ITN_ERR_ARG, "the solve was submitted without the log-norm");
+  const unsigned char* h = static_cast<const unsigned char*>(c->h_pin) + kPinLogzAt;
+  if (totals) memcpy(totals, h, 16 * (size_t)c->n_nets);
+  if (flags) memcpy(flags, h + 16 * (size_t)c->n_nets, 4 * (size_t)c->n_nets);
+  return ITN_OK;
+}
+
+int32_t itn_bp_solve(itn_ctx* c, int32_t dtype, const void* tensors, const void* messages_in,
+                     const itn_bp_opts* o, itn_bp_result* res, void* messages_out, double* totals,
+                     int32_t* flags) {
+  NvtxScope nvtx_("itn_bp_solve");
+  if (int r = itn_bp_solve_submit(c, dtype, tensors, messages_in, o, messages_out, (totals || flags) ? 1 : 0))
+    return r;
+  return itn_bp_solve_wait(c, res, totals, flags);
 }
 
 }  // extern "C"
@@ -2139,6 +2192,7 @@ int32_t itn_apply_gates(itn_ctx* c, int32_t dtype, int64_t n_gates, const itn_ga
                         int64_t out_capacity, double* out_s, int64_t s_capacity, int32_t* out_bond,
                         double* device_ms) {
   NvtxScope nvtx_("itn_apply_gates");
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
   if (n_gates < 0) return fail(c, ITN_ERR_ARG, "negative gate count");
@@ -2275,6 +2329,7 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
                              int32_t precision, void* out, int64_t out_capacity, int32_t* out_rank,
                              int64_t* out_labels, int64_t* out_dims, double* device_ms) {
   NvtxScope nvtx_("itn_contract_network");
+  if (int r_ = not_busy(c)) return r_;
   if (!c) return ITN_ERR_ARG;
   if (dtype < ITN_F32 || dtype > ITN_C128) return fail(c, ITN_ERR_ARG, "unknown dtype %d", dtype);
   if (precision != ITN_PREC_NATIVE &&

@@ -34,7 +34,7 @@ EXPORTED = [
     "itn_messages_download", "itn_messages_init", "itn_bp_run", "itn_message_update",
     "itn_iterate_diff", "itn_logscalars", "itn_tc_selftest", "itn_bp_grad",
     "itn_sweep_vjp", "itn_logz_static_scratch", "itn_contraction_order", "itn_contract_network",
-    "itn_apply_gates", "itn_bp_solve", "itn_inject_fault",
+    "itn_apply_gates", "itn_bp_solve", "itn_bp_solve_submit", "itn_bp_solve_wait", "itn_inject_fault",
 ]
 
 
@@ -108,6 +108,8 @@ def _declare(lib):
         "itn_bp_run": (_I32, [_VP, ctypes.POINTER(BpOpts), ctypes.POINTER(BpResult)]),
         "itn_bp_solve": (_I32, [_VP, _I32, _VP, _VP, ctypes.POINTER(BpOpts), ctypes.POINTER(BpResult), _VP, _VP,
                                 _VP]),
+        "itn_bp_solve_submit": (_I32, [_VP, _I32, _VP, _VP, ctypes.POINTER(BpOpts), _VP, _I32]),
+        "itn_bp_solve_wait": (_I32, [_VP, ctypes.POINTER(BpResult), _VP, _VP]),
         "itn_message_update": (_I32, [_VP, _I64, _I32]),
         "itn_iterate_diff": (_I32, [_VP, _I32, _VP, _VP, ctypes.POINTER(ctypes.c_double)]),
         "itn_logscalars": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),

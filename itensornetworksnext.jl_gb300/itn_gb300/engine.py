@@ -151,6 +151,41 @@ class BPEngine:
         res = RunResult(r.iterations, r.at_iteration, r.delta, r.device_ms, r.kernel_launches)
         return res, (self._bethe(tot, fl) if logz else None), out
 
+    def solve_submit(self, tensors: np.ndarray, messages: np.ndarray, *, messages_out: np.ndarray | None = None,
+                     logz: bool = True, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
+                     precision="native", split_sweeps=0) -> None:
+        """Queue what `solve` does and return without waiting (itn_bp_solve_submit); `solve_wait`
+        returns its (RunResult, log-norm or None, messages).  The arrays are kept alive until
+        then.  With two engines on one device, the uploads of one network overlap the solve of
+        the other."""
+        t = np.ascontiguousarray(tensors)
+        m = np.ascontiguousarray(messages, dtype=t.dtype)
+        if t.size != int(self.graph.toff[-1]) or m.size != int(self.graph.moff[-1]):
+            raise ValueError("packed tensor or message size does not match the network")
+        out = messages_out if messages_out is not None else np.empty(int(self.graph.moff[-1]), dtype=t.dtype)
+        if out.dtype != t.dtype or out.size != m.size or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("messages_out must be a contiguous array of the network's message size and dtype")
+        o, keep = self._opts(schedule, edges, maxiter, tol, normalize, precision, split_sweeps)
+        self._check(self.lib.itn_bp_solve_submit(self._ctx, L.DTYPE_CODE[t.dtype], L.ptr(t), L.ptr(m),
+                                                 ctypes.byref(o), L.ptr(out), 1 if logz else 0))
+        self.dtype = t.dtype
+        self._submitted = (t, m, out, o, keep, logz)
+
+    def solve_wait(self):
+        """Wait for the solve queued by `solve_submit` (itn_bp_solve_wait)."""
+        sub = getattr(self, "_submitted", None)
+        if sub is None:
+            raise RuntimeError("no solve was submitted")
+        out, logz = sub[2], sub[5]
+        r = L.BpResult()
+        nn = self.graph.n_nets
+        tot = np.empty((nn, 2)) if logz else None
+        fl = np.empty(nn, dtype=np.int32) if logz else None
+        self._submitted = None
+        self._check(self.lib.itn_bp_solve_wait(self._ctx, ctypes.byref(r), L.ptr(tot), L.ptr(fl)))
+        res = RunResult(r.iterations, r.at_iteration, r.delta, r.device_ms, r.kernel_launches)
+        return res, (self._bethe(tot, fl) if logz else None), out
+
     def run(self, *, schedule="parallel", edges=None, maxiter=None, tol=None, normalize=True,
             precision="native", split_sweeps=0) -> RunResult:
         o, _keep = self._opts(schedule, edges, maxiter, tol, normalize, precision, split_sweeps)

@@ -48,6 +48,8 @@ def test_null_arguments_rejected(lib_built):
     assert lib.itn_destroy(None) == L.ITN_ERR_ARG
     assert lib.itn_bp_run(None, None, None) == L.ITN_ERR_ARG
     assert lib.itn_bp_solve(None, 0, None, None, None, None, None, None, None) == L.ITN_ERR_ARG
+    assert lib.itn_bp_solve_submit(None, 0, None, None, None, None, 1) == L.ITN_ERR_ARG
+    assert lib.itn_bp_solve_wait(None, None, None, None) == L.ITN_ERR_ARG
     assert lib.itn_last_error(None) == b"null context"
 
 

@@ -323,6 +323,65 @@ def test_one_call_solve_matches_separate_calls(case):
         np.testing.assert_array_equal(e.messages(), want_m)
 
 
+@pytest.mark.parametrize("case", ["tc_mixed", "fp64_tol"])
+def test_submitted_solves_on_two_contexts_match_one_call_solves(case):
+    """Networks solved back to back on two contexts with itn_bp_solve_submit / _wait (the next
+    network's uploads queued while the previous solve runs) give exactly what itn_bp_solve gives
+    for each: same messages bit for bit, iteration counts and log-norms -- for a deferred run on
+    the tensor cores and for a run with a tolerance (which completes inside the submit)."""
+    if case == "tc_mixed":
+        g = G.square_lattice(4, 4, 8, periodic=True, phys=2)
+        dt, scale, kw = np.float32, G.peps_scale(g), dict(maxiter=6, precision="bf16", split_sweeps=2)
+    else:
+        g = G.square_lattice(4, 4, 2, periodic=False, phys=2)
+        dt, scale, kw = np.float64, 1.0, dict(maxiter=100, tol=1e-12)
+    m0 = G.identity_messages(g, dt)
+    nets = [G.random_tensors(g, np.random.default_rng(40 + k), dt, scale) for k in range(5)]
+    want = []
+    with BPEngine(g) as e:
+        for t in nets:
+            r, z, m = e.solve(t, m0, **kw)
+            want.append((r.iterations, r.at_iteration, z, m.copy()))
+    got = []
+    with BPEngine(g) as e0, BPEngine(g) as e1:
+        eng = [e0, e1]
+        for k, t in enumerate(nets):
+            eng[k % 2].solve_submit(t, m0, **kw)
+            if k >= 1:
+                got.append(eng[(k - 1) % 2].solve_wait())
+        got.append(eng[(len(nets) - 1) % 2].solve_wait())
+    for (it, at, z, m), (r, z2, m2) in zip(want, got):
+        assert r.iterations == it and r.at_iteration == at
+        assert z2 == z
+        np.testing.assert_array_equal(m2, m)
+
+
+def test_submitted_solve_blocks_other_calls_until_waited():
+    """Between itn_bp_solve_submit and itn_bp_solve_wait every other call on the context is
+    refused with ITN_ERR_STATE (the solve owns the stream's staging), a second wait is refused,
+    and the context works normally after the wait."""
+    from itn_gb300 import ItnError
+    from itn_gb300 import _lib as L
+    g = G.square_lattice(4, 4, 2, periodic=False, phys=2)
+    t = G.random_tensors(g, np.random.default_rng(7), np.float64)
+    m0 = G.identity_messages(g)
+    with BPEngine(g) as e:
+        e.solve_submit(t, m0, maxiter=5)
+        with pytest.raises(ItnError) as ei:
+            e.run(maxiter=1)
+        assert ei.value.status == L.ITN_ERR_STATE
+        with pytest.raises(ItnError) as ei:
+            e.set_tensors(t)
+        assert ei.value.status == L.ITN_ERR_STATE
+        r, z, m = e.solve_wait()
+        assert r.iterations == 5
+        with pytest.raises(RuntimeError):
+            e.solve_wait()
+        r2, z2, m2 = e.solve(t, m0, maxiter=5)
+        np.testing.assert_array_equal(m2, m)
+        assert z2 == z
+
+
 def test_batched_size_classes_match_oracle():
     """A batch large enough (more than 16 items per SM) for the parallel sweep to launch its
     small vertices (at most 256 tensor entries) as a second class of one-warp CTAs: the
