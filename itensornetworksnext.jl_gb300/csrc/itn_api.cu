@@ -1933,12 +1933,59 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
                       o->normalized, nullptr, c->stream));
     AdjState hs;
     memset(&hs, 0, sizeof(hs));
+    // One adjoint iteration is two launches (the dual program, then the update with the
+    // device-side stopping rule); a chunk of kAdjChunk iterations is captured once as a CUDA
+    // graph per set of buffers and replayed, so the launches do not wait on the host.  The
+    // iterations after convergence return at once (done flag).
+    auto adj_iteration = [&]() -> int {
+      if (int r = apply_dual_mu(c, m, c->d_cot.p, &adj->done)) return r;
+      cudaError_t e = launch_adj_update(dt, c->d_moff.as<long long>(), ns, c->d_g.p, c->d_cot.p, c->d_lam.p,
+                                        c->d_F.p, c->d_S.p, c->d_mu.p, o->normalized, adj, c->stream);
+      return e == cudaSuccess ? ITN_OK : cuda_fail(c, e, "launch_adj_update");
+    };
+    constexpr int kAdjChunk = 8;
+    // The dual program's plan, made outside the capture (it sizes the global scratch, and no
+    // allocation may happen inside a capture).  The cache key holds the plan's bytes (every
+    // pointer and size baked into the captured launches) and the update's buffers, so a graph
+    // is replayed only on exactly the state it was captured for.
+    GenericArgs pa;
+    LaunchCfg pc;
+    memset(&pa, 0, sizeof(pa));
+    memset(&pc, 0, sizeof(pc));
+    if (int r = plan_dual(c, pa, pc, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, m)) return r;
+    std::string key("adjoint ");
+    key.append(reinterpret_cast<const char*>(&pa), sizeof(pa));
+    key.append(reinterpret_cast<const char*>(&pc), sizeof(pc));
+    char tail[320];
+    snprintf(tail, sizeof(tail), " %d %d %d %p %p %p %p %p %p %p %p %p", dt, o->normalized, ns, m, c->d_cot.p,
+             c->d_mu.p, c->d_lam.p, c->d_g.p, c->d_F.p, c->d_S.p, (void*)adj, c->d_moff.p);
+    key += tail;
     for (int issued = 0; issued < maxit;) {
-      const int chunk = std::min(maxit - issued, 8);
-      for (int k = 0; k < chunk; ++k) {
-        if (int r = apply_dual_mu(c, m, c->d_cot.p, &adj->done)) return r;
-        CK(launch_adj_update(dt, c->d_moff.as<long long>(), ns, c->d_g.p, c->d_cot.p, c->d_lam.p, c->d_F.p,
-                             c->d_S.p, c->d_mu.p, o->normalized, adj, c->stream));
+      const int chunk = std::min(maxit - issued, kAdjChunk);
+      if (chunk == kAdjChunk) {
+        auto it = c->graphs.find(key);
+        if (it == c->graphs.end()) {
+          cudaGraph_t graph = nullptr;
+          cudaGraphExec_t exec = nullptr;
+          CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+          int r = ITN_OK;
+          for (int k = 0; k < chunk && r == ITN_OK; ++k) r = adj_iteration();
+          cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+          if (r) {
+            if (graph) cudaGraphDestroy(graph);
+            return r;
+          }
+          if (ce != cudaSuccess) return cuda_fail(c, ce, "adjoint stream capture");
+          ce = cudaGraphInstantiate(&exec, graph, 0);
+          cudaGraphDestroy(graph);
+          if (ce != cudaSuccess) return cuda_fail(c, ce, "adjoint graph instantiate");
+          it = c->graphs.emplace(key, exec).first;
+          c->graph_launches[key] = 2 * chunk;
+        }
+        CK(cudaGraphLaunch(it->second, c->stream));
+      } else {
+        for (int k = 0; k < chunk; ++k)
+          if (int r = adj_iteration()) return r;
       }
       issued += chunk;
       CK(cudaMemcpyAsync(&hs, adj, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));

@@ -155,7 +155,8 @@ def test_tc_rejects_unsupported_network():
 @pytest.mark.parametrize("L,n,split,prec", [(32, 7, 0, "bf16"), (32, 6, 2, "bf16"), (4, 5, 1, "bf16"),
                                             (3, 9, 0, "bf16"), (48, 5, 1, "bf16"), (32, 5, 0, "tf32"),
                                             (4, 6, 3, "tf32"), (4, 2, 0, "bf16"), (4, 1, 0, "bf16"),
-                                            (4, 3, 5, "bf16"), (32, 5, 0, "tf32x3"), (4, 4, 0, "tf32x3")])
+                                            (4, 3, 5, "bf16"), (32, 5, 0, "tf32x3"), (4, 4, 0, "tf32x3"),
+                                            (32, 7, 7, "bf16")])
 def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     """Without a convergence test the sweeps run as one cooperative launch per precision
     part (tagged message entries instead of kernel boundaries); with one the engine
@@ -164,7 +165,10 @@ def test_persistent_matches_per_sweep_launches(L, n, split, prec):
     32x32 and 48x48 (about four items per group per sweep) have more half-vertex items than
     groups, 4x4 and 3x3 (the smallest periodic lattice, one CTA) fewer.  Two-sweep parts run
     as per-sweep launches in both forms, one-sweep parts read the plain input and write the
-    plain output in the same sweep, and more split sweeps than sweeps makes every sweep split."""
+    plain output in the same sweep, and more split sweeps than sweeps makes every sweep split.
+    Launches of 4 or fewer groups per CTA (split, TF32, TF32 hi/lo) deal (sweep, item) tickets
+    round-robin over the whole launch; 32x32 with 7 split sweeps gives each of the 608 groups
+    tickets of several sweeps."""
     g, t = _lattice(L, 11)
     rng = np.random.default_rng(12)
     m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
