@@ -2,8 +2,11 @@
 
 The reference has no gradient, so the check is central finite differences (step 1e-4,
 FP64) of the converged Bethe log-norm, evaluated by FP64 GPU solves whose parity with
-the oracle is covered by test_gpu_bp.py.  Bounds: FP64 gradient within 1e-6 relative of
-FD per direction; the 12x12 D=6 FP32 gradient (FP64 log-scalars) within 1e-5.
+the oracle is covered by test_gpu_bp.py, and by the FP64 CPU oracle itself.  Bounds: FP64
+gradient within 1e-6 relative of FD per direction; the 12x12 D=6 FP32 gradient (FP64
+log-scalars) within 1e-5.  The unrolled gradient (through a fixed number of sweeps, with
+per-sweep checkpointing) is checked against central differences of the oracle's unrolled
+log-norm.
 """
 import numpy as np
 import pytest
@@ -143,6 +146,34 @@ def test_peps12x12_D6_fp32_gradient():
           f"grad {info['device_ms']:.3f} ms, rel err vs FD over 32 directions {rel:.2e} "
           f"(worst direction {np.max(np.abs(gd - fds)) / np.max(np.abs(fds)):.2e} of the largest)")
     assert rel <= 1e-5
+
+
+def test_implicit_gradient_against_oracle_finite_differences():
+    """The implicit (converged fixed point) FP64 gradient against central differences of the
+    FP64 CPU oracle's converged Bethe log-norm (BP to 1e-14 from the identity, the same
+    schedule and stopping rule): within 1e-6 relative per direction."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(24)
+    g = G.square_lattice(4, 4, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m0 = G.identity_messages(g)
+
+    def oracle_logz(x):
+        m, it, _, _ = O.bp_run(g, x, m0, maxiter=5000, tol=1e-14)
+        assert it < 5000
+        return O.bethe_free_energy(g, x, m)
+
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.set_messages(m0)
+        e.run(maxiter=5000, tol=1e-14)
+        grad, info = e.grad(adjoint=True, tol=1e-12)
+    h = 1e-4
+    for _ in range(6):
+        d = rng.standard_normal(t.size)
+        d /= np.linalg.norm(d)
+        fd = (oracle_logz(t + h * d) - oracle_logz(t - h * d)) / (2 * h)
+        assert abs(grad @ d - fd) <= 1e-6 * max(abs(fd), 1.0), (grad @ d, fd)
 
 
 # ---- unrolled gradient through the sweeps, with per-sweep checkpointing -------------------------
