@@ -85,18 +85,25 @@ __device__ __forceinline__ void z3_final(const T* src, const T* A, int n, int D,
   const float inv_in = 1.f / (float)inner;
   v0 = tzero<T>();
   v1 = tzero<T>();
+  // When `inner` is a multiple of 16, threads of different k (or b) reading the same position
+  // hit the same shared-memory banks; each thread then walks the positions from its own
+  // offset (mod R), so that threads reading at the same moment hit different banks (uniform
+  // D = 8 batches: 62.8 -> 58.0 ms per solve).  Other strides keep the plain order.
+  const bool spread = (inner & 15) == 0;
   if (Q >= g.nt) {
     for (int h = 0; h < 2; ++h) {
       const int q = g.tid + g.nt * h;
       if (q >= Q) break;
       const int b = q / D, k = q - b * D;
+      const int rot = spread ? (k + D * b) % R : 0;
       T acc = tzero<T>();
-      int o = 0, i = 0;
+      int o = qdiv(rot, inv_in), i = rot - o * inner;
+      const int O = R / inner;
       for (int r = 0; r < R; ++r) {
         acc = fmac(src[(o * D + k) * inner + i], conjx(A[(o * D + b) * inner + i]), acc);
         if (++i == inner) {
           i = 0;
-          ++o;
+          if (++o == O) o = 0;
         }
       }
       if (h == 0) v0 = acc;
@@ -108,8 +115,11 @@ __device__ __forceinline__ void z3_final(const T* src, const T* A, int n, int D,
   T acc = tzero<T>();
   if (gs < G) {
     const int b = q / D, k = q - b * D;
+    const int rot = spread ? (k + D * b) % R : 0;
     for (int r = gs; r < R; r += G) {
-      const int o = qdiv(r, inv_in), i = r - o * inner;
+      int rr = r + rot;
+      if (rr >= R) rr -= R;
+      const int o = qdiv(rr, inv_in), i = rr - o * inner;
       acc = fmac(src[(o * D + k) * inner + i], conjx(A[(o * D + b) * inner + i]), acc);
     }
   }
@@ -149,12 +159,13 @@ __device__ __forceinline__ double grp_sum_d(double v, double* wred, const Grp& g
 // Normalise (sum of entries) and store the message on `slot`; with a convergence test, the
 // slot's fidelity diff against the previous message (beliefpropagation.jl:261-267).
 template <typename T>
-__device__ __forceinline__ void z3_store(const Z3Args& a, int slot, int Q, T v0, T v1, T* red, const Grp& g) {
+__device__ __forceinline__ void z3_store(const Z3Args& a, int slot, long long mo, int Q, T v0, T v1, T* red,
+                                         const Grp& g) {
   const bool has1 = g.tid + g.nt < Q, has0 = g.tid < Q;
   const T s = grp_sum(add(has0 ? v0 : tzero<T>(), has1 ? v1 : tzero<T>()), red, g);
   const bool scale = a.normalize && !is_zero(s);
-  T* dst = reinterpret_cast<T*>(a.msg_out) + a.moff[slot];
-  const T* old = reinterpret_cast<const T*>(a.msg_in) + a.moff[slot];
+  T* dst = reinterpret_cast<T*>(a.msg_out) + mo;
+  const T* old = reinterpret_cast<const T*>(a.msg_in) + mo;
   double n1 = 0, n2 = 0, dre = 0, dim = 0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -189,21 +200,20 @@ __device__ __forceinline__ void z3_store(const Z3Args& a, int slot, int Q, T v0,
   }
 }
 
-// The three updates of vertex u by one group (slice: A, two buffers of nmax entries, three
-// messages of up to 64 entries, 256 reduction entries).
+// The three updates of work item `it` (one vertex) by one group (slice: A, two buffers of nmax
+// entries, three messages of up to 64 entries, 256 reduction entries).
 template <typename T>
-__device__ void z3_item(const Z3Args& a, int u, T* sA, T* sB, T* sC, T* sm, T* red, const Grp& g) {
-  const int s0 = a.off[u];
-  const int D0 = a.bond[s0], D1 = a.bond[s0 + 1], D2 = a.bond[s0 + 2];
-  const long long t0 = a.toff[u];
-  const int n = (int)(a.toff[u + 1] - t0);
-  const T* A = reinterpret_cast<const T*>(a.tens) + t0;
+__device__ void z3_item(const Z3Args& a, int it, T* sA, T* sB, T* sC, T* sm, T* red, const Grp& g) {
+  const Z3Meta& mt = a.meta[it];
+  const int s0 = mt.s0, n = mt.n;
+  const int D0 = mt.D[0], D1 = mt.D[1], D2 = mt.D[2];
+  const T* A = reinterpret_cast<const T*>(a.tens) + mt.t0;
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
   for (int j = g.tid; j < n; j += g.nt) sA[j] = A[j];
   const int Dl[3] = {D0, D1, D2};
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
-    const T* m = min_ + a.moff[a.rev[s0 + l]];
+    const T* m = min_ + mt.moff_in[l];
     for (int j = g.tid; j < Dl[l] * Dl[l]; j += g.nt) sm[64 * l + j] = m[j];
   }
   g.sync();
@@ -214,17 +224,17 @@ __device__ void z3_item(const Z3Args& a, int u, T* sA, T* sB, T* sC, T* sm, T* r
   z3_absorb(sB, sC, n, D1, in1, sm + 64, g);  // T01
   g.sync();
   z3_final(sC, sA, n, D2, in2, red, g, v0, v1);
-  z3_store(a, s0 + 2, D2 * D2, v0, v1, red, g);
+  z3_store(a, s0 + 2, mt.moff_out[2], D2 * D2, v0, v1, red, g);
   z3_absorb(sB, sC, n, D2, in2, sm + 128, g);  // T02
   g.sync();
   z3_final(sC, sA, n, D1, in1, red, g, v0, v1);
-  z3_store(a, s0 + 1, D1 * D1, v0, v1, red, g);
+  z3_store(a, s0 + 1, mt.moff_out[1], D1 * D1, v0, v1, red, g);
   z3_absorb(sA, sB, n, D1, in1, sm + 64, g);  // T1
   g.sync();
   z3_absorb(sB, sC, n, D2, in2, sm + 128, g);  // T12
   g.sync();
   z3_final(sC, sA, n, D0, in0, red, g, v0, v1);
-  z3_store(a, s0, D0 * D0, v0, v1, red, g);
+  z3_store(a, s0, mt.moff_out[0], D0 * D0, v0, v1, red, g);
   g.sync();  // the slice is reused by the group's next vertex
 }
 
@@ -250,7 +260,7 @@ __global__ void __launch_bounds__(kZ3Threads) sweep_z3_kernel(Z3Args a) {
     T* sm = sC + c.nmax;
     T* red = sm + 192;
     const int gw = ((int)blockIdx.x - c.cta_start) * c.groups + grp, nw = c.ctas * c.groups;
-    for (int it = c.first + gw; it < c.first + c.count; it += nw) z3_item<T>(a, a.items[it], sA, sB, sC, sm, red, g);
+    for (int it = c.first + gw; it < c.first + c.count; it += nw) z3_item<T>(a, it, sA, sB, sC, sm, red, g);
   }
   if (a.conv) conv_finish_cta(a.conv);
 }

@@ -189,7 +189,8 @@ struct itn_ctx {
   bool z3 = false;
   std::vector<int> items_z3;
   std::vector<double> z3_work;      // per item: entries x (D0 + D1 + D2), the sweep's cost share
-  DevBuf d_items_z3;
+  std::vector<Z3Meta> meta_z3;      // per item: tensor / message offsets and bond dimensions
+  DevBuf d_items_z3, d_meta_z3;
   std::array<int, 4> z3_budget{{0, 0, 0, 0}};  // autotuned shared memory per CTA (bytes), per dtype
   std::array<int, 4> z3_mult{{0, 0, 0, 0}};    // autotuned CTAs per resident CTA slot
   // Parallel-sweep items in size classes (items_par is sorted by tensor size, largest
@@ -779,6 +780,23 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
     for (int u : c->items_z3)
       c->z3_work.push_back((double)(c->toff[u + 1] - c->toff[u]) *
                            (c->bond[c->off[u]] + c->bond[c->off[u] + 1] + c->bond[c->off[u] + 2]));
+    c->meta_z3.resize(nv);
+    for (int64_t i = 0; i < nv; ++i) {
+      const int u = c->items_z3[i];
+      Z3Meta& mt = c->meta_z3[i];
+      memset(&mt, 0, sizeof(mt));
+      mt.t0 = c->toff[u];
+      mt.n = (int)(c->toff[u + 1] - c->toff[u]);
+      mt.s0 = (int)c->off[u];
+      for (int l = 0; l < 3; ++l) {
+        const int64_t s = c->off[u] + l;
+        mt.D[l] = c->bond[s];
+        mt.moff_in[l] = c->moff[c->rev[s]];
+        mt.moff_out[l] = c->moff[s];
+      }
+    }
+  } else {
+    c->meta_z3.clear();
   }
   c->z3_budget = {0, 0, 0, 0};
   c->z3_mult = {0, 0, 0, 0};
@@ -797,7 +815,8 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
       (r = upload_vec(c, c->d_items_par, c->items_par, c->stream)) ||
       (r = upload_vec(c, c->d_items_scal, c->items_scal, c->stream)) ||
       (r = upload_vec(c, c->d_items_dump, c->items_dump, c->stream)) ||
-      (r = upload_vec(c, c->d_items_z3, c->items_z3, c->stream)) || (r = sync_programs(c)))
+      (r = upload_vec(c, c->d_items_z3, c->items_z3, c->stream)) ||
+      (r = upload_vec(c, c->d_meta_z3, c->meta_z3, c->stream)) || (r = sync_programs(c)))
     return r;
   {
     std::vector<int> epos(ns, -1);
@@ -1096,15 +1115,10 @@ bool use_sweep_z3(const itn_ctx* c) { return c->z3 && !use_sweep_d8(c); }
 int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult, const void* in, void* out,
             int normalize, double* slot_diff, ConvState* cv) {
   memset(&a, 0, sizeof(a));
-  a.off = c->d_off.as<int>();
-  a.rev = c->d_rev.as<int>();
-  a.bond = c->d_bond.as<int>();
-  a.toff = c->d_toff.as<long long>();
-  a.moff = c->d_moff.as<long long>();
+  a.meta = c->d_meta_z3.as<Z3Meta>();
   a.tens = c->d_tens.p;
   a.msg_in = in;
   a.msg_out = out;
-  a.items = c->d_items_z3.as<int>();
   a.normalize = normalize;
   a.slot_diff = slot_diff;
   a.conv = cv;

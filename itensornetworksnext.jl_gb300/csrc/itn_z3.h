@@ -25,16 +25,23 @@ struct Z3Class {
   int slice;
 };
 
+// Everything a group needs to start on one work item, in work-list order: one dependent load
+// instead of the chain off -> bond / rev -> moff.
+struct Z3Meta {
+  long long t0;            // first tensor entry
+  long long moff_in[3];    // offsets of the incoming messages on legs 0, 1, 2
+  long long moff_out[3];   // offsets of the outgoing messages (slots s0, s0 + 1, s0 + 2)
+  int s0;                  // first slot of the vertex
+  int n;                   // tensor entries
+  int D[3];                // bond dimensions of legs 0, 1, 2
+  int pad;
+};
+
 struct Z3Args {
-  const int* off;          // nv + 1 (three slots per vertex)
-  const int* rev;          // nslots
-  const int* bond;         // nslots
-  const long long* toff;   // nv + 1
-  const long long* moff;   // nslots + 1
+  const Z3Meta* meta;      // per work item, largest tensors first
   const void* tens;
   const void* msg_in;
   void* msg_out;
-  const int* items;        // vertices, largest tensors first
   int normalize;
   double* slot_diff;       // per-slot fidelity diffs (null: no convergence test)
   ConvState* conv;         // outer-loop state; every CTA takes part in the step
