@@ -43,6 +43,16 @@ __device__ __forceinline__ double wsum_d(double v) {
   return v;
 }
 
+// Asynchronous copy of one element (4, 8 or 16 bytes) from global to shared memory
+// (cp.async); cp_async_wait_all waits for this thread's copies.
+template <int B>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(s), "l"(gmem), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // floor(x / d) for 0 <= x < 4096 and 1 <= d <= 4096 from a float reciprocal: the quotient of
 // (x + 0.5) / d stays at least 0.5 / d away from an integer, far more than the rounding error.
 __device__ __forceinline__ int qdiv(int x, float inv) { return (int)(((float)x + 0.5f) * inv); }
@@ -200,23 +210,43 @@ __device__ __forceinline__ void z3_store(const Z3Args& a, int slot, long long mo
   }
 }
 
-// The three updates of work item `it` (one vertex) by one group (slice: A, two buffers of nmax
-// entries, three messages of up to 64 entries, 256 reduction entries).
-template <typename T>
-__device__ void z3_item(const Z3Args& a, int it, T* sA, T* sB, T* sC, T* sm, T* red, const Grp& g) {
+// Copy item `it`'s site tensor into `dst` and its three incoming messages into the staging
+// `sm`, synchronously or (ASYNC) with cp.async.
+template <typename T, bool ASYNC>
+__device__ __forceinline__ void z3_load(const Z3Args& a, int it, T* dst, T* sm, const Grp& g) {
   const Z3Meta& mt = a.meta[it];
-  const int s0 = mt.s0, n = mt.n;
-  const int D0 = mt.D[0], D1 = mt.D[1], D2 = mt.D[2];
   const T* A = reinterpret_cast<const T*>(a.tens) + mt.t0;
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
-  for (int j = g.tid; j < n; j += g.nt) sA[j] = A[j];
-  const int Dl[3] = {D0, D1, D2};
+  for (int j = g.tid; j < mt.n; j += g.nt) {
+    if constexpr (ASYNC) cp_async<sizeof(T)>(dst + j, A + j);
+    else dst[j] = A[j];
+  }
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
     const T* m = min_ + mt.moff_in[l];
-    for (int j = g.tid; j < Dl[l] * Dl[l]; j += g.nt) sm[64 * l + j] = m[j];
+    for (int j = g.tid; j < mt.D[l] * mt.D[l]; j += g.nt) {
+      if constexpr (ASYNC) cp_async<sizeof(T)>(sm + 64 * l + j, m + j);
+      else sm[64 * l + j] = m[j];
+    }
   }
-  g.sync();
+}
+
+// The three updates of work item `it` (one vertex) by one group (slice: A, two buffers of nmax
+// entries, three messages of up to 64 entries, 256 reduction entries).  `loaded`: the tensor
+// and messages are already in sA and sm (prefetched by the previous item).  `next` >= 0: once
+// the last absorption is done, sB and sm are free, and the next item's tensor and messages are
+// copied into them asynchronously while this item's last contraction and store run; the
+// caller swaps sA and sB.
+template <typename T>
+__device__ void z3_item(const Z3Args& a, int it, int next, bool loaded, T* sA, T* sB, T* sC, T* sm, T* red,
+                        const Grp& g) {
+  const Z3Meta& mt = a.meta[it];
+  const int s0 = mt.s0, n = mt.n;
+  const int D0 = mt.D[0], D1 = mt.D[1], D2 = mt.D[2];
+  if (!loaded) {
+    z3_load<T, false>(a, it, sA, sm, g);
+    g.sync();
+  }
   const int in0 = D1 * D2, in1 = D2, in2 = 1;
   T v0, v1;
   z3_absorb(sA, sB, n, D0, in0, sm, g);  // T0
@@ -233,8 +263,10 @@ __device__ void z3_item(const Z3Args& a, int it, T* sA, T* sB, T* sC, T* sm, T* 
   g.sync();
   z3_absorb(sB, sC, n, D2, in2, sm + 128, g);  // T12
   g.sync();
+  if (next >= 0) z3_load<T, true>(a, next, sB, sm, g);
   z3_final(sC, sA, n, D0, in0, red, g, v0, v1);
   z3_store(a, s0, mt.moff_out[0], D0 * D0, v0, v1, red, g);
+  if (next >= 0) cp_async_wait_all();
   g.sync();  // the slice is reused by the group's next vertex
 }
 
@@ -260,7 +292,16 @@ __global__ void __launch_bounds__(kZ3Threads) sweep_z3_kernel(Z3Args a) {
     T* sm = sC + c.nmax;
     T* red = sm + 192;
     const int gw = ((int)blockIdx.x - c.cta_start) * c.groups + grp, nw = c.ctas * c.groups;
-    for (int it = c.first + gw; it < c.first + c.count; it += nw) z3_item<T>(a, it, sA, sB, sC, sm, red, g);
+    bool loaded = false;
+    const int end = c.first + c.count;
+    for (int it = c.first + gw; it < end; it += nw) {
+      const int next = it + nw < end ? it + nw : -1;
+      z3_item<T>(a, it, next, loaded, sA, sB, sC, sm, red, g);
+      loaded = next >= 0;
+      T* tmp = sA;
+      sA = sB;
+      sB = tmp;
+    }
   }
   if (a.conv) conv_finish_cta(a.conv);
 }
