@@ -46,7 +46,7 @@ METRIC = "BP message updates/s (32x32, D=8) mixed vs plain FP32; grad time @1e-6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 UNIT = "message updates/s"
 # solves in flight in the serving form of the end-to-end measurement (one context each)
-E2E_CONTEXTS = 4
+E2E_CONTEXTS = 8
 
 
 def workload():
@@ -362,7 +362,7 @@ def run_gpu(args):
     # ... and the serving form of the same call: E2E_CONTEXTS contexts, each step submitted with
     # itn_bp_solve_submit and collected with itn_bp_solve_wait E2E_CONTEXTS - 1 steps later, so
     # that later steps' uploads overlap earlier steps' solves; every step still copies its own
-    # inputs in and its messages and log-norm out.  The contexts' buffers (~400 MB) exceed L2.
+    # inputs in and its messages and log-norm out.  The contexts' buffers (~800 MB) exceed L2.
     engs = [eng] + [BPEngine(g, device=device) for _ in range(E2E_CONTEXTS - 1)]
     m_out = [m_host] + [torch.empty(int(g.moff[-1]), dtype=torch.float32, pin_memory=True).numpy()
                         for _ in range(E2E_CONTEXTS - 1)]
