@@ -193,6 +193,7 @@ struct itn_ctx {
   DevBuf d_items_z3, d_meta_z3;
   std::array<int, 4> z3_budget{{0, 0, 0, 0}};  // autotuned shared memory per CTA (bytes), per dtype
   std::array<int, 4> z3_mult{{0, 0, 0, 0}};    // autotuned CTAs per resident CTA slot
+  std::array<int, 4> z3_k0{{0, 0, 0, 0}};      // autotuned fixed cost per vertex (work units)
   // Parallel-sweep items in size classes (items_par is sorted by tensor size, largest
   // first), in launch order: contiguous item ranges with their own staging limits and CTA
   // size; a single class uses the whole network's limits and the tuned CTA size.
@@ -800,6 +801,7 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
   }
   c->z3_budget = {0, 0, 0, 0};
   c->z3_mult = {0, 0, 0, 0};
+  c->z3_k0 = {0, 0, 0, 0};
   c->tuned_block.assign(4, 0);
   if (c->prog_host.empty()) c->prog_host.push_back(0);
   c->prog_dirty = true;
@@ -1112,8 +1114,8 @@ bool use_sweep_z3(const itn_ctx* c) { return c->z3 && !use_sweep_d8(c); }
 // size classes by the largest tensor (at most 1024, 512, ... entries), warps per CTA of a
 // class = slices of its largest vertex that fit the budget (at most 8), CTAs shared among
 // the classes in proportion to their work, the total `mult` x the CTAs resident at once.
-int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult, const void* in, void* out,
-            int normalize, double* slot_diff, ConvState* cv) {
+int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult, int k0, const void* in,
+            void* out, int normalize, double* slot_diff, ConvState* cv) {
   memset(&a, 0, sizeof(a));
   a.meta = c->d_meta_z3.as<Z3Meta>();
   a.tens = c->d_tens.p;
@@ -1140,8 +1142,11 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
   smem = std::min(smem, kZ3MaxSmem);
   const int per_sm = std::max(1, z3_blocks_per_sm(c->dtype, smem));
   const int total = std::max(1, c->sm_count * per_sm * std::max(mult, 1));
+  // a class's CTAs are in proportion to its work: entries x (D0 + D1 + D2) per vertex plus a
+  // fixed cost k0 per vertex (loading, barriers and index arithmetic, which dominate small
+  // vertices; without it the classes of small vertices got too few CTAs and finished last)
   double wsum = 0;
-  for (double w : c->z3_work) wsum += w;
+  for (double w : c->z3_work) wsum += w + k0;
   int start = 0;
   a.n_classes = (int)ranges.size();
   for (size_t k = 0; k < ranges.size(); ++k) {
@@ -1157,7 +1162,7 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
     while (cl.groups * 2 <= fit) cl.groups *= 2;
     cl.wpi = (kZ3Threads / 32) / cl.groups;
     double w = 0;
-    for (int q = cl.first; q < cl.first + cl.count; ++q) w += c->z3_work[q];
+    for (int q = cl.first; q < cl.first + cl.count; ++q) w += c->z3_work[q] + k0;
     const int need = (cl.count + cl.groups - 1) / cl.groups;
     cl.ctas = std::max(1, std::min(need, (int)std::lround(total * w / std::max(wsum, 1.0))));
     cl.cta_start = start;
@@ -1167,45 +1172,50 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
   return ITN_OK;
 }
 
-// Autotuner of the grouped sweep: time one sweep per (shared-memory budget, CTA multiplier)
-// candidate on the current messages (best of three after a warm-up launch) and keep the
-// fastest shape for this dtype.
+// Autotuner of the grouped sweep: time one sweep per (shared-memory budget, CTA multiplier,
+// fixed cost per vertex in the class split) candidate on the current messages (best of two
+// after a warm-up launch) and keep the fastest shape for this dtype.  On the 256-network
+// complex64 batch the fixed cost took the solve from 15.8 to 10.4 ms.
 int autotune_z3(itn_ctx* c) {
   const int dt = c->dtype;
   if (c->z3_budget[dt] > 0) return ITN_OK;
   const int budgets[4] = {24 << 10, 48 << 10, 96 << 10, 200 << 10};
   const int mults[2] = {1, 2};
+  const int k0s[3] = {0, 1250, 5000};
   float best = 1e30f;
-  int bb = budgets[1], bm = 1;
+  int bb = budgets[1], bm = 1, bk = 0;
   for (int budget : budgets)
-    for (int mult : mults) {
-      Z3Args a;
-      int grid = 0;
-      size_t smem = 0;
-      if (int r = plan_z3(c, a, grid, smem, budget, mult, c->d_msg[c->cur].p, c->d_msg[c->cur ^ 1].p, 1, nullptr,
-                          nullptr))
-        return r;
-      float ms = 1e30f;
-      for (int rep = 0; rep < 4; ++rep) {
-        float t = 0.f;
-        CK(cudaEventRecord(c->ev0, c->stream));
-        CK(launch_sweep_z3(dt, a, grid, smem, c->stream));
-        CK(cudaEventRecord(c->ev1, c->stream));
-        CK(cudaEventSynchronize(c->ev1));
-        CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
-        if (rep > 0) ms = std::min(ms, t);
+    for (int mult : mults)
+      for (int k0 : k0s) {
+        Z3Args a;
+        int grid = 0;
+        size_t smem = 0;
+        if (int r = plan_z3(c, a, grid, smem, budget, mult, k0, c->d_msg[c->cur].p, c->d_msg[c->cur ^ 1].p, 1,
+                            nullptr, nullptr))
+          return r;
+        float ms = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+          float t = 0.f;
+          CK(cudaEventRecord(c->ev0, c->stream));
+          CK(launch_sweep_z3(dt, a, grid, smem, c->stream));
+          CK(cudaEventRecord(c->ev1, c->stream));
+          CK(cudaEventSynchronize(c->ev1));
+          CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+          if (rep > 0) ms = std::min(ms, t);
+        }
+        if (getenv("ITN_DEBUG"))
+          fprintf(stderr, "[itn] z3 autotune: budget %d KB mult %d k0 %d grid %d smem %zu: %.4f ms\n", budget >> 10,
+                  mult, k0, grid, smem, ms);
+        if (ms < best) {
+          best = ms;
+          bb = budget;
+          bm = mult;
+          bk = k0;
+        }
       }
-      if (getenv("ITN_DEBUG"))
-        fprintf(stderr, "[itn] z3 autotune: budget %d KB mult %d grid %d smem %zu: %.4f ms\n", budget >> 10, mult,
-                grid, smem, ms);
-      if (ms < best) {
-        best = ms;
-        bb = budget;
-        bm = mult;
-      }
-    }
   c->z3_budget[dt] = bb;
   c->z3_mult[dt] = bm;
+  c->z3_k0[dt] = bk;
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
   return ITN_OK;
@@ -1291,7 +1301,8 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
       Z3Args za;
       int grid = 0;
       size_t smem = 0;
-      if (int r = plan_z3(c, za, grid, smem, c->z3_budget[c->dtype], c->z3_mult[c->dtype], c->d_msg[in].p,
+      if (int r = plan_z3(c, za, grid, smem, c->z3_budget[c->dtype], c->z3_mult[c->dtype], c->z3_k0[c->dtype],
+                          c->d_msg[in].p,
                           c->d_msg[out].p, o->normalize, use_tol ? c->d_slot_diff.as<double>() : nullptr, conv(c)))
         return r;
       CK(launch_sweep_z3(c->dtype, za, grid, smem, c->stream));
