@@ -131,6 +131,9 @@ mutable struct DeviceNetwork{V}
     elt::DataType
     # per vertex: canonical axis names (site name or nothing, then the link of each leg)
     canon::Vector{Vector{Any}}
+    # host arrays of a solve queued by gpu_solve_submit! (kept alive until gpu_solve_wait!)
+    pending::Any
+    n_nets::Int
 end
 
 function destroy!(d::DeviceNetwork)
@@ -182,7 +185,7 @@ function DeviceNetwork(nn::NormNetwork; device::Integer = 0)
             (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Int64}), ctx, eltype_code(elt), ptrs, strides))
     end
     moff = cumsum(vcat(Int64(0), Int64.(bond) .^ 2))
-    d = DeviceNetwork(ctx, verts, slot, off, bond, moff, elt, canon)
+    d = DeviceNetwork(ctx, verts, slot, off, bond, moff, elt, canon, nothing, 1)
     finalizer(destroy!, d)
     return d
 end
@@ -307,6 +310,49 @@ function gpu_solve(problem::INN.BeliefPropagationProblem{<:NormNetwork},
     end
     download_messages!(cache, d, nn)
     return DeviceMessageCache(cache, d)
+end
+
+"""
+    gpu_solve_submit!(d::DeviceNetwork, tensors::Vector{T}, messages_in::Vector{T},
+                      messages_out::Vector{T}; maxiter, precision = :native, split_sweeps = 0,
+                      logz = true)
+    gpu_solve_wait!(d::DeviceNetwork) -> (ItnBpResult, totals)
+
+A serving loop over many networks of the same graph: `gpu_solve_submit!` queues the uploads of
+the packed canonical tensors and messages (the layouts of `itn_tensors_upload` /
+`itn_messages_upload`), a parallel solve of `maxiter` sweeps, the log-norm and the download of
+the final messages into `messages_out`, and returns at once (`itn_bp_solve_submit`);
+`gpu_solve_wait!` waits for them (`itn_bp_solve_wait`) and returns the run result and, with
+`logz`, the per-network (re, im) log-norm totals.  With several `DeviceNetwork`s in flight the
+uploads of later networks overlap the solves of earlier ones.  The arrays must stay alive and
+unchanged until the wait; they are kept in `d` until then.
+"""
+function gpu_solve_submit!(d::DeviceNetwork, tensors::Vector{T}, messages_in::Vector{T},
+                           messages_out::Vector{T}; maxiter::Integer, precision::Symbol = :native,
+                           split_sweeps::Integer = 0, logz::Bool = true) where {T}
+    opts = ItnBpOpts(0, Int32(maxiter), -1.0, Int32(1), precision_code(precision),
+        Int32(split_sweeps), 0, C_NULL, 0)
+    check(d.ctx, ccall((:itn_bp_solve_submit, libitn), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ref{ItnBpOpts}, Ptr{Cvoid}, Int32),
+        d.ctx, eltype_code(T), tensors, messages_in, opts, messages_out, Int32(logz)))
+    d.pending = (tensors, messages_in, messages_out, logz)
+    return nothing
+end
+
+function gpu_solve_wait!(d::DeviceNetwork)
+    isnothing(d.pending) && throw(ArgumentError("no solve was submitted on this DeviceNetwork"))
+    logz = d.pending[4]
+    res = Ref{ItnBpResult}()
+    totals = logz ? zeros(Float64, 2 * d.n_nets) : Float64[]
+    flags = logz ? zeros(Int32, d.n_nets) : Int32[]
+    GC.@preserve totals flags begin
+        st = ccall((:itn_bp_solve_wait, libitn), Int32,
+            (Ptr{Cvoid}, Ref{ItnBpResult}, Ptr{Float64}, Ptr{Int32}),
+            d.ctx, res, logz ? pointer(totals) : C_NULL, logz ? pointer(flags) : C_NULL)
+        d.pending = nothing
+        check(d.ctx, st)
+    end
+    return res[], totals
 end
 
 """

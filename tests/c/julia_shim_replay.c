@@ -161,7 +161,31 @@ int main(int argc, char **argv) {
       toff += n;
     }
   }
+  /* the canonical packed tensors, for the serving calls below */
+  double canon[22];
+  CHECK(itn_tensors_download(ctx, ITN_F64, canon) == ITN_OK, itn_last_error(ctx));
   itn_destroy(ctx);
+
+  /* gpu_solve_submit!(d, tensors, messages_in, messages_out; maxiter = 10) and gpu_solve_wait!(d)
+   * on a fresh DeviceNetwork: ItnBpOpts(parallel, 10, -1.0, 1, precision, split, 0, C_NULL, 0);
+   * 10 parallel sweeps make BP exact on this tree */
+  {
+    itn_ctx *c3 = NULL;
+    CHECK(itn_create(&c3, 0, 0) == ITN_OK, "itn_create");
+    CHECK(itn_graph_upload(c3, 3, off, nbr, bond, NULL, phys, 2, NULL) == ITN_OK, itn_last_error(c3));
+    jl_bp_opts so = {0, 10, -1.0, 1, 0, 0, 0, NULL, 0};
+    double mout[26], stot[2];
+    int32_t sflags[1];
+    jl_bp_result sr;
+    CHECK(itn_bp_solve_submit(c3, ITN_F64, canon, packed, (const itn_bp_opts *)&so, mout, 1) == ITN_OK,
+          itn_last_error(c3));
+    CHECK(itn_messages_download(c3, ITN_F64, mout) == ITN_ERR_STATE, "calls refused while a solve is pending");
+    CHECK(itn_bp_solve_wait(c3, (itn_bp_result *)&sr, stot, sflags) == ITN_OK, itn_last_error(c3));
+    CHECK(sr.iterations == 10, "submitted solve ran 10 sweeps");
+    CHECK((sflags[0] & 4) == 0 && fabs(exp(stot[0]) - zz) <= 1e-12 * zz, "submitted solve: log-norm on a tree");
+    CHECK(itn_bp_solve_wait(c3, (itn_bp_result *)&sr, NULL, NULL) == ITN_ERR_STATE, "a second wait is refused");
+    itn_destroy(c3);
+  }
 
   /* contract_network(::GPUExact, nn): [ket(v), conj_bra(v)] per vertex, labels of each
    * column-major array reversed, codes in order of first appearance, greedy order */
