@@ -1174,14 +1174,15 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
 
 // Autotuner of the grouped sweep: time one sweep per (shared-memory budget, CTA multiplier,
 // fixed cost per vertex in the class split) candidate on the current messages (best of two
-// after a warm-up launch) and keep the fastest shape for this dtype.  On the 256-network
-// complex64 batch the fixed cost took the solve from 15.8 to 10.4 ms.
+// after a warm-up launch) and keep the fastest shape for this dtype (180 launches, once per
+// network and dtype).  On the 256-network complex64 batch the fixed cost took the solve from
+// 15.8 to 10.4 ms, the 64 KB budget and 3-4x CTAs to 9.7 ms.
 int autotune_z3(itn_ctx* c) {
   const int dt = c->dtype;
   if (c->z3_budget[dt] > 0) return ITN_OK;
-  const int budgets[4] = {24 << 10, 48 << 10, 96 << 10, 200 << 10};
-  const int mults[2] = {1, 2};
-  const int k0s[3] = {0, 1250, 5000};
+  const int budgets[5] = {24 << 10, 48 << 10, 64 << 10, 96 << 10, 200 << 10};
+  const int mults[4] = {1, 2, 3, 4};
+  const int k0s[3] = {0, 5000, 20000};
   float best = 1e30f;
   int bb = budgets[1], bm = 1, bk = 0;
   for (int budget : budgets)
