@@ -1111,7 +1111,7 @@ bool use_sweep_d8(const itn_ctx* c) { return c->scal_d8 && c->dtype == ITN_F32; 
 bool use_sweep_z3(const itn_ctx* c) { return c->z3 && !use_sweep_d8(c); }
 
 // Launch shape of the grouped sweep for a shared-memory budget per CTA and a CTA multiplier:
-// size classes by the largest tensor (at most 1024, 512, ... entries), warps per CTA of a
+// size classes by the largest tensor (at most 1024, 682, 454, ... entries), warps per CTA of a
 // class = slices of its largest vertex that fit the budget (at most 8), CTAs shared among
 // the classes in proportion to their work, the total `mult` x the CTAs resident at once.
 int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult, int k0, const void* in,
@@ -1127,13 +1127,17 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
   const size_t es = dtype_size(c->dtype);
   const int n = (int)c->items_z3.size();
   auto size_of = [&](int i) { const int u = c->items_z3[i]; return (int)(c->toff[u + 1] - c->toff[u]); };
-  // classes: items whose tensors have (limit / 2, limit] entries, limit = 1024, 512, ...
+  // classes: items whose tensors have (2 limit / 3, limit] entries, limit = 1024, 682, 454, ...
+  // (a class's shared-memory slices are sized for its largest tensor; with halving classes the
+  // smallest vertex of a class used half of its slice, and the mixed 256-network batch took
+  // 9.76 ms per solve against 9.39 ms with thirds; quarters gave 9.45 ms)
   std::vector<std::pair<int, int>> ranges;
   int i = 0, limit = kZ3MaxTensor;
+  auto lower = [](int l) { return (2 * l) / 3; };
   while (i < n) {
-    while (limit / 2 >= size_of(i) && limit > 8 && (int)ranges.size() + 1 < kZ3MaxClasses) limit /= 2;
+    while (lower(limit) >= size_of(i) && limit > 8 && (int)ranges.size() + 1 < kZ3MaxClasses) limit = lower(limit);
     int j = i;
-    while (j < n && (size_of(j) > limit / 2 || limit <= 8 || (int)ranges.size() + 1 == kZ3MaxClasses)) ++j;
+    while (j < n && (size_of(j) > lower(limit) || limit <= 8 || (int)ranges.size() + 1 == kZ3MaxClasses)) ++j;
     ranges.push_back({i, j});
     i = j;
   }
@@ -1176,7 +1180,7 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
 // fixed cost per vertex in the class split) candidate on the current messages (best of two
 // after a warm-up launch) and keep the fastest shape for this dtype (180 launches, once per
 // network and dtype).  On the 256-network complex64 batch the fixed cost took the solve from
-// 15.8 to 10.4 ms, the 64 KB budget and 3-4x CTAs to 9.7 ms.
+// 15.8 to 10.4 ms, the 64 KB budget and 3-4x CTAs to 9.7 ms, size classes in thirds to 9.4 ms.
 int autotune_z3(itn_ctx* c) {
   const int dt = c->dtype;
   if (c->z3_budget[dt] > 0) return ITN_OK;

@@ -8,7 +8,7 @@
 namespace itn {
 
 constexpr int kZ3Threads = 256;          // 8 warps per CTA, one vertex per warp at a time
-constexpr int kZ3MaxClasses = 8;
+constexpr int kZ3MaxClasses = 16;
 constexpr size_t kZ3MaxSmem = 227 * 1024;
 constexpr int kZ3MaxTensor = 1024;       // entries of a vertex tensor (d * D0 * D1 * D2)
 constexpr int kZ3MaxBond = 8;
