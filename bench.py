@@ -683,6 +683,7 @@ def bench_16x16(device):
         out[name] = {"iterations": best.iterations, "ms": best.device_ms,
                      "updates_per_s": best.iterations * g.nslots / (best.device_ms * 1e-3)}
         e.close()
+    out["tensor_cores"] = bench_padded_tc(device)
     g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
     t6 = G.random_tensors(g6, np.random.default_rng(63), np.float64, G.peps_scale(g6))
     e = BPEngine(g6, device=device)
@@ -695,6 +696,37 @@ def bench_16x16(device):
     z, _, ms = contract_network(ts, ls, return_time=True)
     out["exact_6x6_D3"] = {"logz_exact": float(np.log(z[()])), "logz_bp": lz_bp,
                            "bp_abs_err": abs(lz_bp - float(np.log(z[()]))), "contract_ms": ms}
+    return out
+
+
+def bench_padded_tc(device):
+    """Tensor-core sweeps of open-boundary lattices (vertices of 2-4 legs, zero-padded to the
+    8 x 8 x 8 x 8 x 2 frame, one launch per sweep) beside the FP32 CUDA-core sweeps of the same
+    networks: 16x16 D=4 and 12x12 D=6, d=2, N(0,1)/sqrt(d D^4), 30 parallel sweeps from the
+    normalised identity (device time of the solve, best of 3), and with the stopping rule
+    maxiter 50 / tol 1e-10 for the FP32-accurate modes."""
+    from itn_gb300 import BPEngine
+    from itn_gb300 import graphs as G
+    out = {}
+    for L, D in ((16, 4), (12, 6)):
+        g = G.square_lattice(L, L, D, periodic=False, phys=2)
+        t = G.random_tensors(g, np.random.default_rng(100 * L + D), np.float64, G.peps_scale(g))
+        e = BPEngine(g, device=device)
+        e.set_tensors(t.astype(np.float32))
+        res = {}
+        for name, kw in (("fp32_cuda_cores", {}), ("bf16_27_split_3", dict(precision="bf16", split_sweeps=3)),
+                         ("tf32x3", dict(precision="tf32x3")), ("fp32_cuda_cores_tol", dict(tol=1e-10)),
+                         ("tf32x3_tol", dict(precision="tf32x3", tol=1e-10))):
+            maxiter = 50 if "tol" in kw else 30
+            best = None
+            for rep in range(3):
+                e.init_messages()
+                r = e.run(maxiter=maxiter, **kw)
+                best = r if best is None or r.device_ms < best.device_ms else best
+            res[name] = {"iterations": best.iterations, "ms": best.device_ms,
+                         "updates_per_s": best.iterations * g.nslots / (best.device_ms * 1e-3)}
+        e.close()
+        out[f"open{L}x{L}_D{D}"] = res
     return out
 
 

@@ -51,7 +51,11 @@ enum { ITN_SCHED_PARALLEL = 0, ITN_SCHED_SEQUENTIAL = 1 };
  * accumulation for all but the last split_sweeps sweeps, which run in split
  * (hi/lo) precision; requires ITN_F32 storage.
  * ITN_PREC_TF32X3: every sweep on the tensor cores with TF32 hi/lo operands (three TF32
- * products per contraction, about FP32 accuracy); split_sweeps is ignored; ITN_F32 storage. */
+ * products per contraction, about FP32 accuracy); split_sweeps is ignored; ITN_F32 storage.
+ * The tensor-core modes take norm networks (layers = 2) whose vertices have at most 4 legs,
+ * bonds of at most 8 and a physical dimension of at most 2; anything smaller than 4 legs of
+ * 8 with d = 2 is zero-padded to that frame (exact: padded products are zero) and swept with
+ * one launch per sweep; other networks give ITN_ERR_UNSUPPORTED. */
 enum { ITN_PREC_NATIVE = 0, ITN_PREC_BF16 = 1, ITN_PREC_TF32 = 2, ITN_PREC_TF32X3 = 3 };
 enum { ITN_MSG_IDENTITY_NORMALIZED = 0, ITN_MSG_IDENTITY = 1, ITN_MSG_ONES = 2 };
 

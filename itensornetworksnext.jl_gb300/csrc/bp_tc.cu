@@ -1,6 +1,8 @@
-// bp_tc.cu -- tensor-core (tcgen05) BP sweep for norm networks whose vertices all
-// have four legs of bond dimension 8 and a physical dimension of 2 (the square-lattice
-// PEPS workload).
+// bp_tc.cu -- tensor-core (tcgen05) BP sweep for norm networks whose vertices have four
+// legs of bond dimension 8 and a physical dimension of 2 (the square-lattice PEPS workload),
+// and, zero-padded to that frame, any norm network with at most four legs per vertex, bonds
+// of at most 8 and a physical dimension of at most 2 (open boundaries, D < 8, d = 1; see
+// TcPadSlot).
 //
 // Per vertex u with site tensor A[s][p][q], p = (k0,k1), q = (k2,k3) (64 each), and
 // incoming messages m_l[b][k] (bra, ket) on legs l = 0..3, the four outgoing messages
@@ -148,8 +150,30 @@ __host__ __device__ constexpr TcSmem tc_smem() {
   return L;
 }
 
+// Padded networks: vertices with fewer than four legs, bonds below 8 or a physical dimension
+// of 1 run on the same kernel in an 8 x 8 x 8 x 8 x 2 frame.  Vertex u keeps four virtual legs
+// (virtual slots 4u .. 4u+3): leg l < z is its l-th CSR leg, legs z..3 are dummies of
+// dimension 1 whose incoming message is the 1 x 1 message [1].  The site tensor is zero
+// outside its own index ranges, and so are the incoming messages outside D x D, so every
+// product with a padded index is exactly zero: the outgoing messages are the unpadded
+// network's in the top-left D x D corner, zeros elsewhere (their sums, hence the
+// normalisation, are unchanged), and the outputs on dummy legs are not stored.
+struct TcPadSlot {
+  int in_off;   // first entry of the incoming message (the reverse slot's); -1 on a dummy leg
+  int out_off;  // first entry of the outgoing message (this slot's); -1 on a dummy leg
+  int slot;     // CSR slot of the leg (convergence diffs); -1 on a dummy leg
+  int dim;      // bond dimension (1 on a dummy leg)
+};
+struct TcPadVertex {
+  long long toff;  // first entry of the vertex's tensor, row-major [phys][leg 0]..[leg z-1]
+  int d;           // physical dimension (1 or 2)
+  int dims[4];     // bond dimensions of the four virtual legs (1 on dummies)
+  int pad_;
+};
+
 struct TcArgs {
   const int* rev;
+  const TcPadSlot* pad;        // padded network: per virtual slot (null: every vertex is 4 legs of 8)
   const unsigned char* image;  // operand image of the mode (OpT<OP>::img_vertex bytes per vertex)
   const float* msg_in;
   float* msg_out;
@@ -285,11 +309,26 @@ __device__ __forceinline__ void st_tagged(unsigned long long* p, float v, uint32
 }
 __device__ __forceinline__ uint32_t sweep_tag(uint32_t epoch, int t) { return (epoch << 12) | (uint32_t)t; }
 
+// Entry e (bra e / 8, ket e % 8) of a padded network's incoming message on a virtual leg.
+__device__ __forceinline__ float pad_in_entry(const float* __restrict__ m, const TcPadSlot& ps, int e) {
+  const int b = e >> 3, k = e & 7;
+  if (ps.in_off < 0) return e == 0 ? 1.f : 0.f;
+  return (b < ps.dim && k < ps.dim) ? __ldcg(m + ps.in_off + b * ps.dim + k) : 0.f;
+}
+
 // This thread's two incoming entries of `item` for sweep t (no waiting): from the plain
 // input buffer at t = 0 (tagged as ready), else from the tagged buffer of sweep t.
+template <bool PAD>
 __device__ __forceinline__ void fetch_in(const TcArgs& a, uint32_t epoch, int item, int t, int l0, int e0,
                                          unsigned long long& w0, unsigned long long& w1) {
   const int u = item >> 1;
+  if constexpr (PAD) {
+    // padded networks run one launch per sweep (t = 0): read the plain input buffer
+    const unsigned long long tg = (unsigned long long)sweep_tag(epoch, 0) << 32;
+    w0 = tg | __float_as_uint(pad_in_entry(a.msg_in, a.pad[4 * u + l0], e0));
+    w1 = tg | __float_as_uint(pad_in_entry(a.msg_in, a.pad[4 * u + l0 + 2], e0));
+    return;
+  }
   const int sa = a.rev[4 * u + l0], sb = a.rev[4 * u + l0 + 2];
   if (t == 0) {
     const unsigned long long tg = (unsigned long long)sweep_tag(epoch, 0) << 32;
@@ -327,8 +366,10 @@ __device__ __forceinline__ bool wait_in(const TcArgs& a, uint32_t epoch, int ite
   return false;
 }
 
-template <int OP, int GROUPS, bool PERSIST>
+// PAD: padded network (a.pad, see TcPadSlot; per-sweep launches only).
+template <int OP, int GROUPS, bool PERSIST, bool PAD = false>
 __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::per_sm) bp_tc_kernel(TcArgs a) {
+  static_assert(!(PAD && PERSIST), "padded networks run one launch per sweep");
   using O = OpT<OP>;
   constexpr bool SPLIT = O::split;
   static_assert(tmem_cols_for(GROUPS) <= 512, "at most 512 TMEM columns per CTA");
@@ -390,8 +431,9 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
   bool fail = false; // this thread's waits (folded into `ok` once per item)
   constexpr uint32_t idesc128 = O::tf32 ? ptx::idesc_tf32_f32(128, 64) : ptx::idesc_bf16_f32(128, 64);
   constexpr uint32_t idesc64 = O::tf32 ? ptx::idesc_tf32_f32(64, 64) : ptx::idesc_bf16_f32(64, 64);
-  // Every vertex has 4 legs of dimension 8 (checked by tc_prepare), so vertex u owns slots
-  // 4u..4u+3 and slot s's message starts at 64 s.  Thread t carries entry e = t & 63 of
+  // Every vertex has 4 legs of dimension 8 (checked by tc_prepare; a padded network has
+  // them in its virtual-slot table), so vertex u owns slots 4u..4u+3 and slot s's message
+  // starts at 64 s (padded: at the table's offsets).  Thread t carries entry e = t & 63 of
   // the incoming messages on legs l0 = t >> 6 and l0 + 2; those of the next item are
   // fetched while the current one is processed.
   const int l0 = tid >> 6, e0 = tid & 63;
@@ -404,7 +446,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     ld_pend = true;
   }
   const bool skip = a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done);
-  if (first && !skip) fetch_in(a, epoch, item, t, l0, e0, w0, w1);
+  if (first && !skip) fetch_in<PAD>(a, epoch, item, t, l0, e0, w0, w1);
   if (!first || skip) t = nsweeps;
   while (t < nsweeps) {
     // this group's next item
@@ -424,7 +466,8 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
     const int s0 = 4 * u;
     // pair (A, B) builds P; pair (H, Lg) receives the outgoing messages
     const int pa = h ? 2 : 0, pb = pa + 1, H = h ? 0 : 2, Lg = H + 1;
-    if (!wait_in(a, epoch, item, t, l0, e0, w0, w1, PERSIST && a.stall && gid == 0 && t == 1)) fail = true;
+    // (a padded network's entries come tagged from the plain input: nothing to wait for)
+    if (!PAD && !wait_in(a, epoch, item, t, l0, e0, w0, w1, PERSIST && a.stall && gid == 0 && t == 1)) fail = true;
     msg[l0 * 64 + e0] = __uint_as_float((uint32_t)w0);
     msg[(l0 + 2) * 64 + e0] = __uint_as_float((uint32_t)w1);
     group_sync(bar_id);
@@ -556,7 +599,7 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
       issue_image<OP>(sm + L.img, a.image, item2, bar_load);
       ld_pend = true;
     }
-    if (has_next) fetch_in(a, epoch, item2, t2, l0, e0, w0, w1);
+    if (has_next) fetch_in<PAD>(a, epoch, item2, t2, l0, e0, w0, w1);
     // 5. epilogue 2 from registers.  Z = Z[(bh,bl)][(kh,kl)] (bra indices of legs H, Lg
     //    on rows, kets on columns) is read with the 16x32bx2 shape: thread (w, l) holds row
     //    16w + (l & 15), i.e. bh = 2w + ((l >> 3) & 1), bl = l & 7, and the columns of its
@@ -630,13 +673,48 @@ __global__ void __launch_bounds__(kThreads * GROUPS, GROUPS > 1 ? 1 : OpT<OP>::p
       const int own = warp & 1;  // which half of the 64 entries this warp stores
       const float v = scale ? o[own] / sum : o[own];
       const int e = 64 * slot + lane + 32 * own;
-      if (!PERSIST || last) {
+      if constexpr (PAD) {
+        // store the D x D corner at the CSR slot's offset; nothing on a dummy leg
+        const TcPadSlot ps = a.pad[slot];
+        if (ps.slot >= 0) {
+          const int D = ps.dim, b = (lane + 32 * own) >> 3, k = lane & 7;
+          if (b < D && k < D) a.msg_out[ps.out_off + b * D + k] = v;
+          if (a.slot_diff && own == 0) {
+            // the previous iterate in the same padded frame (zeros outside D x D)
+            double n1 = 0, n2 = 0, dd = 0;
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const int bb = (lane + 32 * hh) >> 3;
+              const float vv = scale ? o[hh] / sum : o[hh];
+              const double ov = (bb < D && k < D) ? (double)a.msg_in[ps.out_off + bb * D + k] : 0.0;
+              n1 += (double)vv * vv;
+              n2 += ov * ov;
+              dd += (double)vv * ov;
+            }
+#pragma unroll
+            for (int kk = 16; kk >= 1; kk >>= 1) {
+              n1 += __shfl_xor_sync(0xffffffffu, n1, kk);
+              n2 += __shfl_xor_sync(0xffffffffu, n2, kk);
+              dd += __shfl_xor_sync(0xffffffffu, dd, kk);
+            }
+            if (lane == 0) {
+              const double val = 1.0 - dd * dd / (n1 * n2);
+              a.slot_diff[ps.slot] = val;
+              if (a.conv) {
+                if (val != val) atomicExch(&a.conv->nan_flag, 1);
+                else atomicMax(&a.conv->dmax, enc_double(val));
+                __threadfence();
+              }
+            }
+          }
+        }
+      } else if (!PERSIST || last) {
         a.msg_out[e] = v;
       } else {
         st_tagged(a.tagged + (size_t)((t + 1) & 3) * a.tagged_stride + e, v, sweep_tag(epoch, t + 1));
       }
       // the convergence diff needs all 64 entries: the even warp of each leg computes it
-      if (a.slot_diff && own == 0) {
+      if (!PAD && a.slot_diff && own == 0) {
         const float* old = a.msg_in + 64 * slot;
         double n1 = 0, n2 = 0, dd = 0;
 #pragma unroll
@@ -716,15 +794,32 @@ __device__ __forceinline__ void stage_block(const float* __restrict__ tens, int 
   __syncthreads();
 }
 
+// The same block of a padded network's vertex: entry (p, q) = (k0 k1, k2 k3) of A_s in the
+// 8 x 8 x 8 x 8 frame, zero outside the vertex's own index ranges (s < d, k_l < D_l).
+__device__ __forceinline__ void stage_block_pad(const float* __restrict__ tens, const TcPadVertex& pv, int s,
+                                                float* t) {
+  const int d0 = pv.dims[0], d1 = pv.dims[1], d2 = pv.dims[2], d3 = pv.dims[3];
+  for (int j = threadIdx.x; j < 4096; j += blockDim.x) {
+    const int k0 = j >> 9, k1 = (j >> 6) & 7, k2 = (j >> 3) & 7, k3 = j & 7;
+    float v = 0.f;
+    if (s < pv.d && k0 < d0 && k1 < d1 && k2 < d2 && k3 < d3)
+      v = tens[pv.toff + (((long long)(s * d0 + k0) * d1 + k1) * d2 + k2) * d3 + k3];
+    t[(j >> 6) * kImgLd + (j & 63)] = v;
+  }
+  __syncthreads();
+}
+
 // BF16 image, per vertex [A_pq(s=0,1) | A_qp(s=0,1)] hi [+ the same for lo]
 template <bool SPLIT>
 __global__ void __launch_bounds__(256) tc_image_kernel(const float* __restrict__ tens, int nv,
+                                                       const TcPadVertex* __restrict__ pad,
                                                        unsigned char* __restrict__ img) {
   constexpr uint32_t bytes = (SPLIT ? 8 : 4) * kBlk;
   __shared__ float t[64 * kImgLd];
   const int u = blockIdx.x >> 1, s = blockIdx.x & 1;
   if (u >= nv) return;
-  stage_block(tens, u, s, t);
+  if (pad) stage_block_pad(tens, pad[u], s, t);
+  else stage_block(tens, u, s, t);
   unsigned char* base = img + (size_t)u * bytes + (size_t)s * kBlk;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     const int r = ((i >> 6) << 3) + (i & 7), k0 = ((i >> 3) & 7) << 3;
@@ -755,13 +850,15 @@ __global__ void __launch_bounds__(256) tc_image_kernel(const float* __restrict__
 // SPLIT: lo = the TF32 rounding of x - hi), 16 KB per block
 template <bool SPLIT>
 __global__ void __launch_bounds__(256) tc_image_tf32_kernel(const float* __restrict__ tens, int nv,
+                                                            const TcPadVertex* __restrict__ pad,
                                                             unsigned char* __restrict__ img) {
   using O = OpT<SPLIT ? kOpTf32Split : kOpTf32>;
   constexpr uint32_t blk = O::blk;
   __shared__ float t[64 * kImgLd];
   const int u = blockIdx.x >> 1, s = blockIdx.x & 1;
   if (u >= nv) return;
-  stage_block(tens, u, s, t);
+  if (pad) stage_block_pad(tens, pad[u], s, t);
+  else stage_block(tens, u, s, t);
   unsigned char* base = img + (size_t)u * O::img_vertex + (size_t)s * blk;
   for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
     const int r = ((i >> 7) << 3) + (i & 7), k0 = ((i >> 3) & 15) << 2;
@@ -1127,6 +1224,13 @@ struct TcEngine {
   uint64_t epoch_uses = 0;
   uint64_t wait_ns = kDefaultWaitNs;  // limit of a wait on another item's message
   int stall = 0;                      // fault injection (TcArgs::stall)
+  // padded network (some vertex with fewer than 4 legs, a bond below 8 or d = 1): per-sweep
+  // launches of the PAD kernel on the virtual-slot table
+  bool padded = false;
+  TcPadSlot* d_pad_slots = nullptr;  // 4 per vertex
+  TcPadVertex* d_pad_verts = nullptr;
+  size_t pad_cap = 0;  // vertices the two tables hold
+  int occ_pad[kNumOps] = {0, 0, 0, 0};
 };
 
 TcEngine* tc_create() { return new TcEngine(); }
@@ -1139,6 +1243,8 @@ void tc_destroy(TcEngine* e) {
   if (e->d_err) cudaFree(e->d_err);
   if (e->d_tagged) cudaFree(e->d_tagged);
   if (e->d_epoch) cudaFree(e->d_epoch);
+  if (e->d_pad_slots) cudaFree(e->d_pad_slots);
+  if (e->d_pad_verts) cudaFree(e->d_pad_verts);
   delete e;
 }
 
@@ -1152,6 +1258,7 @@ void tc_invalidate(TcEngine* e) {
 
 namespace {
 template <int OP> const void* k_launch() { return (const void*)bp_tc_kernel<OP, 1, false>; }
+template <int OP> const void* k_launch_pad() { return (const void*)bp_tc_kernel<OP, 1, false, true>; }
 template <int OP> const void* k_persist() { return (const void*)bp_tc_kernel<OP, OpT<OP>::groups, true>; }
 
 // Residency of the per-sweep kernel from its own resources (shared memory plus the 1 KB the
@@ -1165,11 +1272,15 @@ void tc_configure(TcEngine* e, int smem_sm, int regs_sm) {
   cudaFuncSetAttribute(k_launch<OP>(), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   cudaFuncSetAttribute(k_persist<OP>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ptot);
   cudaFuncSetAttribute(k_persist<OP>(), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  cudaFuncAttributes fa;
-  cudaFuncGetAttributes(&fa, k_launch<OP>());
+  cudaFuncSetAttribute(k_launch_pad<OP>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  cudaFuncSetAttribute(k_launch_pad<OP>(), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   const int by_smem = smem_sm / (int)(L.total + 1024);
-  const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 4;
-  e->occ[OP] = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTmemCols));
+  for (int pad = 0; pad < 2; ++pad) {
+    cudaFuncAttributes fa;
+    cudaFuncGetAttributes(&fa, pad ? k_launch_pad<OP>() : k_launch<OP>());
+    const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 4;
+    (pad ? e->occ_pad : e->occ)[OP] = std::max(1, std::min(std::min(by_smem, by_regs), 512 / kTmemCols));
+  }
   int per_sm = 0;
   const cudaError_t oe =
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist<OP>(), kThreads * OpT<OP>::groups, ptot);
@@ -1178,11 +1289,10 @@ void tc_configure(TcEngine* e, int smem_sm, int regs_sm) {
 }
 }  // namespace
 
-cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, const int32_t* bond,
-                       const int32_t* phys, const int* d_off, const int* d_rev,
-                       const long long* d_moff, const void* d_tens, const int64_t* toff,
+cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, const int64_t* rev,
+                       const int64_t* moff, const int32_t* bond, const int32_t* phys, const int* d_off,
+                       const int* d_rev, const long long* d_moff, const void* d_tens, const int64_t* toff,
                        int precision, cudaStream_t st, const char** why) {
-  (void)toff;
   *why = nullptr;
   if (precision < 1 || precision > 3) {
     *why = "unknown tensor-core precision";
@@ -1195,16 +1305,27 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
     *why = "tensor-core sweep needs a norm network (layers = 2)";
     return cudaSuccess;
   }
+  // every vertex fits the 8 x 8 x 8 x 8 x 2 frame; the uniform case (4 legs of 8, d = 2) runs
+  // the unpadded kernels, persistent launches included
+  bool uniform = true;
   for (int64_t u = 0; u < nv; ++u) {
-    if (off[u] != 4 * u || off[u + 1] - off[u] != 4 || phys[u] != 2) {
-      *why = "tensor-core sweep needs every vertex to have 4 legs and physical dimension 2";
+    const int64_t z = off[u + 1] - off[u];
+    if (z > 4 || phys[u] < 1 || phys[u] > 2) {
+      *why = "tensor-core sweep needs at most 4 legs and a physical dimension of at most 2 per vertex";
       return cudaSuccess;
     }
-    for (int64_t s = off[u]; s < off[u + 1]; ++s)
-      if (bond[s] != 8) {
-        *why = "tensor-core sweep needs bond dimension 8 on every edge";
+    if (z != 4 || phys[u] != 2) uniform = false;
+    for (int64_t s = off[u]; s < off[u + 1]; ++s) {
+      if (bond[s] < 1 || bond[s] > 8) {
+        *why = "tensor-core sweep needs bond dimensions of at most 8";
         return cudaSuccess;
       }
+      if (bond[s] != 8) uniform = false;
+    }
+  }
+  if (!uniform && moff[off[nv]] > (int64_t)0x7fffffff) {
+    *why = "tensor-core sweep of a padded network needs fewer than 2^31 message entries";
+    return cudaSuccess;
   }
   int m128 = 0, m64 = 0;
   cudaError_t err = tc_run_probe(st, &m128, &m64, nullptr, nullptr);
@@ -1222,6 +1343,51 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
   }
   cudaMemsetAsync(e->d_err, 0, sizeof(int), st);
   if (!e->valid) {
+    e->padded = !uniform;
+    if (e->padded) {
+      std::vector<TcPadSlot> ps((size_t)4 * nv);
+      std::vector<TcPadVertex> pv((size_t)nv);
+      for (int64_t u = 0; u < nv; ++u) {
+        const int z = (int)(off[u + 1] - off[u]);
+        pv[u].toff = toff[u];
+        pv[u].d = phys[u];
+        pv[u].pad_ = 0;
+        for (int l = 0; l < 4; ++l) {
+          TcPadSlot& q = ps[4 * u + l];
+          if (l < z) {
+            const int64_t sl = off[u] + l;
+            q.in_off = (int)moff[rev[sl]];
+            q.out_off = (int)moff[sl];
+            q.slot = (int)sl;
+            q.dim = bond[sl];
+          } else {
+            q.in_off = q.out_off = q.slot = -1;
+            q.dim = 1;
+          }
+          pv[u].dims[l] = q.dim;
+        }
+      }
+      if (e->pad_cap < (size_t)nv) {
+        if (e->d_pad_slots) cudaFree(e->d_pad_slots);
+        if (e->d_pad_verts) cudaFree(e->d_pad_verts);
+        e->d_pad_slots = nullptr;
+        e->d_pad_verts = nullptr;
+        e->pad_cap = 0;
+        err = cudaMalloc(&e->d_pad_slots, (size_t)std::max<int64_t>(nv, 1) * 4 * sizeof(TcPadSlot));
+        if (err != cudaSuccess) return err;
+        err = cudaMalloc(&e->d_pad_verts, (size_t)std::max<int64_t>(nv, 1) * sizeof(TcPadVertex));
+        if (err != cudaSuccess) return err;
+        e->pad_cap = (size_t)std::max<int64_t>(nv, 1);
+      }
+      if (nv > 0) {
+        // pageable sources: the copies have read them when the calls return
+        err = cudaMemcpyAsync(e->d_pad_slots, ps.data(), ps.size() * sizeof(TcPadSlot), cudaMemcpyHostToDevice, st);
+        if (err == cudaSuccess)
+          err = cudaMemcpyAsync(e->d_pad_verts, pv.data(), pv.size() * sizeof(TcPadVertex), cudaMemcpyHostToDevice,
+                                st);
+        if (err != cudaSuccess) return err;
+      }
+    }
     // the BF16 hi/lo image serves the BF16 sweeps and the split sweeps of every mode
     const size_t split_bytes = (size_t)nv * OpT<kOpSplit>::img_vertex;
     if (e->image_bytes < split_bytes) {
@@ -1232,7 +1398,7 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       e->image_bytes = split_bytes;
     }
     tc_image_kernel<true><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens), (int)nv,
-                                                              e->image);
+                                                              e->padded ? e->d_pad_verts : nullptr, e->image);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (!e->configured) {
@@ -1280,8 +1446,8 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       if (err != cudaSuccess) return err;
       e->image_tf32_bytes = tf32_bytes;
     }
-    tc_image_tf32_kernel<false><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens),
-                                                                    (int)nv, e->image_tf32);
+    tc_image_tf32_kernel<false><<<(unsigned)(2 * nv), 256, 0, st>>>(
+        reinterpret_cast<const float*>(d_tens), (int)nv, e->padded ? e->d_pad_verts : nullptr, e->image_tf32);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     e->have_tf32 = true;
@@ -1295,8 +1461,8 @@ cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, 
       if (err != cudaSuccess) return err;
       e->image_tf32x3_bytes = bytes;
     }
-    tc_image_tf32_kernel<true><<<(unsigned)(2 * nv), 256, 0, st>>>(reinterpret_cast<const float*>(d_tens),
-                                                                   (int)nv, e->image_tf32x3);
+    tc_image_tf32_kernel<true><<<(unsigned)(2 * nv), 256, 0, st>>>(
+        reinterpret_cast<const float*>(d_tens), (int)nv, e->padded ? e->d_pad_verts : nullptr, e->image_tf32x3);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     e->have_tf32x3 = true;
@@ -1320,6 +1486,7 @@ static int tc_op(const TcRun& r) {
 static TcArgs tc_args(TcEngine* e, const TcRun& r) {
   TcArgs a;
   a.rev = e->d_rev;
+  a.pad = e->padded ? e->d_pad_slots : nullptr;
   const int op = tc_op(r);
   a.image = op == kOpTf32 ? e->image_tf32 : op == kOpTf32Split ? e->image_tf32x3 : e->image;
   a.msg_in = reinterpret_cast<const float*>(r.msg_in);
@@ -1341,8 +1508,13 @@ static TcArgs tc_args(TcEngine* e, const TcRun& r) {
 namespace {
 template <int OP>
 cudaError_t launch_sweep(TcEngine* e, const TcArgs& a, cudaStream_t st) {
-  const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[OP]));
-  bp_tc_kernel<OP, 1, false><<<grid, kThreads, tc_smem<OP>().total, st>>>(a);
+  if (e->padded) {
+    const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ_pad[OP]));
+    bp_tc_kernel<OP, 1, false, true><<<grid, kThreads, tc_smem<OP>().total, st>>>(a);
+  } else {
+    const int grid = std::max(1, std::min(2 * e->nv, e->sm_count * e->occ[OP]));
+    bp_tc_kernel<OP, 1, false><<<grid, kThreads, tc_smem<OP>().total, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -1383,7 +1555,9 @@ cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaS
   if ((op == kOpTf32 && !e->have_tf32) || (op == kOpTf32Split && !e->have_tf32x3)) return cudaErrorInvalidValue;
   // two sweeps would write the plain output buffer while the first sweep's readers of
   // the same buffer may still be running; tags hold 12 bits of sweep index
-  if (!e->persist_ok[op] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
+  // (a padded network has items without incoming messages, which could run ahead of the
+  // four rotating buffers: it always runs one launch per sweep)
+  if (e->padded || !e->persist_ok[op] || nsweeps < 1 || nsweeps == 2 || nsweeps > 4095) return cudaSuccess;
   TcArgs a = tc_args(e, r);
   a.nsweeps = nsweeps;
   cudaError_t err;

@@ -1413,9 +1413,10 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
       tc_set_stall(c->tc, c->stall);
     }
     const char* why = nullptr;
-    cudaError_t e = tc_prepare(c->tc, c->layers, c->nv, c->off.data(), c->bond.data(), c->phys.data(),
-                               c->d_off.as<int>(), c->d_rev.as<int>(), c->d_moff.as<long long>(),
-                               c->d_tens.p, c->toff.data(), o->precision, c->stream, &why);
+    cudaError_t e = tc_prepare(c->tc, c->layers, c->nv, c->off.data(), c->rev.data(), c->moff.data(),
+                               c->bond.data(), c->phys.data(), c->d_off.as<int>(), c->d_rev.as<int>(),
+                               c->d_moff.as<long long>(), c->d_tens.p, c->toff.data(), o->precision, c->stream,
+                               &why);
     if (why) return fail(c, ITN_ERR_UNSUPPORTED, "%s", why);
     if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core prepare");
   }

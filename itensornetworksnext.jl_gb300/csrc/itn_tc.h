@@ -22,11 +22,14 @@ TcEngine* tc_create();
 void tc_destroy(TcEngine* e);
 // Drop cached operand copies (the network or the tensors changed).
 void tc_invalidate(TcEngine* e);
-// Check that the uploaded network fits the tensor-core kernel and build its operand
-// copies.  On an unsupported network *why is set and cudaSuccess returned.
-cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, const int32_t* bond,
-                       const int32_t* phys, const int* d_off, const int* d_rev,
-                       const long long* d_moff, const void* d_tens, const int64_t* toff,
+// Check that the uploaded network fits the tensor-core kernel (a norm network whose vertices
+// have at most 4 legs, bonds of at most 8 and a physical dimension of at most 2; anything but
+// 4 legs of 8 with d = 2 runs zero-padded to that frame) and build its operand copies.  On an
+// unsupported network *why is set and cudaSuccess returned.  off, rev, moff, bond, phys, toff:
+// the host copies of the uploaded CSR graph, message and tensor offsets.
+cudaError_t tc_prepare(TcEngine* e, int layers, int64_t nv, const int64_t* off, const int64_t* rev,
+                       const int64_t* moff, const int32_t* bond, const int32_t* phys, const int* d_off,
+                       const int* d_rev, const long long* d_moff, const void* d_tens, const int64_t* toff,
                        int precision, cudaStream_t st, const char** why);
 // Enqueue one sweep (all directed messages) on the stream.
 cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st);
@@ -34,7 +37,7 @@ cudaError_t tc_sweep(TcEngine* e, const TcRun& r, cudaStream_t st);
 // groups; intermediate messages travel through tagged device buffers): reads r.msg_in,
 // writes r.msg_out (the two may be the same buffer).  Needs r.slot_diff == null (no
 // convergence test inside).  *used = false (and nothing enqueued) when the device cannot
-// host the cooperative grid, or for nsweeps == 2 or > 4095.
+// host the cooperative grid, for a padded network, or for nsweeps == 2 or > 4095.
 cudaError_t tc_sweeps_persistent(TcEngine* e, const TcRun& r, int nsweeps, cudaStream_t st, bool* used);
 // Device address of the engine's error flag, non-zero once a bounded wait inside the
 // tensor-core kernel gave up (reset by tc_prepare; null before the first prepare).

@@ -439,8 +439,10 @@ class SimpleMessageUpdate:
 @dataclass
 class GPUMessageUpdate:
     """Whole-solve GPU strategy: ``schedule`` "parallel" (Jacobi) or "sequential";
-    ``precision`` "native", or "bf16" (tcgen05, float32 networks with 4 legs of dim 8)
-    with ``split_sweeps`` final split-precision sweeps."""
+    ``precision`` "native", or "bf16" / "tf32" / "tf32x3" (tcgen05; float32 norm networks
+    with at most 4 legs per vertex, bonds of at most 8 and d <= 2, smaller vertices
+    zero-padded to 4 legs of 8 and d = 2) with ``split_sweeps`` final split-precision
+    sweeps."""
     normalize: bool = True
     schedule: str = "parallel"
     precision: str = "native"
