@@ -613,8 +613,8 @@ def bench_batched(device, pg=None, rank=0, world=1, steps=3):
 def run_case(name, device=0):
     """Small runs of one kernel family each, for ncu captures (profiles/*.md give the
     commands): d8 = FP32 32x32 D=8 sweeps (sweep_d8_kernel); mixed = the 30-sweep mixed solve
-    (bp_tc_kernel, tc_image_kernel); grad = the 12x12 D=6 FP32 gradient (bp2_dual_kernel,
-    adj_update_kernel); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
+    (bp_tc_kernel, tc_image_kernel); grad = the 12x12 D=6 FP32 gradient (bp2_dual_kernel, the
+    adjoint update fused into it); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
     contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel); batched = the
     256-network complex64 batch (sweep_z3_kernel); exact6 = the exact FP64 contraction of the
     6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>)."""

@@ -620,8 +620,12 @@ __device__ __forceinline__ void dispatch_absorb_dual(const T* src, const T* srcT
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d) {
+__device__ void adj_step_dev(AdjState* s);
+
+// MINB = 2: at most 128 registers, so that two CTAs of 256 threads share an SM (the
+// autotuner's 256-thread candidate); MINB = 1 for CTAs of up to 128 threads.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, DualArgs d) {
   extern __shared__ __align__(16) unsigned char smem[];
   // the dual launch sizes nbuf for both planes: nbuf = 2 * logical buffers
   const SmemLayout L = smem_layout<T>(a, blockDim.x, a.gscratch == nullptr);
@@ -643,6 +647,7 @@ __global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d
     meta->phase = 0;
   }
   __syncthreads();
+  double adj_dmax = 0, adj_lmax = 0;  // fused adjoint update: this thread's maxima
 
   for (int it = blockIdx.x; it < a.n_items; it += gridDim.x) {
     const int u = a.items[2 * it];
@@ -691,20 +696,68 @@ __global__ void __launch_bounds__(256) bp2_dual_kernel(GenericArgs a, DualArgs d
           for (int e = threadIdx.x; e < D * D; e += blockDim.x) out[e] = T(0);
           __syncthreads();
         }
-        T* dst = reinterpret_cast<T*>(d.tan_out) + a.moff[a.rev[s0 + leg]];
-        for (int e = threadIdx.x; e < D * D; e += blockDim.x)
-          dst[e] = d.transpose ? out[(e % D) * D + e / D] : out[e];
+        const int slot = a.rev[s0 + leg];
+        if (d.adj) {
+          // the adjoint update of this slot: lambda <- g + (J^T mu), mu' = (lambda - <lambda, F>) / S
+          const long long o0 = a.moff[slot];
+          const T* g = reinterpret_cast<const T*>(d.g) + o0;
+          const T* F = reinterpret_cast<const T*>(d.F) + o0;
+          T* lam = reinterpret_cast<T*>(d.lam) + o0;
+          T dot = 0;
+          for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            const T v = g[e] + (d.transpose ? out[(e % D) * D + e / D] : out[e]);
+            adj_dmax = fmax(adj_dmax, fabs((double)(v - lam[e])));
+            adj_lmax = fmax(adj_lmax, fabs((double)v));
+            lam[e] = v;
+            if (d.normalize) dot += v * F[e];
+          }
+          dot = block_sum(dot, red);
+          const T is = T(1) / reinterpret_cast<const T*>(d.S)[slot];
+          T* mu = reinterpret_cast<T*>(d.mu_next) + o0;
+          for (int e = threadIdx.x; e < D * D; e += blockDim.x) mu[e] = (lam[e] - dot) * is;
+        } else {
+          T* dst = reinterpret_cast<T*>(d.tan_out) + a.moff[slot];
+          for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+            dst[e] = d.transpose ? out[(e % D) * D + e / D] : out[e];
+        }
         __syncthreads();
       } else if (type == OP_DUMP) {
-        const T* plane = d.dump_tangent ? srcT : src;
-        const T scale = d.dump_tangent ? T(1) : T(1) / reinterpret_cast<const T*>(d.zv)[u];
         T* g = reinterpret_cast<T*>(d.grad_out) + a.toff[u];
-        if (plane)
-          for (int j = threadIdx.x; j < n; j += blockDim.x) g[j] += plane[j] * scale;
+        if (d.dump_tangent == 2) {
+          // both planes: value / Z_u + tangent
+          const T scale = T(1) / reinterpret_cast<const T*>(d.zv)[u];
+          for (int j = threadIdx.x; j < n; j += blockDim.x) g[j] += src[j] * scale + (srcT ? srcT[j] : T(0));
+        } else {
+          const T* plane = d.dump_tangent ? srcT : src;
+          const T scale = d.dump_tangent ? T(1) : T(1) / reinterpret_cast<const T*>(d.zv)[u];
+          if (plane)
+            for (int j = threadIdx.x; j < n; j += blockDim.x) g[j] += plane[j] * scale;
+        }
         __syncthreads();
       }
     }
     __syncthreads();
+  }
+  if (d.adj) {
+    // fold max |lambda_new - lambda| and max |lambda_new| into the state (order-encoded); the
+    // last CTA to finish runs the stopping rule (a stopped loop returns at once in every CTA,
+    // so the ticket stays at zero)
+    for (int o = 16; o >= 1; o >>= 1) {
+      adj_dmax = fmax(adj_dmax, __shfl_xor_sync(0xffffffffu, adj_dmax, o));
+      adj_lmax = fmax(adj_lmax, __shfl_xor_sync(0xffffffffu, adj_lmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&d.adj->dmax, enc_double(adj_dmax));
+      atomicMax(&d.adj->lmax, enc_double(adj_lmax));
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&d.adj->ticket, 1u) == gridDim.x - 1) {
+      __threadfence();
+      adj_step_dev(d.adj);
+      d.adj->ticket = 0;
+      __threadfence();
+    }
   }
 }
 
@@ -777,49 +830,6 @@ __device__ void adj_step_dev(AdjState* s) {
 }
 
 __global__ void adj_step_kernel(AdjState* s) { adj_step_dev(s); }
-
-// The tail of one adjoint iteration in one launch, one warp per slot: lambda <- g + cot
-// (max |lambda_new - lambda| and max |lambda_new| folded into the state, order-encoded), the
-// next iteration's mu exactly as grad_mu_kernel computes it, and the stopping rule in the
-// last block to finish (the other blocks have folded their maxima by then).  A stopped
-// loop returns at once in every block, so the ticket stays at zero.
-template <typename T>
-__global__ void __launch_bounds__(256) adj_update_kernel(const long long* moff, int nslots, const T* g, const T* cot,
-                                                         T* lam, const T* F, const T* S, T* mu, int normalize,
-                                                         AdjState* adj) {
-  if (*reinterpret_cast<const volatile int*>(&adj->done)) return;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  double dmax = 0, lmax = 0;
-  if (warp < nslots) {
-    T dot = 0;
-    for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) {
-      const T v = g[j] + cot[j];
-      dmax = fmax(dmax, fabs((double)(v - lam[j])));
-      lmax = fmax(lmax, fabs((double)v));
-      lam[j] = v;
-      if (normalize) dot += v * F[j];
-    }
-    dot = warp_sum(dot);
-    const T is = T(1) / S[warp];
-    for (long long j = moff[warp] + lane; j < moff[warp + 1]; j += 32) mu[j] = (lam[j] - dot) * is;
-  }
-  for (int o = 16; o >= 1; o >>= 1) {
-    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-    lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-  }
-  if (lane == 0) {
-    atomicMax(&adj->dmax, enc_double(dmax));
-    atomicMax(&adj->lmax, enc_double(lmax));
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0 && atomicAdd(&adj->ticket, 1u) == gridDim.x - 1) {
-    __threadfence();
-    adj_step_dev(adj);
-    adj->ticket = 0;
-    __threadfence();
-  }
-}
 
 // ---- the one-layer kernel ----------------------------------------------------------------
 // items: (vertex, leg mask); mask bit v set -> compute m_{u->v}; mask == 0 -> vertex scalar.
@@ -1709,16 +1719,26 @@ cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long 
 }
 
 
+namespace {
+// the dual kernel for a CTA size: more than 128 threads take the 128-register variant
+template <typename T>
+void (*dual_kernel_for(int block))(GenericArgs, DualArgs) {
+  return block > 128 ? bp2_dual_kernel<T, 2> : bp2_dual_kernel<T, 1>;
+}
+}  // namespace
+
 cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg, cudaStream_t st) {
   if (cfg.grid <= 0 || a.n_items <= 0) return cudaSuccess;
   if (dtype == DT_F32) {
-    cudaError_t e = cudaFuncSetAttribute(bp2_dual_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    auto k = dual_kernel_for<float>(cfg.block);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess) return e;
-    bp2_dual_kernel<float><<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
+    k<<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
   } else if (dtype == DT_F64) {
-    cudaError_t e = cudaFuncSetAttribute(bp2_dual_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    auto k = dual_kernel_for<double>(cfg.block);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess) return e;
-    bp2_dual_kernel<double><<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
+    k<<<cfg.grid, cfg.block, cfg.smem, st>>>(a, d);
   } else {
     return cudaErrorInvalidValue;
   }
@@ -1728,11 +1748,13 @@ cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, cons
 int dual_max_active(int dtype, int block, size_t smem) {
   int n = 0;
   if (dtype == DT_F32) {
-    cudaFuncSetAttribute(bp2_dual_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_dual_kernel<float>, block, smem);
+    auto k = dual_kernel_for<float>(block);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem);
   } else {
-    cudaFuncSetAttribute(bp2_dual_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_dual_kernel<double>, block, smem);
+    auto k = dual_kernel_for<double>(block);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem);
   }
   return n;
 }
@@ -1769,17 +1791,6 @@ cudaError_t launch_grad_mu(int dtype, const long long* moff, int nslots, const v
   const int grid = (nslots * 32 + 255) / 256;
   ITN_REAL_DISPATCH(dtype, grad_mu_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)lam, (const T*)F,
                                                                   (const T*)S, (T*)mu, normalize, done);
-                    return cudaGetLastError());
-}
-
-cudaError_t launch_adj_update(int dtype, const long long* moff, int nslots, const void* g, const void* cot,
-                              void* lam, const void* F, const void* S, void* mu, int normalize, AdjState* adj,
-                              cudaStream_t st) {
-  if (nslots <= 0) return launch_adj_step(adj, st);
-  const int grid = (nslots * 32 + 255) / 256;
-  ITN_REAL_DISPATCH(dtype, adj_update_kernel<T><<<grid, 256, 0, st>>>(moff, nslots, (const T*)g, (const T*)cot,
-                                                                     (T*)lam, (const T*)F, (const T*)S, (T*)mu,
-                                                                     normalize, adj);
                     return cudaGetLastError());
 }
 

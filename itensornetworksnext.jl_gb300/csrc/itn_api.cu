@@ -18,6 +18,7 @@
 #include <array>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -221,7 +222,7 @@ struct itn_ctx {
   std::vector<int> slot_dst, slot_eidx;  // per slot: destination vertex, undirected edge index
   DevBuf d_slot_dst, d_slot_eidx;
   // gradient work buffers
-  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_cot, d_adj;
+  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_mu2, d_cot, d_adj;
   DevBuf d_ckpt, d_seg;  // unrolled gradient: kept sweep states, recomputed segment
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
@@ -261,6 +262,8 @@ struct itn_ctx {
   std::map<std::string, int> graph_launches;
   // CTA size chosen by the autotuner for the parallel sweep, per dtype (0: not tuned)
   std::vector<int> tuned_block = std::vector<int>(4, 0);
+  std::vector<int> dual_block = std::vector<int>(4, 0);  // CTA size of the dual (gradient) launches
+  uint64_t net_sig = 0;  // hash of the uploaded network's structure (keys the tuning cache)
 
   // tensor-core engine (bp_tc.cu), created on first use
   TcEngine* tc = nullptr;
@@ -803,6 +806,22 @@ int32_t itn_graph_upload(itn_ctx* c, int64_t nv, const int64_t* csr_off, const i
   c->z3_mult = {0, 0, 0, 0};
   c->z3_k0 = {0, 0, 0, 0};
   c->tuned_block.assign(4, 0);
+  c->dual_block.assign(4, 0);
+  {
+    // FNV-1a over the structure the launch shapes depend on
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+      const unsigned char* b = static_cast<const unsigned char*>(p);
+      for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const int64_t hdr[3] = {c->nv, c->nslots, (int64_t)c->layers};
+    mix(hdr, sizeof(hdr));
+    mix(c->off.data(), c->off.size() * sizeof(int64_t));
+    mix(c->nbr.data(), c->nbr.size() * sizeof(int64_t));
+    mix(c->bond.data(), c->bond.size() * sizeof(int32_t));
+    mix(c->phys.data(), c->phys.size() * sizeof(int32_t));
+    c->net_sig = h;
+  }
   if (c->prog_host.empty()) c->prog_host.push_back(0);
   c->prog_dirty = true;
   std::vector<int> off32(c->off.begin(), c->off.end()), rev32(c->rev.begin(), c->rev.end());
@@ -1059,6 +1078,34 @@ struct ParPlan {
   std::vector<std::array<LaunchCfg, 2>> cfg;
 };
 
+// Process-wide cache of autotuned launch shapes, keyed by the tuner, the device, the dtype and
+// the network's structure: every context that uploads the same network reuses the first
+// context's choice, so solves of one network on several contexts (a serving loop's contexts,
+// a context re-created per request) tune once and run the same launch shapes, which also keeps
+// their results bit-identical (a different CTA size changes the order of partial sums).
+std::mutex g_tune_mu;
+std::map<std::string, std::array<int, 3>> g_tune_cache;
+
+std::string tune_key(const itn_ctx* c, const char* tuner) {
+  char b[160];
+  snprintf(b, sizeof(b), "%s d%d t%d n%lld s%lld h%016llx", tuner, c->device, c->dtype, (long long)c->nv,
+           (long long)c->nslots, (unsigned long long)c->net_sig);
+  return b;
+}
+
+bool tune_lookup(const itn_ctx* c, const char* tuner, std::array<int, 3>& v) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune_cache.find(tune_key(c, tuner));
+  if (it == g_tune_cache.end()) return false;
+  v = it->second;
+  return true;
+}
+
+void tune_store(const itn_ctx* c, const char* tuner, const std::array<int, 3>& v) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[tune_key(c, tuner)] = v;
+}
+
 // Autotuner for the parallel sweep: time one sweep per candidate CTA size (64, 128, 256
 // threads; each with its own residency) from the current messages into the other
 // ping-pong buffer and keep the fastest for this network and dtype.
@@ -1066,6 +1113,11 @@ int autotune_sweep(itn_ctx* c) {
   if (c->tuned_block[c->dtype] > 0 || c->items_par.empty()) return ITN_OK;
   if (getenv("ITN_NO_AUTOTUNE")) {
     c->tuned_block[c->dtype] = -1;
+    return ITN_OK;
+  }
+  std::array<int, 3> cached;
+  if (tune_lookup(c, "sweep", cached)) {
+    c->tuned_block[c->dtype] = cached[0];
     return ITN_OK;
   }
   const int cands[3] = {64, 128, 256};
@@ -1096,6 +1148,7 @@ int autotune_sweep(itn_ctx* c) {
     }
   }
   c->tuned_block[c->dtype] = best_b > 0 ? best_b : -1;
+  tune_store(c, "sweep", {c->tuned_block[c->dtype], 0, 0});
   if (getenv("ITN_DEBUG")) fprintf(stderr, "[itn] autotune: sweep CTA size %d (%.3f ms)\n", best_b, best);
   // cached graphs were captured with the previous launch shape
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
@@ -1184,6 +1237,13 @@ int plan_z3(itn_ctx* c, Z3Args& a, int& grid, size_t& smem, int budget, int mult
 int autotune_z3(itn_ctx* c) {
   const int dt = c->dtype;
   if (c->z3_budget[dt] > 0) return ITN_OK;
+  std::array<int, 3> cached;
+  if (tune_lookup(c, "z3", cached)) {
+    c->z3_budget[dt] = cached[0];
+    c->z3_mult[dt] = cached[1];
+    c->z3_k0[dt] = cached[2];
+    return ITN_OK;
+  }
   const int budgets[5] = {24 << 10, 48 << 10, 64 << 10, 96 << 10, 200 << 10};
   const int mults[4] = {1, 2, 3, 4};
   const int k0s[3] = {0, 5000, 20000};
@@ -1221,6 +1281,7 @@ int autotune_z3(itn_ctx* c) {
   c->z3_budget[dt] = bb;
   c->z3_mult[dt] = bm;
   c->z3_k0[dt] = bk;
+  tune_store(c, "z3", {bb, bm, bk});
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
   return ITN_OK;
@@ -1673,7 +1734,7 @@ int plan_dual(itn_ctx* c, GenericArgs& a, LaunchCfg& cfg, const int* d_items, in
   a.buf_elems = (c->max_tensor + 15) & ~15LL;
   a.msg_cap = 2 * c->msg_cap;
   a.max_d2 = c->max_d2;
-  cfg.block = block_for(c);
+  cfg.block = c->dtype >= 0 && c->dtype < 4 && c->dual_block[c->dtype] > 0 ? c->dual_block[c->dtype] : block_for(c);
   bool in_smem = true;
   size_t smem = generic_smem_bytes(c->dtype, a, cfg.block, true);
   if (smem > (size_t)c->smem_optin) {
@@ -1717,6 +1778,58 @@ int adjoint_prepare(itn_ctx* c, const void* m, int normalized) {
 // the normalisation (mu = (lam - <lam, F>) / S) and pushed back through the products by
 // the dual interpreter (tangent of the leave-one-out contraction on every leg).
 // cot = J^T-product of the dual interpreter for tangents mu already in c->d_mu.
+// Autotuner for the dual launches (the J^T products of the adjoint iteration): time one
+// launch per candidate CTA size -- 64 and 128 threads with the unrestricted kernel, 256 with
+// the 128-register one (two CTAs per SM) -- on tangents from c->d_mu into c->d_cot, and keep
+// the fastest for this network and dtype.  Runs outside any capture (it plans, which may size
+// the global scratch, and it synchronises).
+int autotune_dual(itn_ctx* c, const void* m) {
+  if (c->dtype < 0 || c->dtype >= 4 || c->dual_block[c->dtype] != 0 || c->items_par.empty()) return ITN_OK;
+  if (getenv("ITN_NO_AUTOTUNE")) {
+    c->dual_block[c->dtype] = -1;
+    return ITN_OK;
+  }
+  std::array<int, 3> cached;
+  if (tune_lookup(c, "dual", cached)) {
+    c->dual_block[c->dtype] = cached[0];
+    return ITN_OK;
+  }
+  const int cands[3] = {64, 128, 256};
+  float best = 1e30f;
+  int best_b = 0;
+  for (int b : cands) {
+    c->dual_block[c->dtype] = b;
+    GenericArgs a;
+    LaunchCfg cfg;
+    if (plan_dual(c, a, cfg, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, m)) {
+      cudaGetLastError();
+      continue;
+    }
+    DualArgs d;
+    memset(&d, 0, sizeof(d));
+    d.tan_in = c->d_mu.p;
+    d.tan_out = c->d_cot.p;
+    float ms = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {  // the first launch warms the caches
+      float t = 0.f;
+      CK(cudaEventRecord(c->ev0, c->stream));
+      CK(launch_dual(c->dtype, a, d, cfg, c->stream));
+      CK(cudaEventRecord(c->ev1, c->stream));
+      CK(cudaEventSynchronize(c->ev1));
+      CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+      if (rep > 0) ms = std::min(ms, t);
+    }
+    if (ms < best) {
+      best = ms;
+      best_b = b;
+    }
+  }
+  c->dual_block[c->dtype] = best_b > 0 ? best_b : -1;
+  tune_store(c, "dual", {c->dual_block[c->dtype], 0, 0});
+  if (getenv("ITN_DEBUG")) fprintf(stderr, "[itn] autotune: dual CTA size %d (%.4f ms)\n", best_b, best);
+  return ITN_OK;
+}
+
 int apply_dual_mu(itn_ctx* c, const void* m, void* cot, const int* done) {
   const int np = (int)c->items_par.size() / 2;
   GenericArgs da;
@@ -1929,17 +2042,20 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
   CK(c->d_grad.ensure(std::max<size_t>(tb, 16)));
   CK(cudaMemsetAsync(c->d_grad.p, 0, tb, c->stream));
   const int nd = (int)c->items_dump.size() / 2, np = (int)c->items_par.size() / 2;
-  // direct term: dlogZ_u/dA_u = (T_u(m) + T_u(m^T)) / Z_u
+  // direct term: dlogZ_u/dA_u = (T_u(m) + T_u(m^T)) / Z_u -- here without the adjoint, after
+  // the adjoint loop with its correction in the same two launches
   GenericArgs a;
   LaunchCfg cfg;
-  if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
   DualArgs d;
   memset(&d, 0, sizeof(d));
   d.grad_out = c->d_grad.p;
   d.zv = c->d_zv.p;
-  for (int tr = 0; tr < 2; ++tr) {
-    d.transpose = tr;
-    CK(launch_dual(dt, a, d, cfg, c->stream));
+  if (!o->adjoint) {
+    if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
+    for (int tr = 0; tr < 2; ++tr) {
+      d.transpose = tr;
+      CK(launch_dual(dt, a, d, cfg, c->stream));
+    }
   }
   int iters = 0;
   double resid = 0.0;
@@ -1964,17 +2080,42 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
                       o->normalized, nullptr, c->stream));
     AdjState hs;
     memset(&hs, 0, sizeof(hs));
-    // One adjoint iteration is two launches (the dual program, then the update with the
-    // device-side stopping rule); a chunk of kAdjChunk iterations is captured once as a CUDA
-    // graph per set of buffers and replayed, so the launches do not wait on the host.  The
-    // iterations after convergence return at once (done flag).
+    CK(c->d_mu2.ensure(std::max<size_t>(mb, 16)));
+    // One adjoint iteration is one launch: the dual program (J^T mu through the products)
+    // with the update fused into its final contractions (lambda, the next mu and, in the
+    // last CTA, the device-side stopping rule).  mu alternates between two buffers (the
+    // launch reads one while it writes the other), so iteration k reads buffer k & 1; a
+    // chunk of kAdjChunk (even) iterations is captured once as a CUDA graph per set of
+    // buffers and replayed, so the launches do not wait on the host.  The iterations after
+    // convergence return at once (done flag).
+    void* mu_buf[2] = {c->d_mu.p, c->d_mu2.p};
+    int adj_k = 0;
     auto adj_iteration = [&]() -> int {
-      if (int r = apply_dual_mu(c, m, c->d_cot.p, &adj->done)) return r;
-      cudaError_t e = launch_adj_update(dt, c->d_moff.as<long long>(), ns, c->d_g.p, c->d_cot.p, c->d_lam.p,
-                                        c->d_F.p, c->d_S.p, c->d_mu.p, o->normalized, adj, c->stream);
-      return e == cudaSuccess ? ITN_OK : cuda_fail(c, e, "launch_adj_update");
+      if (c->items_par.empty()) {
+        // no messages: the stopping rule alone (a zero change stops the loop at once)
+        CK(launch_adj_step(adj, c->stream));
+        return ITN_OK;
+      }
+      GenericArgs da;
+      LaunchCfg dcfg;
+      if (int r = plan_dual(c, da, dcfg, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, m)) return r;
+      DualArgs dd;
+      memset(&dd, 0, sizeof(dd));
+      dd.tan_in = mu_buf[adj_k & 1];
+      dd.done = &adj->done;
+      dd.adj = adj;
+      dd.g = c->d_g.p;
+      dd.lam = c->d_lam.p;
+      dd.F = c->d_F.p;
+      dd.S = c->d_S.p;
+      dd.mu_next = mu_buf[(adj_k + 1) & 1];
+      dd.normalize = o->normalized;
+      ++adj_k;
+      CK(launch_dual(c->dtype, da, dd, dcfg, c->stream));
+      return ITN_OK;
     };
     constexpr int kAdjChunk = 8;
+    static_assert(kAdjChunk % 2 == 0, "every chunk starts from mu buffer 0");
     // The dual program's plan, made outside the capture (it sizes the global scratch, and no
     // allocation may happen inside a capture).  The cache key holds the plan's bytes (every
     // pointer and size baked into the captured launches) and the update's buffers, so a graph
@@ -1983,16 +2124,18 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     LaunchCfg pc;
     memset(&pa, 0, sizeof(pa));
     memset(&pc, 0, sizeof(pc));
+    if (int r = autotune_dual(c, m)) return r;
     if (int r = plan_dual(c, pa, pc, c->d_items_par.as<int>(), (int)c->items_par.size() / 2, m)) return r;
     std::string key("adjoint ");
     key.append(reinterpret_cast<const char*>(&pa), sizeof(pa));
     key.append(reinterpret_cast<const char*>(&pc), sizeof(pc));
     char tail[320];
-    snprintf(tail, sizeof(tail), " %d %d %d %p %p %p %p %p %p %p %p %p", dt, o->normalized, ns, m, c->d_cot.p,
-             c->d_mu.p, c->d_lam.p, c->d_g.p, c->d_F.p, c->d_S.p, (void*)adj, c->d_moff.p);
+    snprintf(tail, sizeof(tail), " fused %d %d %d %p %p %p %p %p %p %p %p %p", dt, o->normalized, ns, m,
+             c->d_mu2.p, c->d_mu.p, c->d_lam.p, c->d_g.p, c->d_F.p, c->d_S.p, (void*)adj, c->d_moff.p);
     key += tail;
     for (int issued = 0; issued < maxit;) {
       const int chunk = std::min(maxit - issued, kAdjChunk);
+      adj_k = issued;  // even: the chunk starts reading mu buffer 0
       if (chunk == kAdjChunk) {
         auto it = c->graphs.find(key);
         if (it == c->graphs.end()) {
@@ -2011,7 +2154,7 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
           cudaGraphDestroy(graph);
           if (ce != cudaSuccess) return cuda_fail(c, ce, "adjoint graph instantiate");
           it = c->graphs.emplace(key, exec).first;
-          c->graph_launches[key] = 2 * chunk;
+          c->graph_launches[key] = chunk;
         }
         CK(cudaGraphLaunch(it->second, c->stream));
       } else {
@@ -2026,11 +2169,13 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     iters = hs.iters;
     resid = hs.resid;
     if (hs.nan) return fail(c, ITN_ERR_NAN, "adjoint iteration produced NaN");
-    // correction lambda^T dF/dA: tangent part of the all-legs contraction with mu
+    // direct term + the correction lambda^T dF/dA (tangent part of the all-legs contraction
+    // with mu): value plane / Z_u + tangent plane, in one launch per orientation
     CK(launch_grad_mu(dt, c->d_moff.as<long long>(), ns, c->d_lam.p, c->d_F.p, c->d_S.p, c->d_mu.p,
                       o->normalized, nullptr, c->stream));
+    if (int r = plan_dual(c, a, cfg, c->d_items_dump.as<int>(), nd, m)) return r;
     d.tan_in = c->d_mu.p;
-    d.dump_tangent = 1;
+    d.dump_tangent = 2;
     for (int tr = 0; tr < 2; ++tr) {
       d.transpose = tr;
       CK(launch_dual(dt, a, d, cfg, c->stream));

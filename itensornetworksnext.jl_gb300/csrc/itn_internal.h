@@ -58,20 +58,35 @@ struct GenericArgs {
 };
 
 // Extra arguments of the dual-number (forward-mode) interpreter used by the gradient.
+struct AdjState;
+
 struct DualArgs {
   const void* tan_in;  // tangent per outgoing slot (mu_{u->v}); null = zero tangents
   void* tan_out;       // FINAL: tangent of the message on leg w, stored at slot rev(u->w)
   int transpose;       // stage m^T and mu^T (second orientation of the real gradient)
   void* grad_out;      // DUMP target (packed canonical tensors)
   const void* zv;      // per-vertex Z_u (DUMP of the value plane scales by 1/Z_u)
-  int dump_tangent;    // DUMP the tangent plane (unscaled) instead of the value plane
+  int dump_tangent;    // DUMP: 0 the value plane / Z_u, 1 the tangent plane (unscaled), 2 both summed
   const int* done;     // adjoint loop: skip the launch once the iteration has stopped (may be null)
+  // Adjoint loop with the update fused into the launch (adj != null): the FINAL of slot t
+  // applies lambda_t <- g_t + (J^T mu)_t in place, writes the next iteration's
+  // mu_t = (lambda_t - <lambda_t, F_t>) / S_t (lambda_t when not normalising) to mu_next
+  // (not tan_in: other CTAs still read it) instead of storing the product to tan_out, and
+  // folds max |lambda_new - lambda| and max |lambda_new| into *adj, whose stopping rule the
+  // last CTA to finish runs.
+  AdjState* adj;
+  const void* g;
+  void* lam;
+  const void* F;
+  const void* S;
+  void* mu_next;
+  int normalize;
 };
 
-// Device-side state of the adjoint fixed-point iteration lambda <- g + J^T lambda: the
-// fused update kernel folds max|lambda_new - lambda| and max|lambda_new| into dmax / lmax
-// (order-encoded) and its last block turns them into the relative change and stops the
-// loop; launches after the stop return at once.
+// Device-side state of the adjoint fixed-point iteration lambda <- g + J^T lambda: the dual
+// launch with the fused update (DualArgs::adj) folds max|lambda_new - lambda| and
+// max|lambda_new| into dmax / lmax (order-encoded) and its last CTA turns them into the
+// relative change and stops the loop; launches after the stop return at once.
 struct AdjState {
   unsigned long long dmax, lmax;
   int done;       // stopped (converged, NaN or maxiter)
@@ -80,7 +95,7 @@ struct AdjState {
   int maxiter;
   double tol;
   double resid;   // last relative change
-  unsigned ticket;  // blocks of the fused update finished in this iteration
+  unsigned ticket;  // CTAs of the fused-update launch finished in this iteration
 };
 
 struct LaunchCfg {
@@ -135,9 +150,6 @@ cudaError_t launch_adj_reset(AdjState* adj, double tol, int maxiter, cudaStream_
 cudaError_t launch_adj_step(AdjState* adj, cudaStream_t st);
 // lambda <- g + cot, then mu <- (lambda - <lambda, F>) / S (normalised) or lambda, and the
 // stopping rule, in one launch (the step runs in the last block to finish).
-cudaError_t launch_adj_update(int dtype, const long long* moff, int nslots, const void* g, const void* cot,
-                              void* lam, const void* F, const void* S, void* mu, int normalize, AdjState* adj,
-                              cudaStream_t st);
 cudaError_t launch_reset_state(ConvState* s, double tol, int use_tol, cudaStream_t st);
 cudaError_t launch_step_check(ConvState* s, cudaStream_t st);
 
