@@ -107,9 +107,10 @@ precision_code(p::Symbol) = p === :native ? Int32(0) : p === :bf16 ? Int32(1) :
 solve is one device call: `schedule = :sequential` follows the `edges` order exactly (the
 reference's Gauss-Seidel sweep), `:parallel` updates every edge from the previous sweep's
 messages (Jacobi; `edges` only fixes the edge set).  `precision = :bf16` / `:tf32` run the
-tcgen05 tensor-core sweep on Float32 networks whose vertices have four legs of dimension 8 and
-a site index of dimension 2, with `split_sweeps` final hi/lo sweeps; `:tf32x3` runs every
-sweep with TF32 hi/lo operands.
+tcgen05 tensor-core sweep on Float32 networks whose vertices have at most four legs, bond
+dimensions of at most 8 and a site index of dimension at most 2 (anything smaller than four
+legs of 8 with d = 2, e.g. an open boundary, runs zero-padded to that shape), with
+`split_sweeps` final hi/lo sweeps; `:tf32x3` runs every sweep with TF32 hi/lo operands.
 """
 Base.@kwdef struct GPUMessageUpdate <: MessageUpdateAlgorithm
     normalize::Bool = true
