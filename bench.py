@@ -657,6 +657,8 @@ def run_case(name, device=0):
         ts, ls = norm_network_tensors(g6, t6)
         z, _, ms = contract_network(ts, ls, return_time=True)
         print("exact6 log z", float(np.log(z[()])), "device ms", ms)
+        z, _, ms = contract_network(ts, ls, alg="sweep", return_time=True)
+        print("exact6 sweep order: log z", float(np.log(z[()])), "device ms", ms)
     else:
         raise SystemExit(f"unknown case {name}")
     return 0
@@ -694,8 +696,11 @@ def bench_16x16(device):
     e.close()
     ts, ls = norm_network_tensors(g6, t6)
     z, _, ms = contract_network(ts, ls, return_time=True)
+    zs, _, ms_s = contract_network(ts, ls, alg="sweep", return_time=True)
     out["exact_6x6_D3"] = {"logz_exact": float(np.log(z[()])), "logz_bp": lz_bp,
-                           "bp_abs_err": abs(lz_bp - float(np.log(z[()]))), "contract_ms": ms}
+                           "bp_abs_err": abs(lz_bp - float(np.log(z[()]))), "contract_ms": ms,
+                           "contract_ms_sweep_order": ms_s,
+                           "sweep_vs_greedy_rel_diff": abs(zs[()] - z[()]) / abs(z[()])}
     return out
 
 

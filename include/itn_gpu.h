@@ -182,7 +182,11 @@ int32_t itn_logscalars(itn_ctx *ctx, void *zv, void *ze, double *logzv, double *
  * host data only (no device work).  Tensor t has ranks[t] indices; labels/dims list them
  * tensor after tensor; an index shared by two tensors is contracted, one on a single tensor
  * stays open.  alg 0 = Greedy (pair with the smallest growth, pairs sharing an index first),
- * 1 = LeftAssociative.  steps_out (2 * (n - 1) ints): step k contracts positions
+ * 1 = LeftAssociative, 3 = sweep: the cheaper, in multiply-adds, of the Greedy order and the
+ * orders in which one running product absorbs, step by step, the tensor that leaves it
+ * smallest (started from every tensor, at most 64 starts) -- boundary-sweep orders on
+ * lattices (no counterpart in the reference; an EvaluationOrderAlgorithm of this library).
+ * steps_out (2 * (n - 1) ints): step k contracts positions
  * (steps_out[2k], steps_out[2k+1]) of a working list from which both are removed and to
  * which the result (labels: free of the first ++ free of the second) is appended. */
 int32_t itn_contraction_order(int32_t n_tensors, const int32_t *ranks, const int64_t *labels,
@@ -191,7 +195,8 @@ int32_t itn_contraction_order(int32_t n_tensors, const int32_t *ranks, const int
 /* contract_network(tn; alg = Exact(order, order_alg)) (src/contract_network.jl:7-37): exact
  * contraction by pairwise GPU contractions (device permute + GEMM).  tensors[t] are host
  * row-major arrays in the order of their labels.  alg 0 = Greedy, 1 = LeftAssociative,
- * 2 = explicit `steps` (the itn_contraction_order format).  precision: ITN_PREC_NATIVE
+ * 2 = explicit `steps` (the itn_contraction_order format), 3 = sweep (see
+ * itn_contraction_order).  precision: ITN_PREC_NATIVE
  * (dtype arithmetic on CUDA cores), ITN_PREC_BF16 (float32 data, tcgen05 GEMM with BF16
  * hi/lo split operands, ~16 significant bits) or ITN_PREC_TF32X3 (float32 data, tcgen05 GEMM
  * with TF32 hi/lo split operands: the accuracy of FP32 arithmetic).  The result (row-major in the order of out_labels, at most 48

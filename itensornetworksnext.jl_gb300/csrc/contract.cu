@@ -35,11 +35,131 @@ static double prod_dims(const std::vector<int64_t>& labels, const std::map<int64
   return p;
 }
 
+// Multiply-adds of a pairwise order (the sum over steps of the product of the dimensions of
+// every index of the two operands): the cost the sweep order is compared by.
+double order_cost(const std::vector<std::vector<int64_t>>& labels, const std::map<int64_t, int64_t>& dim,
+                  const std::vector<std::pair<int, int>>& steps) {
+  std::vector<std::vector<int64_t>> L = labels;
+  double total = 0;
+  for (const auto& st : steps) {
+    const std::vector<int64_t>&a = L[st.first], &b = L[st.second];
+    std::vector<int64_t> all = a, lo;
+    for (int64_t x : b)
+      if (std::find(a.begin(), a.end(), x) == a.end()) all.push_back(x);
+    for (int64_t x : a)
+      if (std::find(b.begin(), b.end(), x) == b.end()) lo.push_back(x);
+    for (int64_t x : b)
+      if (std::find(a.begin(), a.end(), x) == a.end()) lo.push_back(x);
+    total += prod_dims(all, dim);
+    std::vector<std::vector<int64_t>> nl;
+    for (int k = 0; k < (int)L.size(); ++k)
+      if (k != st.first && k != st.second) nl.push_back(L[k]);
+    nl.push_back(lo);
+    L.swap(nl);
+  }
+  return total;
+}
+
+// Dense form of a network for the sweep search: label ids 0..m-1 per tensor, their dimensions
+// and each tensor's size.
+struct DenseNet {
+  std::vector<std::vector<int>> lab;
+  std::vector<double> dim, size;
+};
+
+static DenseNet dense_net(const std::vector<std::vector<int64_t>>& labels, const std::map<int64_t, int64_t>& dim) {
+  DenseNet d;
+  std::map<int64_t, int> id;
+  for (const auto& l : labels) {
+    std::vector<int> v;
+    double sz = 1;
+    for (int64_t x : l) {
+      auto it = id.find(x);
+      if (it == id.end()) {
+        it = id.emplace(x, (int)d.dim.size()).first;
+        d.dim.push_back((double)dim.at(x));
+      }
+      v.push_back(it->second);
+      sz *= d.dim[it->second];
+    }
+    d.lab.push_back(v);
+    d.size.push_back(sz);
+  }
+  return d;
+}
+
+// Sweep order from tensor `start`: one running product absorbs, at every step, the tensor
+// that leaves it smallest (among those sharing an index with it; ties: fewer multiply-adds).
+// On lattices this finds boundary-sweep orders (the running product is a boundary state).
+// Returns the order's multiply-adds and writes it as working-list steps.
+static double sweep_from(const DenseNet& net, int start, std::vector<std::pair<int, int>>& steps) {
+  const int n = (int)net.lab.size();
+  steps.clear();
+  std::vector<int> pos(n);  // current position of each input tensor in the working list
+  for (int t = 0; t < n; ++t) pos[t] = t;
+  std::vector<char> used(n, 0), in_run(net.dim.size(), 0);
+  used[start] = 1;
+  for (int x : net.lab[start]) in_run[x] = 1;
+  double run_size = net.size[start], total = 0;
+  int run_pos = start, live = n;
+  for (int k = 1; k < n; ++k) {
+    int best = -1;
+    bool bsh = false;
+    double bsize = 0, bflops = 0;
+    for (int j = 0; j < n; ++j) {
+      if (used[j]) continue;
+      double sh = 1;
+      bool shared = false;
+      for (int x : net.lab[j])
+        if (in_run[x]) {
+          shared = true;
+          sh *= net.dim[x];
+        }
+      const double flops = run_size * net.size[j] / sh, size = flops / sh;
+      const bool better = best < 0 || (shared && !bsh) ||
+                          (shared == bsh && (size < bsize || (size == bsize && flops < bflops)));
+      if (better) {
+        best = j; bsh = shared; bsize = size; bflops = flops;
+      }
+    }
+    // the product's labels: the running labels not on `best`, then best's not on the product
+    for (int x : net.lab[best]) in_run[x] ^= 1;
+    run_size = bsize;
+    total += bflops;
+    // working list: drop both operands, append the product
+    const int i0 = std::min(run_pos, pos[best]), i1 = std::max(run_pos, pos[best]);
+    steps.push_back({i0, i1});
+    for (int t = 0; t < n; ++t)
+      if (!used[t] && t != best) pos[t] -= (pos[t] > i1) + (pos[t] > i0);
+    used[best] = 1;
+    --live;
+    run_pos = live - 1;
+  }
+  return total;
+}
+
 int contraction_order(const std::vector<std::vector<int64_t>>& labels, const std::map<int64_t, int64_t>& dim,
                       int alg, std::vector<std::pair<int, int>>& steps) {
   steps.clear();
   std::vector<std::vector<int64_t>> L = labels;
   const int n = (int)L.size();
+  if (alg == 3) {
+    // the cheaper (in multiply-adds) of the pairwise greedy order and the sweep orders from
+    // every start tensor (at most 64 starts, evenly spaced, for larger networks)
+    contraction_order(labels, dim, 0, steps);
+    double best = order_cost(labels, dim, steps);
+    const DenseNet net = dense_net(labels, dim);
+    const int starts = std::min(n, 64);
+    std::vector<std::pair<int, int>> cand;
+    for (int k = 0; k < starts && n > 1; ++k) {
+      const double cost = sweep_from(net, (int)((int64_t)k * n / starts), cand);
+      if (cost < best) {
+        best = cost;
+        steps = cand;
+      }
+    }
+    return 0;
+  }
   if (alg == 1) {
     // left-associative ((t0 t1) t2) ...: in the shrinking working list the running
     // product sits last; every step contracts it (first operand) with the next input,
@@ -48,12 +168,31 @@ int contraction_order(const std::vector<std::vector<int64_t>>& labels, const std
     for (int k = 2; k < n; ++k) steps.push_back({n - k, 0});
     return 0;
   }
+  // A pair sharing an index always beats one that shares none (k0 below), so while any pair
+  // shares an index only those pairs -- found through the holders of each label -- are
+  // scanned, in the (i, j) order of the full scan: the same choice and tie-breaks as scanning
+  // every pair, in time linear in the number of linked pairs instead of quadratic in n.
   while (L.size() > 1) {
     int bi = -1, bj = -1;
     double bk0 = 0, bk1 = 0, bk2 = 0;
     std::vector<int64_t> blo;
+    std::map<int64_t, std::vector<int>> holders;
     for (int i = 0; i < (int)L.size(); ++i)
-      for (int j = i + 1; j < (int)L.size(); ++j) {
+      for (int64_t x : L[i]) holders[x].push_back(i);
+    std::vector<std::pair<int, int>> linked;
+    for (const auto& kv : holders)
+      for (size_t a = 0; a < kv.second.size(); ++a)
+        for (size_t b = a + 1; b < kv.second.size(); ++b)
+          if (kv.second[a] != kv.second[b])
+            linked.push_back({std::min(kv.second[a], kv.second[b]), std::max(kv.second[a], kv.second[b])});
+    std::sort(linked.begin(), linked.end());
+    linked.erase(std::unique(linked.begin(), linked.end()), linked.end());
+    std::vector<std::pair<int, int>> all_pairs;
+    if (linked.empty())
+      for (int i = 0; i < (int)L.size(); ++i)
+        for (int j = i + 1; j < (int)L.size(); ++j) all_pairs.push_back({i, j});
+    for (const auto& pr : linked.empty() ? all_pairs : linked) {
+        const int i = pr.first, j = pr.second;
         std::vector<int64_t> lo;
         bool shared = false;
         for (int64_t x : L[i]) {

@@ -2535,7 +2535,7 @@ int32_t itn_apply_gates(itn_ctx* c, int32_t dtype, int64_t n_gates, const itn_ga
 int32_t itn_contraction_order(int32_t n, const int32_t* ranks, const int64_t* labels, const int64_t* dims,
                               int32_t alg, int32_t* steps_out) {
   if (!steps_out && n > 1) return ITN_ERR_ARG;
-  if (alg != 0 && alg != 1) return ITN_ERR_ARG;
+  if (alg != 0 && alg != 1 && alg != 3) return ITN_ERR_ARG;
   NetIn net;
   if (int r = read_network(nullptr, n, ranks, labels, dims, net)) return r;
   std::vector<std::pair<int, int>> steps;
@@ -2560,7 +2560,7 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
     return fail(c, ITN_ERR_UNSUPPORTED,
                 "contract_network precision %d needs float32 data (BF16 split or TF32 split)", precision);
   if (!tensors || !out_rank) return fail(c, ITN_ERR_ARG, "null pointer");
-  if (alg != 0 && alg != 1 && alg != 2) return fail(c, ITN_ERR_ARG, "unknown order algorithm %d", alg);
+  if (alg < 0 || alg > 3) return fail(c, ITN_ERR_ARG, "unknown order algorithm %d", alg);
   if (int r = ensure_device(c)) return r;
   NetIn net;
   if (int r = read_network(c, n, ranks, labels, dims, net)) return r;

@@ -11,7 +11,9 @@ namespace itn {
 
 // Pairwise order on a working list: each step (i, j) contracts positions i and j (result
 // labels: free(i) ++ free(j)), removes both and appends the result.  alg 0 = greedy
-// (smallest growth, sharing pairs first), 1 = left-associative.
+// (smallest growth, sharing pairs first), 1 = left-associative, 3 = sweep (the cheaper of the
+// greedy order and running-product sweeps that absorb the neighbour leaving the product
+// smallest, by multiply-adds).
 int contraction_order(const std::vector<std::vector<int64_t>>& labels, const std::map<int64_t, int64_t>& dim,
                       int alg, std::vector<std::pair<int, int>>& steps);
 

@@ -3,8 +3,9 @@
 ``contract_network(tensors, labels; alg, precision)`` contracts a list of tensors whose
 axes carry labels (any hashable): a label on two tensors is summed over, a label on one
 tensor stays open.  The pairwise order is chosen by the library's C++ greedy rule (or
-left-associative, or an explicit step list); every pairwise step runs on the device as a
-permute + GEMM (CUDA cores, or tcgen05 with BF16 hi/lo split operands for float32).
+left-associative, or "sweep": the cheaper of the greedy order and running-product sweeps, or an
+explicit step list); every pairwise step runs on the device as a permute + GEMM (CUDA cores, or
+tcgen05 with BF16 / TF32 hi/lo split operands for float32).
 """
 from __future__ import annotations
 
@@ -15,7 +16,7 @@ import numpy as np
 from . import _lib as L
 from .graphs import Graph
 
-_ALG = {"greedy": 0, "left": 1}
+_ALG = {"greedy": 0, "left": 1, "sweep": 3}
 _PREC = {"native": L.PREC_NATIVE, "bf16": L.PREC_BF16, "tf32x3": L.PREC_TF32X3}
 
 

@@ -392,8 +392,9 @@ end
 
 `contract_network` algorithm (the counterpart of `Exact`, contract_network.jl:7-10) that
 contracts pairwise on the GPU.  `order` is an explicit list of steps in the
-itn_contraction_order format or `nothing`; `order_alg` is `:greedy` or `:left`
-(LeftAssociative); `precision = :bf16` uses tcgen05 BF16 hi/lo products on Float32 data,
+itn_contraction_order format or `nothing`; `order_alg` is `:greedy`, `:left`
+(LeftAssociative) or `:sweep` (the cheaper of the greedy order and running-product boundary
+sweeps: far fewer operations on lattices); `precision = :bf16` uses tcgen05 BF16 hi/lo products on Float32 data,
 `:tf32x3` TF32 hi/lo products (FP32 accuracy on the tensor cores).
 """
 Base.@kwdef struct GPUExact
@@ -445,7 +446,9 @@ function INN.contract_network(alg::GPUExact, tn)
     out = Vector{T}(undef, cap)
     out_labels = zeros(Int64, 48); out_dims = zeros(Int64, 48)
     steps = isnothing(alg.order) ? C_NULL : alg.order
-    order_code = !isnothing(alg.order) ? Int32(2) : alg.order_alg === :left ? Int32(1) : Int32(0)
+    order_code = !isnothing(alg.order) ? Int32(2) : alg.order_alg === :left ? Int32(1) :
+                 alg.order_alg === :sweep ? Int32(3) : alg.order_alg === :greedy ? Int32(0) :
+                 throw(ArgumentError("unknown order_alg $(alg.order_alg)"))
     ctxr = Ref{Ptr{Cvoid}}(C_NULL)
     st = ccall((:itn_create, libitn), Int32, (Ptr{Ptr{Cvoid}}, Int32, Int32), ctxr, alg.device, 0)
     st == ITN_OK || error("itn_create failed with status $st")
