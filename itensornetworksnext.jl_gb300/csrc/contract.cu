@@ -241,6 +241,29 @@ __global__ void permute_tensor_kernel(const T* __restrict__ in, T* __restrict__ 
   }
 }
 
+// The same for tensors of fewer than 2^31 entries: 32-bit index arithmetic (a 64-bit division
+// costs several times a 32-bit one, and a permute of a boundary-sweep product is dominated by
+// its index arithmetic, not its bytes).
+struct PermArgs32 {
+  int rank;
+  int out_dims[kMaxRank];
+  int in_stride[kMaxRank];
+};
+
+template <typename T>
+__global__ void permute_tensor32_kernel(const T* __restrict__ in, T* __restrict__ out, int n, PermArgs32 p) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    int rem = j, off = 0;
+    for (int a = p.rank - 1; a >= 0; --a) {
+      const int d = p.out_dims[a];
+      const int q = rem / d;
+      off += (rem - q * d) * p.in_stride[a];
+      rem = q;
+    }
+    out[j] = in[off];
+  }
+}
+
 // C[M,N] = A[M,K] * B[K,N], row-major, CUDA cores: 64 x 64 tile per CTA, 256 threads,
 // 4 x 4 outputs per thread, K staged through shared memory in slices of 16.
 template <typename T>
@@ -295,25 +318,103 @@ cudaError_t permute_t(const void* in, void* out, const std::vector<int64_t>& in_
                       cudaStream_t st) {
   const int r = (int)in_dims.size();
   if (r > kMaxRank) return cudaErrorInvalidValue;
-  PermArgs p;
-  p.rank = r;
   std::vector<long long> istr(r, 1);
   for (int a = r - 2; a >= 0; --a) istr[a] = istr[a + 1] * in_dims[a + 1];
   long long n = 1;
-  for (int a = 0; a < r; ++a) {
-    p.out_dims[a] = in_dims[perm[a]];
-    p.in_stride[a] = istr[perm[a]];
-    n *= in_dims[a];
-  }
+  for (int a = 0; a < r; ++a) n *= in_dims[a];
   if (n == 0) return cudaSuccess;
+  // merge runs of output axes that are consecutive input axes in the same order (one axis of
+  // the product of their dimensions, strided like the run's innermost axis); unit axes drop
+  std::vector<long long> od, os;
+  for (int a = 0; a < r;) {
+    int b = a;
+    long long d = in_dims[perm[a]];
+    while (b + 1 < r && perm[b + 1] == perm[b] + 1) d *= in_dims[perm[++b]];
+    if (d != 1) {
+      od.push_back(d);
+      os.push_back(istr[perm[b]]);
+    }
+    a = b + 1;
+  }
+  if (od.empty()) {
+    od.push_back(1);
+    os.push_back(1);
+  }
+  const int rank = (int)od.size();
   const int grid = (int)std::min<long long>((n + 255) / 256, 65535);
-  permute_tensor_kernel<T><<<grid, 256, 0, st>>>(reinterpret_cast<const T*>(in), reinterpret_cast<T*>(out), n, p);
+  if (n < (1LL << 31)) {
+    PermArgs32 p;
+    p.rank = rank;
+    for (int a = 0; a < rank; ++a) {
+      p.out_dims[a] = (int)od[a];
+      p.in_stride[a] = (int)os[a];
+    }
+    permute_tensor32_kernel<T><<<grid, 256, 0, st>>>(reinterpret_cast<const T*>(in), reinterpret_cast<T*>(out), (int)n,
+                                                    p);
+  } else {
+    PermArgs p;
+    p.rank = rank;
+    for (int a = 0; a < rank; ++a) {
+      p.out_dims[a] = od[a];
+      p.in_stride[a] = os[a];
+    }
+    permute_tensor_kernel<T><<<grid, 256, 0, st>>>(reinterpret_cast<const T*>(in), reinterpret_cast<T*>(out), n, p);
+  }
   return cudaGetLastError();
+}
+
+// C[M,N] = A[M,K] B[K,N] when one side is thin (at most kThin rows of A or columns of B) and
+// K <= kThinK: the thin operand (at most 32 x 64 entries) is staged in shared memory and each
+// thread computes entries of C directly, grid-stride, consecutive threads on consecutive
+// entries of C, so the long operand's loads are coalesced (SMALL_A) or shared by the threads
+// of one row (SMALL_B) and C's stores are coalesced.  gemm_cc_kernel's 64 x 64 tiles with
+// K slices of 16 would compute mostly padding on such shapes (the steps of a boundary-sweep
+// contraction: M ~ 1e6, N and K ~ 3-18).
+constexpr int kThin = 32, kThinK = 64;
+
+template <typename T, bool SMALL_B>
+__global__ void __launch_bounds__(256) gemm_thin_kernel(const T* __restrict__ A, const T* __restrict__ B,
+                                                        T* __restrict__ C, long long M, long long N, int K) {
+  extern __shared__ __align__(16) unsigned char thin_sm[];
+  T* S = reinterpret_cast<T*>(thin_sm);
+  const long long sn = SMALL_B ? (long long)K * N : M * (long long)K;
+  const T* src = SMALL_B ? B : A;
+  for (long long i = threadIdx.x; i < sn; i += blockDim.x) S[i] = src[i];
+  __syncthreads();
+  const long long total = M * N;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long m = j / N, n = j - m * N;
+    T acc = tzero<T>();
+    if (SMALL_B) {
+      const T* a = A + m * K;
+      for (int k = 0; k < K; ++k) acc = fmac(a[k], S[k * N + n], acc);
+    } else {
+      const T* b = B + n;
+      for (int k = 0; k < K; ++k) acc = fmac(S[m * K + k], b[(long long)k * N], acc);
+    }
+    C[j] = acc;
+  }
 }
 
 template <typename T>
 cudaError_t gemm_t(const void* A, const void* B, void* C, long long M, long long N, long long K, cudaStream_t st) {
   if (M == 0 || N == 0) return cudaSuccess;
+  if (K <= kThinK && (N <= kThin || M <= kThin) && std::max(M, N) >= 256) {
+    const bool small_b = N <= kThin;
+    const size_t smem = (size_t)(small_b ? N : M) * K * sizeof(T);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::max<long long>(1, std::min<long long>((M * N + 255) / 256, (long long)sms * 8));
+    if (small_b)
+      gemm_thin_kernel<T, true><<<grid, 256, smem, st>>>(reinterpret_cast<const T*>(A), reinterpret_cast<const T*>(B),
+                                                        reinterpret_cast<T*>(C), M, N, (int)K);
+    else
+      gemm_thin_kernel<T, false><<<grid, 256, smem, st>>>(reinterpret_cast<const T*>(A), reinterpret_cast<const T*>(B),
+                                                         reinterpret_cast<T*>(C), M, N, (int)K);
+    return cudaGetLastError();
+  }
   const long long tiles = ((N + 63) / 64) * ((M + 63) / 64);
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
   gemm_cc_kernel<T><<<(unsigned)tiles, 256, 0, st>>>(reinterpret_cast<const T*>(A), reinterpret_cast<const T*>(B),

@@ -2622,13 +2622,22 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
         pa.push_back((int)a);
       }
     }
-    for (size_t a = 0; a < A.l.size(); ++a)
-      if (std::find(B.l.begin(), B.l.end(), A.l[a]) != B.l.end()) {
-        shared.push_back(A.l[a]);
-        dsh.push_back(A.d[a]);
-        pa.push_back((int)a);
+    // the shared indices in the larger operand's order, so that only the smaller operand's
+    // permute reorders them (the larger one's keeps its shared axes in place, which is the
+    // identity -- no copy -- when they lead it; in a boundary sweep the larger is the
+    // running product)
+    const bool b_leads = numel(B.d) > numel(A.d);
+    const Item& O = b_leads ? B : A;
+    const Item& P = b_leads ? A : B;
+    for (size_t q = 0; q < O.l.size(); ++q)
+      if (std::find(P.l.begin(), P.l.end(), O.l[q]) != P.l.end()) {
+        shared.push_back(O.l[q]);
+        dsh.push_back(O.d[q]);
       }
-    for (int64_t x : shared) pb.push_back((int)(std::find(B.l.begin(), B.l.end(), x) - B.l.begin()));
+    for (int64_t x : shared) {
+      pa.push_back((int)(std::find(A.l.begin(), A.l.end(), x) - A.l.begin()));
+      pb.push_back((int)(std::find(B.l.begin(), B.l.end(), x) - B.l.begin()));
+    }
     for (size_t b = 0; b < B.l.size(); ++b)
       if (std::find(shared.begin(), shared.end(), B.l[b]) == shared.end()) {
         fb.push_back(B.l[b]);

@@ -158,3 +158,21 @@ def test_tf32_split_tensor_core_gemm_has_fp32_accuracy():
     e, e32 = abs(z - zr) / abs(zr), abs(z32 - zr) / abs(zr)
     print(f"4x4 D=2 norm network (every step stored in FP32): tf32x3 {e:.2e}, fp32 CUDA cores {e32:.2e}")
     assert e <= 1e-5
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex64, np.complex128])
+@pytest.mark.parametrize("m,k,n", [(5000, 9, 7), (7, 9, 5000), (300, 64, 32), (32, 1, 4096), (257, 3, 1)])
+def test_thin_pairwise_contractions(dtype, m, k, n):
+    """Pairwise steps with one thin side (at most 32 rows or columns, K <= 64: the steps of a
+    boundary sweep) run on the thin-operand GEMM; against numpy in FP64 / complex128."""
+    rng = np.random.default_rng(m * 31 + n)
+    a = rng.standard_normal((m, k))
+    b = rng.standard_normal((k, n))
+    if np.dtype(dtype).kind == "c":
+        a = a + 1j * rng.standard_normal((m, k))
+        b = b + 1j * rng.standard_normal((k, n))
+    ref = a @ b
+    out, lab = contract_network([a.astype(dtype), b.astype(dtype)], [["i", "k"], ["k", "j"]])
+    tol = 1e-12 if np.dtype(dtype).itemsize >= 16 or dtype == np.float64 else 1e-5
+    got = out if lab == ["i", "j"] else out.T
+    assert np.max(np.abs(got - ref)) <= tol * np.max(np.abs(ref)) * np.sqrt(k)
