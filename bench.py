@@ -617,7 +617,9 @@ def run_case(name, device=0):
     adjoint update fused into it); gate = one layer of 128 gates (gate_kernel); contract = 2048^3 float32
     contractions in the three precisions (gemm_cc_kernel, gemm_tc_kernel); batched = the
     256-network complex64 batch (sweep_z3_kernel); exact6 = the exact FP64 contraction of the
-    6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>)."""
+    6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>) in the greedy and the sweep
+    order; exact6_sweep = the sweep order alone, twice (permute_tensor32_kernel,
+    gemm_thin_kernel<double>)."""
     from itn_gb300 import BPEngine
     from itn_gb300 import graphs as G
     if name in ("d8", "mixed"):
@@ -658,6 +660,14 @@ def run_case(name, device=0):
         z, _, ms = contract_network(ts, ls, return_time=True)
         print("exact6 log z", float(np.log(z[()])), "device ms", ms)
         z, _, ms = contract_network(ts, ls, alg="sweep", return_time=True)
+        print("exact6 sweep order: log z", float(np.log(z[()])), "device ms", ms)
+    elif name == "exact6_sweep":
+        from itn_gb300.contract import contract_network, norm_network_tensors
+        g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
+        t6 = G.random_tensors(g6, np.random.default_rng(63), np.float64, G.peps_scale(g6))
+        ts, ls = norm_network_tensors(g6, t6)
+        for _ in range(2):
+            z, _, ms = contract_network(ts, ls, alg="sweep", return_time=True)
         print("exact6 sweep order: log z", float(np.log(z[()])), "device ms", ms)
     else:
         raise SystemExit(f"unknown case {name}")
@@ -809,7 +819,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
-    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6"],
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6", "exact6_sweep"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
