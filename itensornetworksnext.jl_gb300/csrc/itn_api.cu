@@ -1777,7 +1777,6 @@ int adjoint_prepare(itn_ctx* c, const void* m, int normalized) {
 // cot = J^T lam for the sweep m -> F(m) (needs adjoint_prepare): lam is projected through
 // the normalisation (mu = (lam - <lam, F>) / S) and pushed back through the products by
 // the dual interpreter (tangent of the leave-one-out contraction on every leg).
-// cot = J^T-product of the dual interpreter for tangents mu already in c->d_mu.
 // Autotuner for the dual launches (the J^T products of the adjoint iteration): time one
 // launch per candidate CTA size -- 64 and 128 threads with the unrestricted kernel, 256 with
 // the 128-register one (two CTAs per SM) -- on tangents from c->d_mu into c->d_cot, and keep
@@ -1827,20 +1826,6 @@ int autotune_dual(itn_ctx* c, const void* m) {
   c->dual_block[c->dtype] = best_b > 0 ? best_b : -1;
   tune_store(c, "dual", {c->dual_block[c->dtype], 0, 0});
   if (getenv("ITN_DEBUG")) fprintf(stderr, "[itn] autotune: dual CTA size %d (%.4f ms)\n", best_b, best);
-  return ITN_OK;
-}
-
-int apply_dual_mu(itn_ctx* c, const void* m, void* cot, const int* done) {
-  const int np = (int)c->items_par.size() / 2;
-  GenericArgs da;
-  LaunchCfg dcfg;
-  if (int r = plan_dual(c, da, dcfg, c->d_items_par.as<int>(), np, m)) return r;
-  DualArgs dd;
-  memset(&dd, 0, sizeof(dd));
-  dd.tan_in = c->d_mu.p;
-  dd.tan_out = cot;
-  dd.done = done;
-  CK(launch_dual(c->dtype, da, dd, dcfg, c->stream));
   return ITN_OK;
 }
 
