@@ -619,7 +619,8 @@ def run_case(name, device=0):
     256-network complex64 batch (sweep_z3_kernel); exact6 = the exact FP64 contraction of the
     6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>) in the greedy and the sweep
     order; exact6_sweep = the sweep order alone, twice (permute_tensor32_kernel,
-    gemm_thin_kernel<double>)."""
+    gemm_thin_kernel<double>); padded = 30-sweep mixed solves of the 16x16 D=4 and 12x12 D=6 open
+    lattices on the zero-padded tensor-core sweep (bp_tc_kernel with PAD, one launch per sweep)."""
     from itn_gb300 import BPEngine
     from itn_gb300 import graphs as G
     if name in ("d8", "mixed"):
@@ -661,6 +662,17 @@ def run_case(name, device=0):
         print("exact6 log z", float(np.log(z[()])), "device ms", ms)
         z, _, ms = contract_network(ts, ls, alg="sweep", return_time=True)
         print("exact6 sweep order: log z", float(np.log(z[()])), "device ms", ms)
+    elif name == "padded":
+        # the padded tensor-core sweep on open lattices (one launch per sweep)
+        for L, D in ((16, 4), (12, 6)):
+            g = G.square_lattice(L, L, D, periodic=False, phys=2)
+            t = G.random_tensors(g, np.random.default_rng(100 * L + D), np.float64, G.peps_scale(g))
+            with BPEngine(g, device=device) as e:
+                e.set_tensors(t.astype(np.float32))
+                for _ in range(2):
+                    e.init_messages()
+                    r = e.run(maxiter=SWEEPS, precision="bf16", split_sweeps=SPLIT_SWEEPS)
+                print(f"padded {L}x{L} D={D} bf16 mixed: device ms {r.device_ms:.4f}, launches {r.kernel_launches}")
     elif name == "exact6_sweep":
         from itn_gb300.contract import contract_network, norm_network_tensors
         g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
@@ -819,7 +831,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
-    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6", "exact6_sweep"],
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6", "exact6_sweep",
+                                                        "padded"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
