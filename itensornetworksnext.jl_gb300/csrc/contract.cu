@@ -397,6 +397,61 @@ __global__ void __launch_bounds__(256) gemm_thin_kernel(const T* __restrict__ A,
   }
 }
 
+// The same product with the long operand read in place, in its own index order: `v` lists its
+// free axes (adjacent ones merged) with their strides and the element offset of each of the K
+// contracted positions.  Saves the permute of the long operand (a read and a write of the whole
+// tensor) at the price of per-entry index arithmetic, which the FP64 product hides.
+template <typename T, bool SMALL_B>
+__global__ void __launch_bounds__(256) gemm_thin_view_kernel(const T* __restrict__ A, const T* __restrict__ B,
+                                                             T* __restrict__ C, long long M, long long N, int K,
+                                                             ThinView v) {
+  extern __shared__ __align__(16) unsigned char thin_sm[];
+  T* S = reinterpret_cast<T*>(thin_sm);
+  const long long sn = SMALL_B ? (long long)K * N : M * (long long)K;
+  long long* koff = reinterpret_cast<long long*>(thin_sm + ((sn * (long long)sizeof(T) + 15) & ~15LL));
+  const T* src = SMALL_B ? B : A;
+  for (long long i = threadIdx.x; i < sn; i += blockDim.x) S[i] = src[i];
+  for (int i = threadIdx.x; i < K; i += blockDim.x) koff[i] = v.koff[i];
+  __syncthreads();
+  const T* L = SMALL_B ? A : B;
+  const long long total = M * N;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long m = j / N, n = j - m * N;
+    long long rem = SMALL_B ? m : n, off = 0;
+    for (int a = v.rank - 1; a >= 0; --a) {
+      const long long d = v.dims[a], q = rem / d;
+      off += (rem - q * d) * v.stride[a];
+      rem = q;
+    }
+    T acc = tzero<T>();
+    if (SMALL_B) {
+      for (int k = 0; k < K; ++k) acc = fmac(L[off + koff[k]], S[k * N + n], acc);
+    } else {
+      for (int k = 0; k < K; ++k) acc = fmac(S[m * K + k], L[off + koff[k]], acc);
+    }
+    C[j] = acc;
+  }
+}
+
+template <typename T>
+cudaError_t gemm_view_t(const void* A, const void* B, void* C, long long M, long long N, long long K, bool small_b,
+                        const ThinView& v, cudaStream_t st) {
+  if (M == 0 || N == 0) return cudaSuccess;
+  const size_t smem = (((size_t)(small_b ? N : M) * K * sizeof(T) + 15) & ~(size_t)15) + (size_t)K * sizeof(long long);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = (int)std::max<long long>(1, std::min<long long>((M * N + 255) / 256, (long long)sms * 8));
+  if (small_b)
+    gemm_thin_view_kernel<T, true><<<grid, 256, smem, st>>>(reinterpret_cast<const T*>(A), reinterpret_cast<const T*>(B),
+                                                           reinterpret_cast<T*>(C), M, N, (int)K, v);
+  else
+    gemm_thin_view_kernel<T, false><<<grid, 256, smem, st>>>(reinterpret_cast<const T*>(A), reinterpret_cast<const T*>(B),
+                                                            reinterpret_cast<T*>(C), M, N, (int)K, v);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t gemm_t(const void* A, const void* B, void* C, long long M, long long N, long long K, cudaStream_t st) {
   if (M == 0 || N == 0) return cudaSuccess;
@@ -429,6 +484,24 @@ cudaError_t contract_permute(int dtype, const void* in, void* out, const std::ve
     case 1: return permute_t<double>(in, out, in_dims, perm, st);
     case 2: return permute_t<c64>(in, out, in_dims, perm, st);
     case 3: return permute_t<c128>(in, out, in_dims, perm, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+bool contract_thin_shape(long long M, long long N, long long K) {
+  return K <= kThinK && (N <= kThin || M <= kThin) && std::max(M, N) >= 256;
+}
+
+bool contract_thin_small_b(long long M, long long N) { return N <= kThin; }
+
+cudaError_t contract_gemm_view(int dtype, const void* A, const void* B, void* C, long long M, long long N,
+                               long long K, bool small_b, const ThinView& v, cudaStream_t st) {
+  if (v.rank > kMaxRank || K > kThinK) return cudaErrorInvalidValue;
+  switch (dtype) {
+    case 0: return gemm_view_t<float>(A, B, C, M, N, K, small_b, v, st);
+    case 1: return gemm_view_t<double>(A, B, C, M, N, K, small_b, v, st);
+    case 2: return gemm_view_t<c64>(A, B, C, M, N, K, small_b, v, st);
+    case 3: return gemm_view_t<c128>(A, B, C, M, N, K, small_b, v, st);
   }
   return cudaErrorInvalidValue;
 }

@@ -2637,11 +2637,59 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
     };
     void *ta = A.p, *tb = B.p, *tc = nullptr;
     cudaError_t e = cudaSuccess;
-    if (!is_id(pa)) {
+    // a thin step whose long operand is not in GEMM order reads that operand in place through a
+    // view (its free axes and contracted positions with their strides) instead of permuting it
+    const bool thin = precision == ITN_PREC_NATIVE && contract_thin_shape(M, N, K);
+    const bool small_b = thin && contract_thin_small_b(M, N);
+    // (int dims in the view: tensors below 2^31 entries)
+    const bool view = thin && !is_id(small_b ? pa : pb) && numel((small_b ? A : B).d) < (1LL << 31);
+    ThinView tv;
+    if (view) {
+      const Item& Lg = small_b ? A : B;
+      std::vector<long long> lstr(Lg.d.size(), 1);
+      for (int q = (int)Lg.d.size() - 2; q >= 0; --q) lstr[q] = lstr[q + 1] * Lg.d[q + 1];
+      std::vector<char> is_sh(Lg.l.size(), 0);
+      std::vector<int> spos;
+      for (int64_t x : shared) {
+        const int q = (int)(std::find(Lg.l.begin(), Lg.l.end(), x) - Lg.l.begin());
+        spos.push_back(q);
+        is_sh[q] = 1;
+      }
+      // contracted positions k, row-major over `shared`
+      for (int k = 0; k < (int)K; ++k) {
+        long long rem = k, off = 0;
+        for (int a = (int)spos.size() - 1; a >= 0; --a) {
+          const long long d = Lg.d[spos[a]];
+          off += (rem % d) * lstr[spos[a]];
+          rem /= d;
+        }
+        tv.koff[k] = off;
+      }
+      // free axes in the operand's order, runs of adjacent free axes merged
+      tv.rank = 0;
+      for (int q = 0; q < (int)Lg.l.size(); ++q) {
+        if (is_sh[q] || Lg.d[q] == 1) continue;
+        const bool merge = tv.rank > 0 && q > 0 && !is_sh[q - 1] && tv.stride[tv.rank - 1] == lstr[q] * Lg.d[q];
+        if (merge) {
+          tv.dims[tv.rank - 1] = (int)(tv.dims[tv.rank - 1] * Lg.d[q]);
+          tv.stride[tv.rank - 1] = lstr[q];
+        } else {
+          tv.dims[tv.rank] = (int)Lg.d[q];
+          tv.stride[tv.rank] = lstr[q];
+          ++tv.rank;
+        }
+      }
+      if (tv.rank == 0) {
+        tv.dims[0] = 1;
+        tv.stride[0] = 1;
+        tv.rank = 1;
+      }
+    }
+    if (!is_id(pa) && !(view && small_b)) {
       e = cudaMallocAsync(&ta, std::max<size_t>((size_t)M * K * es, 16), c->stream);
       if (e == cudaSuccess) e = contract_permute(dtype, A.p, ta, A.d, pa, c->stream);
     }
-    if (e == cudaSuccess && !is_id(pb)) {
+    if (e == cudaSuccess && !is_id(pb) && !(view && !small_b)) {
       e = cudaMallocAsync(&tb, std::max<size_t>((size_t)K * N * es, 16), c->stream);
       if (e == cudaSuccess) e = contract_permute(dtype, B.p, tb, B.d, pb, c->stream);
     }
@@ -2650,6 +2698,8 @@ int32_t itn_contract_network(itn_ctx* c, int32_t dtype, int32_t n, const int32_t
       if (precision == ITN_PREC_BF16 || precision == ITN_PREC_TF32X3)
         e = contract_gemm_tc(reinterpret_cast<const float*>(ta), reinterpret_cast<const float*>(tb),
                              reinterpret_cast<float*>(tc), M, N, K, c->stream, precision == ITN_PREC_TF32X3);
+      else if (view)
+        e = contract_gemm_view(dtype, ta, tb, tc, M, N, K, small_b, tv, c->stream);
       else
         e = contract_gemm(dtype, ta, tb, tc, M, N, K, c->stream);
     }

@@ -22,6 +22,23 @@ cudaError_t contract_permute(int dtype, const void* in, void* out, const std::ve
                              const std::vector<int>& perm, cudaStream_t st);
 
 // C[M,N] = A[M,K] B[K,N] (row-major) on CUDA cores.
+// Thin pairwise steps (at most 32 rows of A or columns of B, K <= 64, the long side >= 256):
+// the long operand can be read in place through a view instead of being permuted first.
+constexpr int kViewMaxRank = 48, kViewMaxK = 64;
+struct ThinView {
+  int rank;                        // free axes of the long operand (adjacent ones merged), outer first
+  int dims[kViewMaxRank];
+  long long stride[kViewMaxRank];  // element strides of those axes in the long operand
+  long long koff[kViewMaxK];       // element offset of each contracted position k (row-major over
+                                   // the contracted axes in the step's order)
+};
+bool contract_thin_shape(long long M, long long N, long long K);
+// true: B is the thin operand (A is read through the view); false: A is thin (B through the view)
+bool contract_thin_small_b(long long M, long long N);
+// C[M,N] = A B with the long operand read through `v` (its pointer in its own layout) and the
+// thin one contiguous ([M,K] row-major A or [K,N] row-major B).
+cudaError_t contract_gemm_view(int dtype, const void* A, const void* B, void* C, long long M, long long N,
+                               long long K, bool small_b, const ThinView& v, cudaStream_t st);
 cudaError_t contract_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K,
                           cudaStream_t st);
 

@@ -176,3 +176,33 @@ def test_thin_pairwise_contractions(dtype, m, k, n):
     tol = 1e-12 if np.dtype(dtype).itemsize >= 16 or dtype == np.float64 else 1e-5
     got = out if lab == ["i", "j"] else out.T
     assert np.max(np.abs(got - ref)) <= tol * np.max(np.abs(ref)) * np.sqrt(k)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex64, np.complex128])
+def test_thin_steps_with_the_long_operand_out_of_order(dtype):
+    """Thin steps whose long operand carries its contracted indices in the middle or first (read
+    in place through a strided view instead of being permuted), with unit and adjacent free
+    axes; against numpy einsum."""
+    rng = np.random.default_rng(5)
+    cases = [
+        # long tensor (a, k, b, c) with k contracted against a thin (k, j)
+        ("akbc,kj->abcj", [(40, 3, 7, 5), (3, 6)]),
+        # contracted axes first and last in the long tensor, thin tensor first in the pair
+        ("jkl,kabcl->jabc", [(4, 3, 2), (3, 9, 1, 30, 2)]),
+        # two contracted axes split around free ones
+        ("kaml,kl->am", [(2, 33, 17, 3), (2, 3)]),
+    ]
+    for spec, shapes in cases:
+        ins, out = spec.split("->")
+        labs = [list(x) for x in ins.split(",")]
+        ts = []
+        for sh in shapes:
+            x = rng.standard_normal(sh)
+            if np.dtype(dtype).kind == "c":
+                x = x + 1j * rng.standard_normal(sh)
+            ts.append(x)
+        ref = np.einsum(spec, *ts)
+        got, lab = contract_network([t.astype(dtype) for t in ts], labs)
+        perm = [lab.index(x) for x in out]
+        tol = 1e-12 if np.dtype(dtype) in (np.float64, np.complex128) else 1e-5
+        assert np.max(np.abs(np.transpose(got, perm) - ref)) <= tol * np.max(np.abs(ref)) * 4, spec
