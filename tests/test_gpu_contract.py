@@ -161,7 +161,8 @@ def test_tf32_split_tensor_core_gemm_has_fp32_accuracy():
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex64, np.complex128])
-@pytest.mark.parametrize("m,k,n", [(5000, 9, 7), (7, 9, 5000), (300, 64, 32), (32, 1, 4096), (257, 3, 1)])
+@pytest.mark.parametrize("m,k,n", [(5000, 9, 7), (7, 9, 5000), (300, 64, 32), (32, 1, 4096), (257, 3, 1),
+                                   (32, 64, 256), (256, 65, 8), (33, 8, 33)])
 def test_thin_pairwise_contractions(dtype, m, k, n):
     """Pairwise steps with one thin side (at most 32 rows or columns, K <= 64: the steps of a
     boundary sweep) run on the thin-operand GEMM; against numpy in FP64 / complex128."""

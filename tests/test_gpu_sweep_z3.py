@@ -77,3 +77,19 @@ def test_grouped_sweep_converged_run():
     assert 1 < r.iterations < 300 and r.at_iteration == r.iterations and r.delta < 1e-10
     ref, _, _, _ = O.bp_run(g, t, G.identity_messages(g, np.complex128), maxiter=r.iterations)
     assert msg_rel(g, m, ref) <= 1e-10
+
+
+def test_contexts_on_one_network_share_the_tuned_shape_bit_for_bit():
+    """The grouped sweep's launch shape is autotuned once per network structure and dtype in a
+    process; a second context on the same network reuses it, so the two solves agree bit for bit
+    (a different shape would change the order of partial sums)."""
+    g, t = _batch(40, (2, 3, 4, 6, 8), 77, np.complex64)
+    out = []
+    for _ in range(2):
+        with BPEngine(g) as e:
+            e.set_tensors(t.astype(np.complex64))
+            e.init_messages()
+            r = e.run(maxiter=12)
+            out.append((r.iterations, e.messages().copy()))
+    assert out[0][0] == out[1][0] == 12
+    np.testing.assert_array_equal(out[0][1], out[1][1])

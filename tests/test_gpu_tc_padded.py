@@ -160,3 +160,40 @@ def test_tc_rejects_unsupported_network():
         with pytest.raises(ItnError) as ei:
             e.run(maxiter=2, precision="bf16")
         assert ei.value.status == 6
+
+
+@pytest.mark.parametrize("prec,split,tol", [("bf16", True, 2e-4), ("tf32x3", False, 1e-5)])
+def test_padded_unnormalised_sweep_against_fp32(prec, split, tol):
+    """SimpleMessageUpdate(normalize = false): the padded sweep stores the raw updates (the
+    dummy legs' [1] messages keep the scale of the unpadded contraction)."""
+    g, t = _network("open8_D8")
+    rng = np.random.default_rng(9)
+    m0 = G.identity_messages(g, np.float32) + 0.05 * G.random_messages(g, rng, np.float32)
+    with BPEngine(g) as e:
+        e.set_tensors(t.astype(np.float32))
+        e.set_messages(m0)
+        e.run(maxiter=1, normalize=False)
+        ref = e.messages()
+        e.set_messages(m0)
+        e.run(maxiter=1, normalize=False, precision=prec, split_sweeps=1 if split else 0)
+        err = msg_rel(g, e.messages(), ref)
+    print(f"unnormalised {prec}: {err:.2e}")
+    assert err <= tol
+
+
+def test_tc_rejects_the_sequential_schedule_and_complex_data():
+    """The tensor-core modes run the parallel schedule on float32 data: anything else is
+    ITN_ERR_UNSUPPORTED before any work."""
+    g = G.square_lattice(4, 4, 2, phys=2)
+    with BPEngine(g) as e:
+        e.set_tensors(np.ones(int(g.toff[-1]), dtype=np.float32))
+        e.init_messages()
+        with pytest.raises(ItnError) as ei:
+            e.run(schedule="sequential", edges=G.tree_edge_sequence(g), maxiter=1, precision="bf16")
+        assert ei.value.status == 6
+    with BPEngine(g) as e:
+        e.set_tensors(np.ones(int(g.toff[-1]), dtype=np.complex64))
+        e.init_messages()
+        with pytest.raises(ItnError) as ei:
+            e.run(maxiter=1, precision="bf16")
+        assert ei.value.status == 6
