@@ -5,9 +5,9 @@ memory pool, a serving process that reserves HBM at start-up), where a cudaMallo
 the library would fail or bypass the pool.  The test hands it device buffers (allocated
 here by torch, standing in for such a pool) and checks its result against the context
 entry point itn_logscalars on two calls in a row -- the second call reuses the shared
-static scratch left by the first.  Tolerances as elsewhere: 1e-10 relative in FP64,
-2e-4 in FP32.  Collected last on purpose (file name) so a stop-at-first-failure run has
-already run every other test.
+static scratch left by the first -- and, in FP64, against the CPU oracle.  Tolerances as
+elsewhere: 1e-10 relative in FP64, 2e-4 in FP32.  Collected last on purpose (file name) so a
+stop-at-first-failure run has already run every other test.
 """
 import ctypes
 
@@ -78,6 +78,22 @@ def test_static_scratch_matches_logscalars(lib, dtype, tol):
         # complex: the imaginary part of a sum of logs is defined modulo 2 pi
         dim = np.angle(np.exp(1j * (total[1] - ref["totals"][0][1])))
         assert abs(dim) <= tol * max(1.0, abs(ref["totals"][0][1]))
+
+
+def test_static_scratch_against_the_fp64_oracle(lib):
+    """The same log-norm against the CPU oracle's FP64 restatement of bethe_free_energy
+    (messagecache.jl:185-201) on the same tensors and messages, within 1e-10 relative, on two
+    calls in a row."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as O
+    rng = np.random.default_rng(17)
+    g = G.square_lattice(5, 5, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    m, _, _, _ = O.bp_run(g, t, G.identity_messages(g), maxiter=20)
+    ref = O.logscalars(g, t, m)["total"][0]
+    for total, flags in _static_logz(lib, torch, g, t, m, L.F64):
+        assert flags == 0
+        assert abs(total[0] - ref) <= 1e-10 * abs(ref)
 
 
 def test_static_scratch_flags_vertices_it_cannot_contract(lib):
