@@ -415,7 +415,8 @@ class _Flat:
 # ---- algorithms --------------------------------------------------------------------------------
 @dataclass
 class Exact:
-    """contract_network's exact algorithm (contract_network.jl:7-10)."""
+    """contract_network's exact algorithm (contract_network.jl:7-10); order_alg is Greedy()
+    (the default), LeftAssociative(), Sweep() or the strings "greedy" / "left" / "sweep"."""
     order: object = None
     order_alg: str = "greedy"
 
@@ -426,6 +427,12 @@ class Greedy:
 
 class LeftAssociative:
     pass
+
+
+class Sweep:
+    """Order algorithm of this library (no counterpart in the reference): the cheaper, in
+    multiply-adds, of the greedy order and running-product orders that absorb at every step the
+    tensor leaving the product smallest -- boundary sweeps on lattices."""
 
 
 @dataclass
@@ -648,6 +655,8 @@ def contract_network(tn, alg=None):
         order_alg = "greedy"
     elif isinstance(order_alg, LeftAssociative):
         order_alg = "left"
+    elif isinstance(order_alg, Sweep):
+        order_alg = "sweep"
     kw = dict(alg=order_alg) if alg.order is None else dict(steps=alg.order)
     data, labels = _contract_arrays([t.data for t in ts], [list(t.dimnames) for t in ts], **kw)
     dims = {}

@@ -189,7 +189,9 @@ def test_contract_network_orders():
     D = N.itensor(np.array([-2.0, 3.0, 4.0, 5.0, 1.0]), k)
     r1 = N.contract_network([A, B, C, D], alg=N.Exact(order_alg=N.LeftAssociative()))
     r2 = N.contract_network([A, B, C, D], alg=N.Exact(order_alg=N.Greedy()))
+    r3 = N.contract_network([A, B, C, D], alg=N.Exact(order_alg=N.Sweep()))
     assert np.array_equal(r1.data, r2.data)
+    assert np.allclose(r3.data, r2.data, rtol=1e-14, atol=0)
 
 
 def test_edge_scalars_of_a_norm_network_cache():
