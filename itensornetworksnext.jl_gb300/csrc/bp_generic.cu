@@ -622,6 +622,44 @@ __device__ __forceinline__ void dispatch_absorb_dual(const T* src, const T* srcT
 
 __device__ void adj_step_dev(AdjState* s);
 
+// Grid-wide barrier of the persistent adjoint loop (a cooperative launch, every CTA resident):
+// each CTA arrives once, the last to arrive advances the generation.  The wait is bounded by
+// elapsed time (globaltimer, checked every 64 polls) and gives up early once another CTA has
+// raised gr->err; false means the loop must stop.
+__device__ bool adj_grid_barrier(AdjGrid* gr, unsigned long long wait_ns) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = &gr->gen;
+    const unsigned g0 = *gen;
+    __threadfence();
+    if (atomicAdd(&gr->count, 1u) == gridDim.x - 1) {
+      gr->count = 0;
+      __threadfence();
+      atomicAdd(&gr->gen, 1u);
+    } else {
+      const uint64_t t0 = ptx::globaltimer();
+      for (unsigned polls = 1; *gen == g0; ++polls) {
+        if (*reinterpret_cast<volatile int*>(&gr->err)) {
+          ok = 0;
+          break;
+        }
+        if ((polls & 63) == 0 && ptx::globaltimer() - t0 > wait_ns) {
+          atomicExch(&gr->err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
 // MINB = 2: at most 128 registers, so that two CTAs of 256 threads share an SM (the
 // autotuner's 256-thread candidate); MINB = 1 for CTAs of up to 128 threads.
 template <typename T, int MINB>
@@ -638,7 +676,9 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
   LegMeta* meta = reinterpret_cast<LegMeta*>(smem + L.meta);
   const T* tens = reinterpret_cast<const T*>(a.tens);
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
-  const T* tin = reinterpret_cast<const T*>(d.tan_in);
+  // persistent adjoint loop: the first iteration's tangents are mu_buf[0]
+  const bool persist = d.grid != nullptr;
+  const T* tin = reinterpret_cast<const T*>(persist ? d.mu_buf[0] : d.tan_in);
   const int half = a.msg_cap / 2;
   if (d.done && *reinterpret_cast<const volatile int*>(d.done)) return;
   if (threadIdx.x == 0) {
@@ -675,6 +715,19 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
       if (threadIdx.x == 0) meta->phase ^= 1;
     }
     __syncthreads();
+    for (int iter = 0;; ++iter) {
+    T* const mu_next = reinterpret_cast<T*>(persist ? d.mu_buf[(iter + 1) & 1] : d.mu_next);
+    if (persist && iter > 0) {
+      // the site tensor and the value messages stay staged; this iteration's tangents
+      const T* tk = reinterpret_cast<const T*>(d.mu_buf[iter & 1]);
+      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+        const int l = staged_leg(meta, j);
+        const int Dl = meta->dims[l], jl = j - meta->moffs[l];
+        const int jj = d.transpose ? (jl % Dl) * Dl + jl / Dl : jl;
+        msgs[half + j] = tk[meta->tsrc[l] + jj];
+      }
+      __syncthreads();
+    }
     const int nops = (int)prog[0];
     for (int q = 1; q <= nops; ++q) {
       const unsigned op = prog[q];
@@ -713,7 +766,7 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
           }
           dot = block_sum(dot, red);
           const T is = T(1) / reinterpret_cast<const T*>(d.S)[slot];
-          T* mu = reinterpret_cast<T*>(d.mu_next) + o0;
+          T* mu = mu_next + o0;
           for (int e = threadIdx.x; e < D * D; e += blockDim.x) mu[e] = (lam[e] - dot) * is;
         } else {
           T* dst = reinterpret_cast<T*>(d.tan_out) + a.moff[slot];
@@ -737,8 +790,41 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
       }
     }
     __syncthreads();
+    if (!persist) break;
+    // end of a persistent iteration: fold this iteration's maxima into slot iter % 3, wait for
+    // every CTA, then every CTA applies the same stopping rule to the same maxima
+    const int k3 = iter % 3;
+    for (int o = 16; o >= 1; o >>= 1) {
+      adj_dmax = fmax(adj_dmax, __shfl_xor_sync(0xffffffffu, adj_dmax, o));
+      adj_lmax = fmax(adj_lmax, __shfl_xor_sync(0xffffffffu, adj_lmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&d.grid->dmax[k3], enc_double(adj_dmax));
+      atomicMax(&d.grid->lmax[k3], enc_double(adj_lmax));
+    }
+    adj_dmax = adj_lmax = 0;
+    __threadfence();
+    // (fault injection: CTA 0 leaves without arriving, so the others' waits run out)
+    if (d.stall && iter == 0 && blockIdx.x == 0) break;
+    if (!adj_grid_barrier(d.grid, d.wait_ns)) break;
+    const double dm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->dmax[k3])),
+                 lm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->lmax[k3]));
+    const double r = lm > 0 ? dm / lm : 0.0;
+    const int its = iter + 1;
+    const bool nan_r = r != r;
+    const bool stop = nan_r || r < d.adj->tol || its >= d.adj->maxiter;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      d.adj->iters = its;
+      d.adj->resid = r;
+      if (nan_r) d.adj->nan = 1;
+      if (stop) d.adj->done = 1;
+      d.grid->dmax[(iter + 2) % 3] = d.grid->lmax[(iter + 2) % 3] = enc_double(0.0);
+      __threadfence();
+    }
+    if (stop) break;
+    }  // persistent iterations
   }
-  if (d.adj) {
+  if (d.adj && !persist) {
     // fold max |lambda_new - lambda| and max |lambda_new| into the state (order-encoded); the
     // last CTA to finish runs the stopping rule (a stopped loop returns at once in every CTA,
     // so the ticket stays at zero)
@@ -1743,6 +1829,34 @@ cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, cons
     return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_dual_persistent(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg,
+                                   cudaStream_t st) {
+  if (cfg.grid <= 0 || cfg.grid != a.n_items || !d.grid) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.gridDim = dim3(cfg.grid);
+  lc.blockDim = dim3(cfg.block);
+  lc.dynamicSmemBytes = cfg.smem;
+  lc.stream = st;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (dtype == DT_F32) {
+    auto k = dual_kernel_for<float>(cfg.block);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&lc, k, a, d);
+  }
+  if (dtype == DT_F64) {
+    auto k = dual_kernel_for<double>(cfg.block);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&lc, k, a, d);
+  }
+  return cudaErrorInvalidValue;
 }
 
 int dual_max_active(int dtype, int block, size_t smem) {

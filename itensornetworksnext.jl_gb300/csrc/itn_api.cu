@@ -222,7 +222,8 @@ struct itn_ctx {
   std::vector<int> slot_dst, slot_eidx;  // per slot: destination vertex, undirected edge index
   DevBuf d_slot_dst, d_slot_eidx;
   // gradient work buffers
-  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_mu2, d_cot, d_adj;
+  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_mu2, d_cot, d_adj, d_adjgrid;
+  bool no_persist_adj = false;  // itn_inject_fault(ITN_FAULT_NO_PERSISTENT_ADJOINT)
   DevBuf d_ckpt, d_seg;  // unrolled gradient: kept sweep states, recomputed segment
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
@@ -524,6 +525,9 @@ int32_t itn_inject_fault(itn_ctx* c, int32_t kind, int64_t value) {
     case ITN_FAULT_ALLOC:
       if (value < 0) return fail(c, ITN_ERR_ARG, "allocation failure count < 0");
       t_fail_allocs = value;
+      return ITN_OK;
+    case ITN_FAULT_NO_PERSISTENT_ADJOINT:
+      c->no_persist_adj = value != 0;
       return ITN_OK;
   }
   return fail(c, ITN_ERR_ARG, "unknown fault kind %d", kind);
@@ -2118,7 +2122,49 @@ int32_t itn_bp_grad(itn_ctx* c, const itn_grad_opts* o, void* grad, itn_grad_res
     snprintf(tail, sizeof(tail), " fused %d %d %d %p %p %p %p %p %p %p %p %p", dt, o->normalized, ns, m,
              c->d_mu2.p, c->d_mu.p, c->d_lam.p, c->d_g.p, c->d_F.p, c->d_S.p, (void*)adj, c->d_moff.p);
     key += tail;
-    for (int issued = 0; issued < maxit;) {
+    // The whole loop as one cooperative launch when every work item gets its own resident CTA:
+    // the site tensors and value messages are staged once, and a grid barrier with the stopping
+    // rule replaces the launch boundary and the host checks between chunks (the same
+    // arithmetic, iteration for iteration).  Otherwise (or when the launch is refused) chunks
+    // of captured launches as below.
+    bool persisted = false;
+    const int n_par = (int)c->items_par.size() / 2;
+    if (!c->no_persist_adj && maxit > 0 && n_par > 0 && pc.grid == n_par &&
+        (int64_t)dual_max_active(dt, pc.block, pc.smem) * c->sm_count >= n_par) {
+      CK(c->d_adjgrid.ensure(sizeof(AdjGrid)));
+      AdjGrid hg;
+      memset(&hg, 0, sizeof(hg));
+      for (int q = 0; q < 3; ++q) hg.dmax[q] = hg.lmax[q] = 0x8000000000000000ull;  // encoded 0.0
+      CK(cudaMemcpyAsync(c->d_adjgrid.p, &hg, sizeof(hg), cudaMemcpyHostToDevice, c->stream));
+      DualArgs dd;
+      memset(&dd, 0, sizeof(dd));
+      dd.done = &adj->done;
+      dd.adj = adj;
+      dd.g = c->d_g.p;
+      dd.lam = c->d_lam.p;
+      dd.F = c->d_F.p;
+      dd.S = c->d_S.p;
+      dd.normalize = o->normalized;
+      dd.grid = c->d_adjgrid.as<AdjGrid>();
+      dd.mu_buf[0] = c->d_mu.p;
+      dd.mu_buf[1] = c->d_mu2.p;
+      dd.wait_ns = c->wait_ns;
+      dd.stall = c->stall;
+      cudaError_t e = launch_dual_persistent(dt, pa, dd, pc, c->stream);
+      if (e == cudaSuccess) {
+        persisted = true;
+        AdjGrid hgo;
+        CK(cudaMemcpyAsync(&hs, adj, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(&hgo, c->d_adjgrid.p, sizeof(hgo), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (hgo.err) return fail(c, ITN_ERR_TIMEOUT, "adjoint iteration: a grid-barrier wait gave up");
+      } else if (e == cudaErrorCooperativeLaunchTooLarge) {
+        cudaGetLastError();
+      } else {
+        return cuda_fail(c, e, "persistent adjoint launch");
+      }
+    }
+    for (int issued = 0; !persisted && issued < maxit;) {
       const int chunk = std::min(maxit - issued, kAdjChunk);
       adj_k = issued;  // even: the chunk starts reading mu buffer 0
       if (chunk == kAdjChunk) {

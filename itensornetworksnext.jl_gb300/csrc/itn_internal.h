@@ -59,6 +59,7 @@ struct GenericArgs {
 
 // Extra arguments of the dual-number (forward-mode) interpreter used by the gradient.
 struct AdjState;
+struct AdjGrid;
 
 struct DualArgs {
   const void* tan_in;  // tangent per outgoing slot (mu_{u->v}); null = zero tangents
@@ -81,6 +82,25 @@ struct DualArgs {
   const void* S;
   void* mu_next;
   int normalize;
+  // Persistent adjoint loop (grid != null; one work item per CTA, every CTA resident): the
+  // launch runs iteration after iteration of the fused update, mu alternating between mu_buf[0]
+  // (read first) and mu_buf[1], with a grid barrier and the stopping rule between iterations;
+  // the site tensor and the value messages are staged once.
+  struct AdjGrid* grid;
+  void* mu_buf[2];
+  unsigned long long wait_ns;  // limit of one grid-barrier wait (the loop stops with grid->err)
+  int stall;                   // fault injection: CTA 0 never arrives at the first barrier
+};
+
+// Device state of the persistent adjoint loop (zeroed before each launch): the grid barrier
+// (arrivals and generation) and the maxima of the iterations in three rotating slots (slot
+// k % 3 is filled in iteration k, read by every CTA after the barrier that ends it, and
+// cleared by CTA 0 for iteration k + 2 -- by then every CTA has read it).
+struct AdjGrid {
+  unsigned count, gen;
+  unsigned long long dmax[3], lmax[3];
+  int err;  // a grid-barrier wait ran out
+  int pad_;
 };
 
 // Device-side state of the adjoint fixed-point iteration lambda <- g + J^T lambda: the dual
@@ -139,6 +159,10 @@ cudaError_t launch_permute(int dtype, int nv, const long long* soff, const long 
 cudaError_t launch_dual(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg,
                         cudaStream_t st);
 int dual_max_active(int dtype, int block, size_t smem);
+// The whole adjoint loop as one cooperative launch (d.grid set, cfg.grid == n_items CTAs all
+// resident); cudaErrorCooperativeLaunchTooLarge when they do not fit.
+cudaError_t launch_dual_persistent(int dtype, const GenericArgs& a, const DualArgs& d, const LaunchCfg& cfg,
+                                   cudaStream_t st);
 cudaError_t launch_grad_prep(int dtype, const long long* moff, int nslots, const void* U, void* F, void* S,
                              int normalize, cudaStream_t st);
 cudaError_t launch_grad_g(int dtype, const long long* moff, const int* rev, const int* dst_vertex,

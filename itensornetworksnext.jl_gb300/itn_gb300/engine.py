@@ -229,8 +229,11 @@ class BPEngine:
         """Test hook (itn_inject_fault): ``"wait_ns"`` sets the elapsed-time limit of the
         tensor-core sweep's waits on other items' messages (<= 0: the default); ``"stall"``
         (1 / 0) makes one such wait look for a message that is never written; ``"alloc"``
-        makes the next ``value`` device allocations on this thread fail."""
-        k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC, "stall": L.FAULT_STALL}[kind]
+        makes the next ``value`` device allocations on this thread fail;
+        ``"no_persistent_adjoint"`` (1 / 0) runs the gradient's adjoint iteration as one launch
+        per iteration instead of one persistent launch."""
+        k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC, "stall": L.FAULT_STALL,
+             "no_persistent_adjoint": L.FAULT_NO_PERSISTENT_ADJOINT}[kind]
         self._check(self.lib.itn_inject_fault(self._ctx, k, int(value)))
 
     def tc_selftest(self) -> dict:

@@ -262,3 +262,54 @@ def test_unrolled_gradient_at_a_fixed_point_matches_the_implicit_one():
         gu, _ = e.grad(sweeps=60, checkpoint=8)
         np.testing.assert_allclose(e.messages(), mstar, rtol=0, atol=1e-12)
     assert np.max(np.abs(gu - gi)) <= 1e-8 * np.max(np.abs(gi))
+
+
+@pytest.mark.parametrize("dtype,L_,D", [(np.float32, 12, 6), (np.float64, 5, 3)])
+def test_persistent_adjoint_equals_per_iteration_launches(dtype, L_, D):
+    """The adjoint iteration as one persistent cooperative launch (tensors and value messages
+    staged once, a grid barrier and the stopping rule between iterations) and as one launch
+    per iteration run the same arithmetic: same iteration count, residual and gradient, bit for
+    bit."""
+    rng = np.random.default_rng(31)
+    g = G.square_lattice(L_, L_, D, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g)).astype(dtype)
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=500, tol=1e-12)
+        g_p, i_p = e.grad(adjoint=True, tol=1e-6)
+        e.inject_fault("no_persistent_adjoint", 1)
+        g_l, i_l = e.grad(adjoint=True, tol=1e-6)
+        e.inject_fault("no_persistent_adjoint", 0)
+        g_p2, _ = e.grad(adjoint=True, tol=1e-6)
+    print(f"{L_}x{L_} D={D} {np.dtype(dtype).name}: persistent {i_p['device_ms']:.3f} ms, "
+          f"per-iteration launches {i_l['device_ms']:.3f} ms, {i_p['adjoint_iterations']} iterations")
+    assert i_p["adjoint_iterations"] == i_l["adjoint_iterations"] >= 2
+    assert i_p["adjoint_residual"] == i_l["adjoint_residual"]
+    np.testing.assert_array_equal(g_p, g_l)
+    np.testing.assert_array_equal(g_p, g_p2)
+
+
+def test_persistent_adjoint_barrier_that_runs_out_reports_timeout():
+    """Fault injection without a GPU fault: one CTA of the persistent adjoint launch leaves
+    before the first grid barrier, the others' bounded waits (1 ms) run out, itn_bp_grad
+    returns ITN_ERR_TIMEOUT, and the same context then computes the gradient normally."""
+    from itn_gb300 import ItnError
+    from itn_gb300 import _lib as L
+    rng = np.random.default_rng(32)
+    g = G.square_lattice(6, 6, 3, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, np.float64, G.peps_scale(g))
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.init_messages()
+        e.run(maxiter=500, tol=1e-12)
+        want, _ = e.grad(adjoint=True, tol=1e-8)
+        e.inject_fault("wait_ns", 1_000_000)
+        e.inject_fault("stall", 1)
+        with pytest.raises(ItnError) as ei:
+            e.grad(adjoint=True, tol=1e-8)
+        assert ei.value.status == L.ITN_ERR_TIMEOUT
+        e.inject_fault("stall", 0)
+        e.inject_fault("wait_ns", 0)
+        got, _ = e.grad(adjoint=True, tol=1e-8)
+    np.testing.assert_array_equal(got, want)
