@@ -337,8 +337,15 @@ int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int
  * before the first grid barrier, the others' waits (limit ITN_FAULT_WAIT_NS) run out and
  * itn_bp_grad returns ITN_ERR_TIMEOUT.  ITN_FAULT_NO_PERSISTENT_ADJOINT (value 1 / 0): the
  * adjoint iteration runs as one launch per iteration instead of one persistent launch (the
- * same arithmetic; lets a test compare the two). */
-enum { ITN_FAULT_WAIT_NS = 1, ITN_FAULT_ALLOC = 2, ITN_FAULT_STALL = 3, ITN_FAULT_NO_PERSISTENT_ADJOINT = 4 };
+ * same arithmetic; lets a test compare the two).  ITN_FAULT_NO_PERSISTENT_SWEEPS (value 1 / 0):
+ * the same for the CUDA-core parallel sweeps of small two-layer networks. */
+enum {
+  ITN_FAULT_WAIT_NS = 1,
+  ITN_FAULT_ALLOC = 2,
+  ITN_FAULT_STALL = 3,
+  ITN_FAULT_NO_PERSISTENT_ADJOINT = 4,
+  ITN_FAULT_NO_PERSISTENT_SWEEPS = 5
+};
 int32_t itn_inject_fault(itn_ctx *ctx, int32_t kind, int64_t value);
 
 /* Diagnostic with no counterpart in the reference: runs a one-CTA tcgen05 BF16 product

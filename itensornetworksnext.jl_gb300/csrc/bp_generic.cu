@@ -365,16 +365,55 @@ __device__ void final_rt(const T* __restrict__ src, const T* __restrict__ A, int
 // Normalise out (D*D entries in shared memory) by its sum, store it to global memory
 // and, when requested, record the convergence value against the previous message.
 // Executed by warp 0.
+// Grid-wide barrier of a persistent cooperative launch (every CTA resident): each CTA arrives
+// once, the last to arrive advances the generation.  The wait is bounded by elapsed time
+// (globaltimer, checked every 64 polls) and gives up early once another CTA has raised *err;
+// false means the launch must stop.
+__device__ bool grid_barrier(unsigned* count, unsigned* gen_p, int* err, unsigned long long wait_ns) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = gen_p;
+    const unsigned g0 = *gen;
+    __threadfence();
+    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+      *count = 0;
+      __threadfence();
+      atomicAdd(gen_p, 1u);
+    } else {
+      const uint64_t t0 = ptx::globaltimer();
+      for (unsigned polls = 1; *gen == g0; ++polls) {
+        if (*reinterpret_cast<volatile int*>(err)) {
+          ok = 0;
+          break;
+        }
+        if ((polls & 63) == 0 && ptx::globaltimer() - t0 > wait_ns) {
+          atomicExch(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
 template <typename T>
-__device__ void store_message(const GenericArgs& a, const T* out, int n, int slot) {
+__device__ void store_message(const GenericArgs& a, const T* out, int n, int slot, const void* msg_in,
+                              void* msg_out, unsigned long long* dmax, int* nanf) {
   const int lane = threadIdx.x & 31;
   if (threadIdx.x >= 32) return;
   T s = tzero<T>();
   for (int j = lane; j < n; j += 32) s = add(s, out[j]);
   s = warp_sum(s);
   const bool scale = a.normalize && !is_zero(s);
-  T* dst = reinterpret_cast<T*>(a.msg_out) + a.moff[slot];
-  const T* old = reinterpret_cast<const T*>(a.msg_in) + a.moff[slot];
+  T* dst = reinterpret_cast<T*>(msg_out) + a.moff[slot];
+  const T* old = reinterpret_cast<const T*>(msg_in) + a.moff[slot];
   double n1 = 0, n2 = 0, dre = 0, dim = 0;
   for (int j = lane; j < n; j += 32) {
     T v = scale ? divx(out[j], s) : out[j];
@@ -396,9 +435,9 @@ __device__ void store_message(const GenericArgs& a, const T* out, int n, int slo
     if (lane == 0) {
       const double val = 1.0 - (dre * dre + dim * dim) / (n1 * n2);
       a.slot_diff[slot] = val;
-      if (a.conv) {
-        if (val != val) atomicExch(&a.conv->nan_flag, 1);
-        else atomicMax(&a.conv->dmax, enc_double(val));
+      if (dmax) {
+        if (val != val) atomicExch(nanf, 1);
+        else atomicMax(dmax, enc_double(val));
         __threadfence();
       }
     }
@@ -477,6 +516,8 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
   const T* min_ = reinterpret_cast<const T*>(a.msg_in);
 
   if (a.conv && *reinterpret_cast<const volatile int*>(&a.conv->done)) return;
+  const bool persist = a.pgrid != nullptr;
+  const int base_iter = persist && a.conv ? a.conv->counter : 0;
   if (threadIdx.x == 0) {
     ptx::mbar_init(&meta->bar, 1);
     ptx::fence_mbar_init();
@@ -498,9 +539,10 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
     if (!bulk)
       for (int j = threadIdx.x; j < n; j += blockDim.x) A[j] = A_g[j];
     const int s0 = meta->s0;
+    const T* min0 = persist ? reinterpret_cast<const T*>(a.msg_buf[0]) : min_;
     for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
       const int l = staged_leg(meta, j);
-      msgs[j] = min_[meta->msrc[l] + (j - meta->moffs[l])];
+      msgs[j] = min0[meta->msrc[l] + (j - meta->moffs[l])];
     }
     if (bulk) {
       // bounded wait; on timeout the copy is re-done with plain loads
@@ -510,6 +552,21 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
       if (threadIdx.x == 0) meta->phase ^= 1;
     }
     __syncthreads();
+    for (int sw = 0;; ++sw) {
+    // sweep sw of a persistent launch reads msg_buf[sw & 1] and writes msg_buf[(sw + 1) & 1]
+    const void* io_in = persist ? a.msg_buf[sw & 1] : a.msg_in;
+    void* io_out = persist ? a.msg_buf[(sw + 1) & 1] : a.msg_out;
+    unsigned long long* io_dmax = persist ? &a.pgrid->dmax[sw % 3] : a.conv ? &a.conv->dmax : nullptr;
+    int* io_nan = persist ? &a.pgrid->nanf[sw % 3] : a.conv ? &a.conv->nan_flag : nullptr;
+    if (persist && sw > 0) {
+      // the site tensor stays staged; this sweep's incoming messages
+      const T* mk = reinterpret_cast<const T*>(io_in);
+      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+        const int l = staged_leg(meta, j);
+        msgs[j] = mk[meta->msrc[l] + (j - meta->moffs[l])];
+      }
+      __syncthreads();
+    }
     const int nops = (int)prog[0];
     for (int q = 1; q <= nops; ++q) {
       const unsigned op = prog[q];
@@ -524,7 +581,7 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
       } else if (type == OP_FINAL) {
         const int D = meta->dims[leg];
         dispatch_final<T>(src, A, meta->outer[leg], D, meta->inner[leg], out, red);
-        store_message<T>(a, out, D * D, s0 + leg);
+        store_message<T>(a, out, D * D, s0 + leg, io_in, io_out, io_dmax, io_nan);
         __syncthreads();
       } else {  // OP_FULL
         T acc = tzero<T>();
@@ -535,8 +592,41 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
       }
     }
     __syncthreads();
+    if (!persist) break;
+    // end of a persistent sweep: wait for every CTA, then every CTA takes the outer-loop step
+    // of conv_step from this sweep's diff maximum (the same decision everywhere)
+    if (!grid_barrier(&a.pgrid->count, &a.pgrid->gen, &a.pgrid->err, a.wait_ns)) break;
+    const int k3 = sw % 3;
+    const int iter = base_iter + sw + 1;
+    const bool last = sw + 1 >= a.nsweeps;
+    double delta = 0.0;
+    bool conv_now = false;
+    if (a.conv && a.conv->use_tol) {
+      delta = *reinterpret_cast<volatile int*>(&a.pgrid->nanf[k3])
+                  ? nan("")
+                  : dec_double(*reinterpret_cast<volatile unsigned long long*>(&a.pgrid->dmax[k3]));
+      conv_now = delta < a.conv->tol;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (a.conv) {
+        a.conv->counter = iter;
+        a.conv->iters = iter;
+        if (a.conv->use_tol) {
+          a.conv->delta = delta;
+          if (conv_now) {
+            a.conv->done = 1;
+            a.conv->at_iter = iter;
+          }
+        }
+      }
+      a.pgrid->dmax[(sw + 2) % 3] = enc_double(-INFINITY);
+      a.pgrid->nanf[(sw + 2) % 3] = 0;
+      __threadfence();
+    }
+    if (last || conv_now) break;
+    }  // persistent sweeps
   }
-  if (a.conv && a.fused_step) conv_finish_cta(a.conv);
+  if (a.conv && a.fused_step && !persist) conv_finish_cta(a.conv);
 }
 
 // ---- dual-number interpreter (real types): value and tangent planes ------------------------
@@ -622,42 +712,9 @@ __device__ __forceinline__ void dispatch_absorb_dual(const T* src, const T* srcT
 
 __device__ void adj_step_dev(AdjState* s);
 
-// Grid-wide barrier of the persistent adjoint loop (a cooperative launch, every CTA resident):
-// each CTA arrives once, the last to arrive advances the generation.  The wait is bounded by
-// elapsed time (globaltimer, checked every 64 polls) and gives up early once another CTA has
-// raised gr->err; false means the loop must stop.
+// Grid-wide barrier of the persistent adjoint loop (see grid_barrier).
 __device__ bool adj_grid_barrier(AdjGrid* gr, unsigned long long wait_ns) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    volatile unsigned* gen = &gr->gen;
-    const unsigned g0 = *gen;
-    __threadfence();
-    if (atomicAdd(&gr->count, 1u) == gridDim.x - 1) {
-      gr->count = 0;
-      __threadfence();
-      atomicAdd(&gr->gen, 1u);
-    } else {
-      const uint64_t t0 = ptx::globaltimer();
-      for (unsigned polls = 1; *gen == g0; ++polls) {
-        if (*reinterpret_cast<volatile int*>(&gr->err)) {
-          ok = 0;
-          break;
-        }
-        if ((polls & 63) == 0 && ptx::globaltimer() - t0 > wait_ns) {
-          atomicExch(&gr->err, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
+  return grid_barrier(&gr->count, &gr->gen, &gr->err, wait_ns);
 }
 
 // MINB = 2: at most 128 registers, so that two CTAs of 256 threads share an SM (the
@@ -999,7 +1056,8 @@ __global__ void __launch_bounds__(256) bp1_kernel(GenericArgs a) {
         if (threadIdx.x == 0) out[k] = acc;
       }
       __syncthreads();
-      store_message<T>(a, out, Dv, s0 + v);
+      store_message<T>(a, out, Dv, s0 + v, a.msg_in, a.msg_out, a.conv ? &a.conv->dmax : nullptr,
+                       a.conv ? &a.conv->nan_flag : nullptr);
       __syncthreads();
     }
   }
@@ -1428,6 +1486,44 @@ int generic_max_active(int dtype, int layers, int block, size_t smem) {
 
 cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
   ITN_DISPATCH(dtype, return launch_generic_t<T>(a, cfg, st));
+}
+
+__global__ void sweep_grid_init_kernel(SweepGrid* g) {
+  if (threadIdx.x == 0) {
+    g->count = 0;
+    g->gen = 0;
+    for (int k = 0; k < 3; ++k) {
+      g->dmax[k] = enc_double(-INFINITY);
+      g->nanf[k] = 0;
+    }
+    g->err = 0;
+  }
+}
+
+template <typename T>
+cudaError_t launch_generic_persistent_t(const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
+  if (a.layers != 2 || !a.pgrid || cfg.grid != a.n_items || a.n_items <= 0) return cudaErrorInvalidValue;
+  sweep_grid_init_kernel<<<1, 32, 0, st>>>(a.pgrid);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  auto k = bp2_kernel<T>;
+  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.gridDim = dim3(cfg.grid);
+  lc.blockDim = dim3(cfg.block);
+  lc.dynamicSmemBytes = cfg.smem;
+  lc.stream = st;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, k, a);
+}
+
+cudaError_t launch_generic_persistent(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
+  ITN_DISPATCH(dtype, return launch_generic_persistent_t<T>(a, cfg, st));
 }
 
 // ---- FP32 sweep of a d = 2 lattice with four legs of dimension 8 per vertex -----------------

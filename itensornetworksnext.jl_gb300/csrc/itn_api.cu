@@ -222,8 +222,9 @@ struct itn_ctx {
   std::vector<int> slot_dst, slot_eidx;  // per slot: destination vertex, undirected edge index
   DevBuf d_slot_dst, d_slot_eidx;
   // gradient work buffers
-  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_mu2, d_cot, d_adj, d_adjgrid;
-  bool no_persist_adj = false;  // itn_inject_fault(ITN_FAULT_NO_PERSISTENT_ADJOINT)
+  DevBuf d_grad, d_U, d_F, d_S, d_g, d_lam, d_mu, d_mu2, d_cot, d_adj, d_adjgrid, d_sweepgrid;
+  bool no_persist_adj = false;     // itn_inject_fault(ITN_FAULT_NO_PERSISTENT_ADJOINT)
+  bool no_persist_sweeps = false;  // itn_inject_fault(ITN_FAULT_NO_PERSISTENT_SWEEPS)
   DevBuf d_ckpt, d_seg;  // unrolled gradient: kept sweep states, recomputed segment
   std::map<std::vector<int64_t>, std::pair<std::vector<int>, std::shared_ptr<DevBuf>>> seq_plans;
 
@@ -528,6 +529,12 @@ int32_t itn_inject_fault(itn_ctx* c, int32_t kind, int64_t value) {
       return ITN_OK;
     case ITN_FAULT_NO_PERSISTENT_ADJOINT:
       c->no_persist_adj = value != 0;
+      return ITN_OK;
+    case ITN_FAULT_NO_PERSISTENT_SWEEPS:
+      c->no_persist_sweeps = value != 0;
+      for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+      c->graphs.clear();
+      c->graph_launches.clear();
       return ITN_OK;
   }
   return fail(c, ITN_ERR_ARG, "unknown fault kind %d", kind);
@@ -1315,9 +1322,35 @@ int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
 
 // Record `nsweeps` outer iterations of the parallel schedule onto the stream, starting
 // from buffer `start`.
+// The CUDA-core sweeps of a two-layer network as one persistent cooperative launch: one item
+// class, every item on its own resident CTA (small networks: the 12x12 and 16x16 lattices), and
+// not switched off by itn_inject_fault(ITN_FAULT_NO_PERSISTENT_SWEEPS).
+bool persistent_sweeps_fit(itn_ctx* c, const ParPlan& p, const itn_bp_opts* o) {
+  if (c->no_persist_sweeps || o->precision != ITN_PREC_NATIVE || c->layers != 2 || p.a.size() != 1) return false;
+  if (use_sweep_z3(c) || use_sweep_d8(c)) return false;
+  const GenericArgs& a = p.a[0][0];
+  const LaunchCfg& cf = p.cfg[0][0];
+  return a.n_items > 0 && cf.grid == a.n_items &&
+         (int64_t)generic_max_active(c->dtype, 2, cf.block, cf.smem) * c->sm_count >= a.n_items;
+}
+
 int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const itn_bp_opts* o,
                     int* launches) {
   const bool use_tol = o->tol >= 0;
+  if (nsweeps > 0 && c->d_sweepgrid.p && persistent_sweeps_fit(c, p, o)) {
+    // sweep t reads buffer (start + t) & 1: msg_buf = {that buffer, the other}
+    const int in = start & 1;
+    GenericArgs a = p.a[0][in];
+    a.pgrid = c->d_sweepgrid.as<SweepGrid>();
+    a.msg_buf[0] = c->d_msg[in].p;
+    a.msg_buf[1] = c->d_msg[in ^ 1].p;
+    a.nsweeps = nsweeps;
+    a.wait_ns = c->wait_ns;
+    a.fused_step = 0;
+    CK(launch_generic_persistent(c->dtype, a, p.cfg[0][in], c->stream));
+    *launches += 2;
+    return ITN_OK;
+  }
   if (o->precision != ITN_PREC_NATIVE && !use_tol) {
     // Without a convergence test the BF16 sweeps and then the split sweeps each run as
     // one persistent launch; a device that cannot host the cooperative grid gets one
@@ -1519,6 +1552,8 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   } else if (o->schedule == ITN_SCHED_PARALLEL && o->precision == ITN_PREC_NATIVE && !use_sweep_d8(c)) {
     if (int r = autotune_sweep(c)) return r;
     if (int r = make_par_plan(c, o, pplan)) return r;
+    // the persistent sweeps' barrier state (allocated here: no allocation inside a capture)
+    if (persistent_sweeps_fit(c, pplan, o)) CK(c->d_sweepgrid.ensure(sizeof(SweepGrid)));
   } else if (o->schedule == ITN_SCHED_SEQUENTIAL) {
     if (int r = make_seq_launches(c, plan, o, slaunch)) return r;
   }

@@ -55,11 +55,30 @@ struct GenericArgs {
   ConvState* conv;         // outer-loop state: early exit when done and the diff max
                            // (nullable: neither)
   int fused_step;          // non-zero: the last CTA performs the outer-loop step
+  // Persistent sweeps of the two-layer interpreter (pgrid != null; one work item per CTA,
+  // every CTA resident): the launch runs up to `nsweeps` parallel sweeps, sweep s reading
+  // msg_buf[s & 1] and writing msg_buf[(s + 1) & 1], with the site tensor staged once, a grid
+  // barrier and the outer-loop step (on every CTA, from the sweep's diff maximum) between sweeps.
+  struct SweepGrid* pgrid;
+  void* msg_buf[2];
+  int nsweeps;
+  unsigned long long wait_ns;  // limit of one grid-barrier wait (the run stops with pgrid->err)
+};
+
+// Grid barrier and per-sweep diff maxima of the persistent sweeps (three rotating slots:
+// slot s % 3 is filled in sweep s, read by every CTA after the barrier that ends it, and reset
+// by CTA 0 for sweep s + 2).  Initialised on the stream before each launch.
+struct SweepGrid {
+  unsigned count, gen;
+  unsigned long long dmax[3];
+  int nanf[3];
+  int err;
 };
 
 // Extra arguments of the dual-number (forward-mode) interpreter used by the gradient.
 struct AdjState;
 struct AdjGrid;
+struct SweepGrid;
 
 struct DualArgs {
   const void* tan_in;  // tangent per outgoing slot (mu_{u->v}); null = zero tangents
@@ -127,6 +146,9 @@ struct LaunchCfg {
 // bp_generic.cu
 size_t generic_smem_bytes(int dtype, const GenericArgs& a, int block, bool buffers_in_smem);
 cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st);
+// Up to a.nsweeps sweeps of a two-layer network as one cooperative launch (a.pgrid set,
+// cfg.grid == a.n_items CTAs, all resident); initialises a.pgrid on the stream first.
+cudaError_t launch_generic_persistent(int dtype, const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st);
 int generic_max_active(int dtype, int layers, int block, size_t smem);
 
 cudaError_t launch_edge_scalars(int dtype, int layers, const long long* moff, const int* rev,

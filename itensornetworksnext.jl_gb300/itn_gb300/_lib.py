@@ -20,7 +20,7 @@ F32, F64, C64, C128 = range(4)
 SCHED_PARALLEL, SCHED_SEQUENTIAL = 0, 1
 PREC_NATIVE, PREC_BF16, PREC_TF32, PREC_TF32X3 = 0, 1, 2, 3
 MSG_IDENTITY_NORMALIZED, MSG_IDENTITY, MSG_ONES = 0, 1, 2
-FAULT_WAIT_NS, FAULT_ALLOC, FAULT_STALL, FAULT_NO_PERSISTENT_ADJOINT = 1, 2, 3, 4
+FAULT_WAIT_NS, FAULT_ALLOC, FAULT_STALL, FAULT_NO_PERSISTENT_ADJOINT, FAULT_NO_PERSISTENT_SWEEPS = 1, 2, 3, 4, 5
 
 DTYPE_CODE = {np.dtype(np.float32): F32, np.dtype(np.float64): F64,
               np.dtype(np.complex64): C64, np.dtype(np.complex128): C128}

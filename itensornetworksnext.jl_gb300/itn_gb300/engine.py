@@ -231,9 +231,11 @@ class BPEngine:
         (1 / 0) makes one such wait look for a message that is never written; ``"alloc"``
         makes the next ``value`` device allocations on this thread fail;
         ``"no_persistent_adjoint"`` (1 / 0) runs the gradient's adjoint iteration as one launch
-        per iteration instead of one persistent launch."""
+        per iteration instead of one persistent launch; ``"no_persistent_sweeps"`` (1 / 0) the
+        same for the CUDA-core parallel sweeps of small networks."""
         k = {"wait_ns": L.FAULT_WAIT_NS, "alloc": L.FAULT_ALLOC, "stall": L.FAULT_STALL,
-             "no_persistent_adjoint": L.FAULT_NO_PERSISTENT_ADJOINT}[kind]
+             "no_persistent_adjoint": L.FAULT_NO_PERSISTENT_ADJOINT,
+             "no_persistent_sweeps": L.FAULT_NO_PERSISTENT_SWEEPS}[kind]
         self._check(self.lib.itn_inject_fault(self._ctx, k, int(value)))
 
     def tc_selftest(self) -> dict:

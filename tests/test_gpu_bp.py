@@ -406,3 +406,35 @@ def test_batched_size_classes_match_oracle():
         wide = np.complex128 if np.iscomplexobj(t) else np.float64
         ref, *_ = O.bp_run(g, t.astype(wide), m0.astype(wide), maxiter=8)
         assert msg_rel(g, m, ref) < tol
+
+
+@pytest.mark.parametrize("dtype,L_,D", [(np.float32, 16, 4), (np.float64, 12, 6), (np.complex128, 6, 3)])
+def test_persistent_sweeps_equal_per_sweep_launches(dtype, L_, D):
+    """Small two-layer networks sweep in one persistent cooperative launch (site tensors staged
+    once, a grid barrier and the outer-loop step between sweeps); the per-sweep launches run
+    the same arithmetic: same iterations, at_iteration, delta and messages, bit for bit, with a
+    tolerance (stopping inside a launch) and without one."""
+    rng = np.random.default_rng(44)
+    g = G.square_lattice(L_, L_, D, periodic=False, phys=2)
+    t = G.random_tensors(g, rng, dtype, G.peps_scale(g))
+    out = {}
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        for mode in (0, 1):
+            e.inject_fault("no_persistent_sweeps", mode)
+            e.init_messages()
+            r1 = e.run(maxiter=60, tol=1e-10)
+            m1 = e.messages().copy()
+            e.init_messages()
+            r2 = e.run(maxiter=7)
+            m2 = e.messages().copy()
+            out[mode] = (r1, m1, r2, m2)
+        e.inject_fault("no_persistent_sweeps", 0)
+    (a1, am1, a2, am2), (b1, bm1, b2, bm2) = out[0], out[1]
+    print(f"{L_}x{L_} D={D}: persistent {a1.device_ms:.3f} ms / per-sweep {b1.device_ms:.3f} ms "
+          f"({a1.iterations} sweeps to 1e-10)")
+    assert (a1.iterations, a1.at_iteration, a1.delta) == (b1.iterations, b1.at_iteration, b1.delta)
+    assert 1 < a1.iterations < 60 and a1.at_iteration == a1.iterations
+    assert a2.iterations == b2.iterations == 7
+    np.testing.assert_array_equal(am1, bm1)
+    np.testing.assert_array_equal(am2, bm2)
