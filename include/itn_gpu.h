@@ -333,9 +333,10 @@ int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int
  * ITN_ERR_TIMEOUT, with the device and the context still usable.  ITN_FAULT_ALLOC: the next
  * `value` device allocations the library makes on the calling thread fail, so the calls
  * making them return ITN_ERR_OOM (the host-side stand-in for exhausted device memory).
- * ITN_FAULT_STALL also applies to the gradient's persistent adjoint launch: one CTA leaves
- * before the first grid barrier, the others' waits (limit ITN_FAULT_WAIT_NS) run out and
- * itn_bp_grad returns ITN_ERR_TIMEOUT.  ITN_FAULT_NO_PERSISTENT_ADJOINT (value 1 / 0): the
+ * ITN_FAULT_STALL also applies to the grid barriers of the gradient's persistent adjoint
+ * launch and of the persistent CUDA-core sweeps: one CTA leaves before the first barrier,
+ * the others' waits (limit ITN_FAULT_WAIT_NS) run out and itn_bp_grad / itn_bp_run return
+ * ITN_ERR_TIMEOUT.  ITN_FAULT_NO_PERSISTENT_ADJOINT (value 1 / 0): the
  * adjoint iteration runs as one launch per iteration instead of one persistent launch (the
  * same arithmetic; lets a test compare the two).  ITN_FAULT_NO_PERSISTENT_SWEEPS (value 1 / 0):
  * the same for the CUDA-core parallel sweeps of small two-layer networks. */

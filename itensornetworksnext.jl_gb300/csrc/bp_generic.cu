@@ -593,6 +593,7 @@ __global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2
     }
     __syncthreads();
     if (!persist) break;
+    if (a.pstall && sw == 0 && blockIdx.x == 0) break;
     // end of a persistent sweep: wait for every CTA, then every CTA takes the outer-loop step
     // of conv_step from this sweep's diff maximum (the same decision everywhere)
     if (!grid_barrier(&a.pgrid->count, &a.pgrid->gen, &a.pgrid->err, a.wait_ns)) break;

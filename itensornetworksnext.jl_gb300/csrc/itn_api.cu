@@ -1346,6 +1346,7 @@ int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const 
     a.msg_buf[1] = c->d_msg[in ^ 1].p;
     a.nsweeps = nsweeps;
     a.wait_ns = c->wait_ns;
+    a.pstall = c->stall;
     a.fused_step = 0;
     CK(launch_generic_persistent(c->dtype, a, p.cfg[0][in], c->stream));
     *launches += 2;
@@ -1574,7 +1575,12 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   if (int r = ensure_pinned(c, kPinErrAt + 16)) return r;
   ConvState* h_state = static_cast<ConvState*>(c->h_pin);
   int* h_tcerr = reinterpret_cast<int*>(static_cast<unsigned char*>(c->h_pin) + kPinErrAt);
-  const int* d_tcerr = o->precision != ITN_PREC_NATIVE ? tc_err_ptr(c->tc) : nullptr;
+  // error flag of the sweep's bounded waits: the tensor-core sweep's, or the grid barrier's
+  // of persistent CUDA-core sweeps (reset by every persistent launch, so read per chunk)
+  const int* d_tcerr = o->precision != ITN_PREC_NATIVE ? tc_err_ptr(c->tc)
+                       : o->schedule == ITN_SCHED_PARALLEL && c->d_sweepgrid.p && persistent_sweeps_fit(c, pplan, o)
+                           ? &c->d_sweepgrid.as<SweepGrid>()->err
+                           : nullptr;
   *h_tcerr = 0;
   while (issued < cap) {
     const int n = (int)std::min<int64_t>(chunk, cap - issued);
@@ -1636,9 +1642,9 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
     total_ms += ms;
     launches += rec_launches;
     issued += n;
-    if (hs.done) break;
+    if (hs.done || (d_tcerr && *h_tcerr)) break;
   }
-  if (d_tcerr && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
+  if (d_tcerr && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "sweep: a bounded device wait gave up");
   // messages now live in buffer (cur + executed sweeps) for the parallel schedule
   if (o->schedule == ITN_SCHED_PARALLEL) c->cur = (c->cur + hs.iters) & 1;
   if (res) {
@@ -1658,7 +1664,7 @@ int bp_run_finish(itn_ctx* c, itn_bp_result* res) {
   c->pending.active = false;
   const ConvState* h_state = static_cast<const ConvState*>(c->h_pin);
   const int* h_tcerr = reinterpret_cast<const int*>(static_cast<const unsigned char*>(c->h_pin) + kPinErrAt);
-  if (c->pending.tc && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "tensor-core sweep: a bounded wait gave up");
+  if (c->pending.tc && *h_tcerr) return fail(c, ITN_ERR_TIMEOUT, "sweep: a bounded device wait gave up");
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   if (res) {

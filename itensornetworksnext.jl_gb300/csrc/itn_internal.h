@@ -63,6 +63,7 @@ struct GenericArgs {
   void* msg_buf[2];
   int nsweeps;
   unsigned long long wait_ns;  // limit of one grid-barrier wait (the run stops with pgrid->err)
+  int pstall;                  // fault injection: CTA 0 never arrives at the first barrier
 };
 
 // Grid barrier and per-sweep diff maxima of the persistent sweeps (three rotating slots:

@@ -227,8 +227,9 @@ class BPEngine:
 
     def inject_fault(self, kind: str, value: int):
         """Test hook (itn_inject_fault): ``"wait_ns"`` sets the elapsed-time limit of the
-        tensor-core sweep's waits on other items' messages (<= 0: the default); ``"stall"``
-        (1 / 0) makes one such wait look for a message that is never written; ``"alloc"``
+        persistent launches' device waits (the tensor-core sweep's waits on other items'
+        messages, the grid barriers; <= 0: the default); ``"stall"`` (1 / 0) makes one such
+        wait look for a message or arrival that never comes; ``"alloc"``
         makes the next ``value`` device allocations on this thread fail;
         ``"no_persistent_adjoint"`` (1 / 0) runs the gradient's adjoint iteration as one launch
         per iteration instead of one persistent launch; ``"no_persistent_sweeps"`` (1 / 0) the

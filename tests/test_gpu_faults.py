@@ -5,6 +5,9 @@
   waits for its own copies, frees its tensor memory and the call returns ITN_ERR_TIMEOUT.
   The same context then solves the network again without the fault and matches a fresh
   solve bit for bit (the GPU and the context stayed usable).
+* The same for the persistent CUDA-core sweep of a small network: one CTA never arrives at
+  the first grid barrier, the others' waits run out after 1 ms and the call returns
+  ITN_ERR_TIMEOUT; the context then solves again bit for bit.
 * A device allocation failure forced on the host makes the call that allocates return
   ITN_ERR_OOM; the context recovers once allocations succeed again.
 """
@@ -44,13 +47,43 @@ def test_tensor_core_wait_that_runs_out_reports_timeout():
         with pytest.raises(ItnError) as ei:
             e.run(maxiter=12, precision="bf16", split_sweeps=2)
         assert ei.value.status == L.ITN_ERR_TIMEOUT
-        assert "bounded wait" in str(ei.value)
+        assert "bounded device wait" in str(ei.value)
         # no fault, default limit: the same context solves the network again
         e.inject_fault("stall", 0)
         e.inject_fault("wait_ns", 0)
         e.init_messages()
         r = e.run(maxiter=12, precision="bf16", split_sweeps=2)
         assert r.iterations == 12
+        np.testing.assert_array_equal(e.messages(), want)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_persistent_sweep_barrier_that_runs_out_reports_timeout(dtype):
+    g = G.square_lattice(12, 12, 4, periodic=False, phys=2)
+    t = G.random_tensors(g, np.random.default_rng(9), dtype, G.peps_scale(g))
+    with BPEngine(g) as ref:
+        ref.set_tensors(t)
+        ref.init_messages()
+        ref.run(maxiter=40, tol=1e-10)
+        want = ref.messages()
+    with BPEngine(g) as e:
+        e.set_tensors(t)
+        e.inject_fault("wait_ns", 1_000_000)
+        e.inject_fault("stall", 1)
+        e.init_messages()
+        with pytest.raises(ItnError) as ei:
+            e.run(maxiter=40, tol=1e-10)
+        assert ei.value.status == L.ITN_ERR_TIMEOUT
+        assert "bounded device wait" in str(ei.value)
+        e.init_messages()
+        with pytest.raises(ItnError) as ei:  # without a tolerance: one chunk of 5 sweeps
+            e.run(maxiter=5)
+        assert ei.value.status == L.ITN_ERR_TIMEOUT
+        e.inject_fault("stall", 0)
+        e.inject_fault("wait_ns", 0)
+        e.init_messages()
+        r = e.run(maxiter=40, tol=1e-10)
+        assert 1 < r.iterations < 40
         np.testing.assert_array_equal(e.messages(), want)
 
 
