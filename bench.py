@@ -622,7 +622,10 @@ def run_case(name, device=0):
     6x6 D=3 norm network (permute_kernel, gemm_cc_kernel<double>) in the greedy and the sweep
     order; exact6_sweep = the sweep order alone, twice (permute_tensor32_kernel,
     gemm_thin_kernel<double>); padded = 30-sweep mixed solves of the 16x16 D=4 and 12x12 D=6 open
-    lattices on the zero-padded tensor-core sweep (bp_tc_kernel with PAD, one launch per sweep)."""
+    lattices on the zero-padded tensor-core sweep (bp_tc_kernel with PAD, one launch per sweep);
+    open16 = FP32 and FP64 solves of the 16x16 D=4 open lattice to tol 1e-10, twice each with
+    the sweeps as one persistent launch (bp2_kernel with a grid barrier), then once with one
+    launch per sweep."""
     from itn_gb300 import BPEngine
     from itn_gb300 import graphs as G
     if name in ("d8", "mixed"):
@@ -675,6 +678,18 @@ def run_case(name, device=0):
                     e.init_messages()
                     r = e.run(maxiter=SWEEPS, precision="bf16", split_sweeps=SPLIT_SWEEPS)
                 print(f"padded {L}x{L} D={D} bf16 mixed: device ms {r.device_ms:.4f}, launches {r.kernel_launches}")
+    elif name == "open16":
+        g = G.square_lattice(16, 16, 4, periodic=False, phys=2)
+        t = G.random_tensors(g, np.random.default_rng(16), np.float64, G.peps_scale(g))
+        for dt in (np.float32, np.float64):
+            with BPEngine(g, device=device) as e:
+                e.set_tensors(t.astype(dt))
+                for mode in (0, 0, 1):
+                    e.inject_fault("no_persistent_sweeps", mode)
+                    e.init_messages()
+                    r = e.run(maxiter=50, tol=1e-10)
+                    print(f"open16 {np.dtype(dt).name} {'per-sweep' if mode else 'persistent'}: "
+                          f"{r.iterations} sweeps, device ms {r.device_ms:.4f}, launches {r.kernel_launches}")
     elif name == "exact6_sweep":
         from itn_gb300.contract import contract_network, norm_network_tensors
         g6 = G.square_lattice(6, 6, 3, periodic=False, phys=2)
@@ -833,7 +848,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default=os.environ.get("ITN_BENCH_PRECISION", "bf16"),
                     choices=["native", "bf16", "tf32", "tf32x3"])
-    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6", "exact6_sweep",
+    ap.add_argument("--case", default=None, choices=["d8", "mixed", "grad", "gate", "contract", "batched", "exact6", "exact6_sweep", "open16",
                                                         "padded"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

@@ -1134,6 +1134,7 @@ int autotune_sweep(itn_ctx* c) {
   const int cands[3] = {64, 128, 256};
   float best = 1e30f;
   int best_b = 0;
+  DevBuf scratch;  // second message buffer of the persistent trials
   for (int b : cands) {
     c->tuned_block[c->dtype] = b;
     GenericArgs a;
@@ -1152,6 +1153,43 @@ int autotune_sweep(itn_ctx* c) {
       CK(cudaEventSynchronize(c->ev1));
       CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
       if (rep > 0) ms = std::min(ms, t);
+    }
+    // A shape that gives every item its own resident CTA runs the solve's sweeps as one
+    // persistent launch (persistent_sweeps_fit): its time is that form's, per sweep, over
+    // kTuneSweeps sweeps on copies of the current messages (the current buffer is not written).
+    // The choice does not depend on ITN_FAULT_NO_PERSISTENT_SWEEPS, so both forms run one shape.
+    constexpr int kTuneSweeps = 8;
+    if (c->layers == 2 && c->par_classes.size() == 1 && cfg.grid == a.n_items && a.n_items > 0 &&
+        (int64_t)generic_max_active(c->dtype, 2, cfg.block, cfg.smem) * c->sm_count >= a.n_items) {
+      const size_t mbytes = (size_t)c->moff[c->nslots] * dtype_size(c->dtype);
+      CK(scratch.ensure(mbytes));
+      CK(c->d_sweepgrid.ensure(sizeof(SweepGrid)));
+      GenericArgs pa = a;
+      pa.conv = nullptr;
+      pa.slot_diff = nullptr;
+      pa.fused_step = 0;
+      pa.normalize = 1;
+      pa.pgrid = c->d_sweepgrid.as<SweepGrid>();
+      pa.msg_buf[0] = c->d_msg[c->cur ^ 1].p;
+      pa.msg_buf[1] = scratch.p;
+      pa.nsweeps = kTuneSweeps;
+      pa.wait_ns = c->wait_ns;
+      pa.pstall = 0;
+      float pms = 1e30f;
+      for (int rep = 0; rep < 3; ++rep) {
+        float t = 0.f;
+        CK(cudaMemcpyAsync(c->d_msg[c->cur ^ 1].p, c->d_msg[c->cur].p, mbytes, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaEventRecord(c->ev0, c->stream));
+        CK(launch_generic_persistent(c->dtype, pa, cfg, c->stream));
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        CK(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+        if (rep > 0) pms = std::min(pms, t / kTuneSweeps);
+      }
+      SweepGrid hg;
+      CK(cudaMemcpy(&hg, c->d_sweepgrid.p, sizeof(hg), cudaMemcpyDeviceToHost));
+      if (hg.err) return fail(c, ITN_ERR_TIMEOUT, "autotune: a grid-barrier wait of the persistent sweep gave up");
+      ms = pms;
     }
     if (ms < best) {
       best = ms;
