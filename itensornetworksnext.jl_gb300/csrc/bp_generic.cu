@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "itn_common.cuh"
 #include "itn_conv.cuh"
@@ -500,10 +501,9 @@ __host__ __device__ inline SmemLayout smem_layout(const GenericArgs& a, int bloc
 }
 
 // ---- the two-layer interpreter ---------------------------------------------------------
-template <typename T>
-// complex64 caps registers at 128 so that small CTAs can co-reside (its D = 8 paths spill a
-// little); the other types keep their full register budget
-__global__ void __launch_bounds__(256, (is_cplx<T>::value && sizeof(T) == 8) ? 2 : 1) bp2_kernel(GenericArgs a) {
+// MINB = 2 caps registers at 128 (see bp2_kernel_for)
+template <typename T, int MINB>
+__global__ void __launch_bounds__(256, MINB) bp2_kernel(GenericArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout L = smem_layout<T>(a, blockDim.x, a.gscratch == nullptr);
   T* bufs = a.gscratch ? reinterpret_cast<T*>(a.gscratch) + (size_t)blockIdx.x * a.nbuf * a.buf_elems
@@ -1420,11 +1420,28 @@ __global__ void reset_state_kernel(ConvState* s, double tol, int use_tol) {
 
 __global__ void step_check_kernel(ConvState* s) { conv_step(s); }
 
+// The two-layer interpreter for a CTA size.  complex64 always caps registers at 128, so that
+// small CTAs co-reside (its D = 8 paths spill a little); float takes the capped variant (no
+// spills) for CTAs of 128 threads or more (four resident CTAs of 128 threads per SM instead of
+// three, so that every item of a 16x16 lattice has its own CTA and the sweeps can run as one
+// persistent launch) and its full register budget at 64 threads; double and complex128 keep
+// their full budget (capped at 128 they spill).
+template <typename T>
+void (*bp2_kernel_for(int block))(GenericArgs) {
+  if constexpr (std::is_same<T, c64>::value) {
+    return bp2_kernel<T, 2>;
+  } else if constexpr (std::is_same<T, float>::value) {
+    return block >= 128 ? bp2_kernel<T, 2> : bp2_kernel<T, 1>;
+  } else {
+    return bp2_kernel<T, 1>;
+  }
+}
+
 template <typename T>
 cudaError_t launch_generic_t(const GenericArgs& a, const LaunchCfg& cfg, cudaStream_t st) {
   if (cfg.grid <= 0 || a.n_items <= 0) return cudaSuccess;
   if (a.layers == 2) {
-    auto k = bp2_kernel<T>;
+    auto k = bp2_kernel_for<T>(cfg.block);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess) return e;
     k<<<cfg.grid, cfg.block, cfg.smem, st>>>(a);
@@ -1443,10 +1460,11 @@ int max_active_t(int layers, int block, size_t smem) {
   if (layers == 2) {
     // complex64 (small CTAs, capped registers): all of the unified L1 / shared memory as
     // shared memory, so that more CTAs co-reside; the real types keep the default split
+    auto k = bp2_kernel_for<T>(block);
     if (is_cplx<T>::value && sizeof(T) == 8)
-      cudaFuncSetAttribute(bp2_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(bp2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp2_kernel<T>, block, smem);
+      cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem);
   } else {
     cudaFuncSetAttribute(bp1_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp1_kernel<T>, block, smem);
@@ -1507,7 +1525,7 @@ cudaError_t launch_generic_persistent_t(const GenericArgs& a, const LaunchCfg& c
   sweep_grid_init_kernel<<<1, 32, 0, st>>>(a.pgrid);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  auto k = bp2_kernel<T>;
+  auto k = bp2_kernel_for<T>(cfg.block);
   e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
