@@ -1600,11 +1600,13 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   int launches = 1;
   // Without a tolerance the whole run is one graph.  With one, sweeps after convergence
   // are no-op launches (~2 us each), so a CUDA-core run goes in growing chunks (16, 32,
-  // 64, 64, ...) with one host check of the done flag per chunk.  Tensor-core runs keep one
-  // graph per maxiter: their split sweeps are the last ones of the graph.
+  // 64, 64, ...) with one host check of the done flag per chunk; a persistent launch stops
+  // at the converged sweep itself, so its chunks are 64 sweeps from the start.  Tensor-core
+  // runs keep one graph per maxiter: their split sweeps are the last ones of the graph.
   const int64_t cap = o->maxiter >= 0 ? o->maxiter : 1000000;
   const bool grow = use_tol && (o->precision == ITN_PREC_NATIVE || o->maxiter < 0);
-  int chunk = grow ? 16 : (o->maxiter >= 0 ? (int)std::min<int64_t>(cap, 1 << 30) : 64);
+  const bool persistent = o->schedule == ITN_SCHED_PARALLEL && c->d_sweepgrid.p && persistent_sweeps_fit(c, pplan, o);
+  int chunk = grow ? (persistent ? 64 : 16) : (o->maxiter >= 0 ? (int)std::min<int64_t>(cap, 1 << 30) : 64);
   int64_t issued = 0;
   float total_ms = 0.f;
   ConvState hs;
@@ -1616,9 +1618,8 @@ int bp_run_impl(itn_ctx* c, const itn_bp_opts* o, itn_bp_result* res, bool defer
   // error flag of the sweep's bounded waits: the tensor-core sweep's, or the grid barrier's
   // of persistent CUDA-core sweeps (reset by every persistent launch, so read per chunk)
   const int* d_tcerr = o->precision != ITN_PREC_NATIVE ? tc_err_ptr(c->tc)
-                       : o->schedule == ITN_SCHED_PARALLEL && c->d_sweepgrid.p && persistent_sweeps_fit(c, pplan, o)
-                           ? &c->d_sweepgrid.as<SweepGrid>()->err
-                           : nullptr;
+                       : persistent ? &c->d_sweepgrid.as<SweepGrid>()->err
+                                    : nullptr;
   *h_tcerr = 0;
   while (issued < cap) {
     const int n = (int)std::min<int64_t>(chunk, cap - issued);
