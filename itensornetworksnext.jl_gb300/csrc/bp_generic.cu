@@ -363,36 +363,36 @@ __device__ void final_rt(const T* __restrict__ src, const T* __restrict__ A, int
   __syncthreads();
 }
 
-// Normalise out (D*D entries in shared memory) by its sum, store it to global memory
-// and, when requested, record the convergence value against the previous message.
-// Executed by warp 0.
-// Grid-wide barrier of a persistent cooperative launch (every CTA resident): each CTA arrives
-// once, the last to arrive advances the generation.  The wait is bounded by elapsed time
-// (globaltimer, checked every 64 polls) and gives up early once another CTA has raised *err;
-// false means the launch must stop.
-__device__ bool grid_barrier(unsigned* count, unsigned* gen_p, int* err, unsigned long long wait_ns) {
+// Grid-wide barrier number k (1, 2, ...) of a persistent cooperative launch (every CTA
+// resident): each CTA adds one arrival to a 64-bit counter that is zeroed before the launch
+// and never reset during it, and barrier k is passed once the counter has reached
+// k * gridDim.x.  The last CTA to arrive sees that in its own atomic's result and leaves at
+// once; the others poll the counter.  The fence before the arrival (after the CTA barrier, so
+// it covers every thread's writes) and the one after the wait order the launch's global
+// writes across the barrier.  The wait is bounded by elapsed time (globaltimer, checked every
+// 64 polls, when it also gives up once another CTA has raised *err); false means the launch
+// must stop.
+__device__ bool grid_barrier(unsigned long long* arrivals, unsigned k, int* err, unsigned long long wait_ns) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned* gen = gen_p;
-    const unsigned g0 = *gen;
+    const unsigned long long target = (unsigned long long)k * gridDim.x;
     __threadfence();
-    if (atomicAdd(count, 1u) == gridDim.x - 1) {
-      *count = 0;
-      __threadfence();
-      atomicAdd(gen_p, 1u);
-    } else {
+    if (atomicAdd(arrivals, 1ull) + 1 < target) {
+      volatile unsigned long long* cnt = arrivals;
       const uint64_t t0 = ptx::globaltimer();
-      for (unsigned polls = 1; *gen == g0; ++polls) {
-        if (*reinterpret_cast<volatile int*>(err)) {
-          ok = 0;
-          break;
-        }
-        if ((polls & 63) == 0 && ptx::globaltimer() - t0 > wait_ns) {
-          atomicExch(err, 1);
-          ok = 0;
-          break;
+      for (unsigned polls = 1; *cnt < target; ++polls) {
+        if ((polls & 63) == 0) {
+          if (*reinterpret_cast<volatile int*>(err)) {
+            ok = 0;
+            break;
+          }
+          if (ptx::globaltimer() - t0 > wait_ns) {
+            atomicExch(err, 1);
+            ok = 0;
+            break;
+          }
         }
         __nanosleep(64);
       }
@@ -404,6 +404,9 @@ __device__ bool grid_barrier(unsigned* count, unsigned* gen_p, int* err, unsigne
   return ok_s != 0;
 }
 
+// Normalise out (D*D entries in shared memory) by its sum, store it to global memory
+// and, when requested, record the convergence value against the previous message.
+// Executed by warp 0.
 template <typename T>
 __device__ void store_message(const GenericArgs& a, const T* out, int n, int slot, const void* msg_in,
                               void* msg_out, unsigned long long* dmax, int* nanf) {
@@ -558,15 +561,6 @@ __global__ void __launch_bounds__(256, MINB) bp2_kernel(GenericArgs a) {
     void* io_out = persist ? a.msg_buf[(sw + 1) & 1] : a.msg_out;
     unsigned long long* io_dmax = persist ? &a.pgrid->dmax[sw % 3] : a.conv ? &a.conv->dmax : nullptr;
     int* io_nan = persist ? &a.pgrid->nanf[sw % 3] : a.conv ? &a.conv->nan_flag : nullptr;
-    if (persist && sw > 0) {
-      // the site tensor stays staged; this sweep's incoming messages
-      const T* mk = reinterpret_cast<const T*>(io_in);
-      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
-        const int l = staged_leg(meta, j);
-        msgs[j] = mk[meta->msrc[l] + (j - meta->moffs[l])];
-      }
-      __syncthreads();
-    }
     const int nops = (int)prog[0];
     for (int q = 1; q <= nops; ++q) {
       const unsigned op = prog[q];
@@ -596,10 +590,19 @@ __global__ void __launch_bounds__(256, MINB) bp2_kernel(GenericArgs a) {
     if (a.pstall && sw == 0 && blockIdx.x == 0) break;
     // end of a persistent sweep: wait for every CTA, then every CTA takes the outer-loop step
     // of conv_step from this sweep's diff maximum (the same decision everywhere)
-    if (!grid_barrier(&a.pgrid->count, &a.pgrid->gen, &a.pgrid->err, a.wait_ns)) break;
+    if (!grid_barrier(&a.pgrid->arrivals, sw + 1, &a.pgrid->err, a.wait_ns)) break;
     const int k3 = sw % 3;
     const int iter = base_iter + sw + 1;
     const bool last = sw + 1 >= a.nsweeps;
+    if (!last) {
+      // the next sweep's incoming messages (the site tensor stays staged), loaded before the
+      // diff maximum is read so that the two reads overlap; unused if the run stops here
+      const T* mk = reinterpret_cast<const T*>(a.msg_buf[(sw + 1) & 1]);
+      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+        const int l = staged_leg(meta, j);
+        msgs[j] = mk[meta->msrc[l] + (j - meta->moffs[l])];
+      }
+    }
     double delta = 0.0;
     bool conv_now = false;
     if (a.conv && a.conv->use_tol) {
@@ -624,6 +627,7 @@ __global__ void __launch_bounds__(256, MINB) bp2_kernel(GenericArgs a) {
       a.pgrid->nanf[(sw + 2) % 3] = 0;
       __threadfence();
     }
+    __syncthreads();  // the restaged messages
     if (last || conv_now) break;
     }  // persistent sweeps
   }
@@ -713,9 +717,9 @@ __device__ __forceinline__ void dispatch_absorb_dual(const T* src, const T* srcT
 
 __device__ void adj_step_dev(AdjState* s);
 
-// Grid-wide barrier of the persistent adjoint loop (see grid_barrier).
-__device__ bool adj_grid_barrier(AdjGrid* gr, unsigned long long wait_ns) {
-  return grid_barrier(&gr->count, &gr->gen, &gr->err, wait_ns);
+// Grid-wide barrier k of the persistent adjoint loop (see grid_barrier).
+__device__ bool adj_grid_barrier(AdjGrid* gr, unsigned k, unsigned long long wait_ns) {
+  return grid_barrier(&gr->arrivals, k, &gr->err, wait_ns);
 }
 
 // MINB = 2: at most 128 registers, so that two CTAs of 256 threads share an SM (the
@@ -864,7 +868,7 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
     __threadfence();
     // (fault injection: CTA 0 leaves without arriving, so the others' waits run out)
     if (d.stall && iter == 0 && blockIdx.x == 0) break;
-    if (!adj_grid_barrier(d.grid, d.wait_ns)) break;
+    if (!adj_grid_barrier(d.grid, iter + 1, d.wait_ns)) break;
     const double dm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->dmax[k3])),
                  lm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->lmax[k3]));
     const double r = lm > 0 ? dm / lm : 0.0;
@@ -1509,8 +1513,7 @@ cudaError_t launch_generic(int dtype, const GenericArgs& a, const LaunchCfg& cfg
 
 __global__ void sweep_grid_init_kernel(SweepGrid* g) {
   if (threadIdx.x == 0) {
-    g->count = 0;
-    g->gen = 0;
+    g->arrivals = 0;
     for (int k = 0; k < 3; ++k) {
       g->dmax[k] = enc_double(-INFINITY);
       g->nanf[k] = 0;

@@ -70,7 +70,7 @@ struct GenericArgs {
 // slot s % 3 is filled in sweep s, read by every CTA after the barrier that ends it, and reset
 // by CTA 0 for sweep s + 2).  Initialised on the stream before each launch.
 struct SweepGrid {
-  unsigned count, gen;
+  unsigned long long arrivals;  // grid-barrier arrivals of the launch
   unsigned long long dmax[3];
   int nanf[3];
   int err;
@@ -112,12 +112,12 @@ struct DualArgs {
   int stall;                   // fault injection: CTA 0 never arrives at the first barrier
 };
 
-// Device state of the persistent adjoint loop (zeroed before each launch): the grid barrier
-// (arrivals and generation) and the maxima of the iterations in three rotating slots (slot
+// Device state of the persistent adjoint loop (zeroed before each launch): the grid barrier's
+// arrival count and the maxima of the iterations in three rotating slots (slot
 // k % 3 is filled in iteration k, read by every CTA after the barrier that ends it, and
 // cleared by CTA 0 for iteration k + 2 -- by then every CTA has read it).
 struct AdjGrid {
-  unsigned count, gen;
+  unsigned long long arrivals;  // grid-barrier arrivals of the launch
   unsigned long long dmax[3], lmax[3];
   int err;  // a grid-barrier wait ran out
   int pad_;
