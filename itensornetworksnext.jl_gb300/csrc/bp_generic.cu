@@ -779,17 +779,6 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
     __syncthreads();
     for (int iter = 0;; ++iter) {
     T* const mu_next = reinterpret_cast<T*>(persist ? d.mu_buf[(iter + 1) & 1] : d.mu_next);
-    if (persist && iter > 0) {
-      // the site tensor and the value messages stay staged; this iteration's tangents
-      const T* tk = reinterpret_cast<const T*>(d.mu_buf[iter & 1]);
-      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
-        const int l = staged_leg(meta, j);
-        const int Dl = meta->dims[l], jl = j - meta->moffs[l];
-        const int jj = d.transpose ? (jl % Dl) * Dl + jl / Dl : jl;
-        msgs[half + j] = tk[meta->tsrc[l] + jj];
-      }
-      __syncthreads();
-    }
     const int nops = (int)prog[0];
     for (int q = 1; q <= nops; ++q) {
       const unsigned op = prog[q];
@@ -869,6 +858,18 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
     // (fault injection: CTA 0 leaves without arriving, so the others' waits run out)
     if (d.stall && iter == 0 && blockIdx.x == 0) break;
     if (!adj_grid_barrier(d.grid, iter + 1, d.wait_ns)) break;
+    {
+      // the next iteration's tangents (the site tensor and the value messages stay staged),
+      // loaded before the maxima are read so that the two reads overlap; unused if the loop
+      // stops here
+      const T* tk = reinterpret_cast<const T*>(d.mu_buf[(iter + 1) & 1]);
+      for (int j = threadIdx.x; j < meta->mtot; j += blockDim.x) {
+        const int l = staged_leg(meta, j);
+        const int Dl = meta->dims[l], jl = j - meta->moffs[l];
+        const int jj = d.transpose ? (jl % Dl) * Dl + jl / Dl : jl;
+        msgs[half + j] = tk[meta->tsrc[l] + jj];
+      }
+    }
     const double dm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->dmax[k3])),
                  lm = dec_double(*reinterpret_cast<volatile unsigned long long*>(&d.grid->lmax[k3]));
     const double r = lm > 0 ? dm / lm : 0.0;
@@ -883,6 +884,7 @@ __global__ void __launch_bounds__(256, MINB) bp2_dual_kernel(GenericArgs a, Dual
       d.grid->dmax[(iter + 2) % 3] = d.grid->lmax[(iter + 2) % 3] = enc_double(0.0);
       __threadfence();
     }
+    __syncthreads();  // the restaged tangents
     if (stop) break;
     }  // persistent iterations
   }
