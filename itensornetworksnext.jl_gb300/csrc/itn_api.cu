@@ -1176,7 +1176,7 @@ int autotune_sweep(itn_ctx* c) {
       pa.wait_ns = c->wait_ns;
       pa.pstall = 0;
       float pms = 1e30f;
-      for (int rep = 0; rep < 3; ++rep) {
+      for (int rep = 0; rep < 5; ++rep) {  // the best of four after a warm-up launch
         float t = 0.f;
         CK(cudaMemcpyAsync(c->d_msg[c->cur ^ 1].p, c->d_msg[c->cur].p, mbytes, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaEventRecord(c->ev0, c->stream));
