@@ -325,8 +325,10 @@ int32_t itn_logz_static_scratch(int32_t device, void *stream, int32_t dtype, int
                                 char *errbuf, int32_t errbuf_len);
 
 /* Fault injection for tests, with no counterpart in the reference (it has no device code
- * to fail).  ITN_FAULT_WAIT_NS: elapsed-time limit in ns of the tensor-core sweep's bounded
- * waits on other items' messages (value <= 0 restores the default of 2 s).
+ * to fail).  ITN_FAULT_WAIT_NS: elapsed-time limit in ns of the bounded device waits of the
+ * persistent launches (the tensor-core sweep's waits on other items' messages, the grid
+ * barriers of the CUDA-core sweeps and of the adjoint; value <= 0 restores the default of
+ * 2 s).
  * ITN_FAULT_STALL (value 1 / 0): in the persistent tensor-core sweeps, one such wait looks
  * for a message that is never written, so it runs out after the limit; the kernel then stops
  * early, waits for its own copies, releases its resources and the call returns

@@ -86,3 +86,22 @@ def test_gate_descriptor_layout(lib_built):
     lib = L.load(lib_built)
     assert lib.itn_apply_gates(None, 1, 0, None, None, 0, None, 0, None, 0, 0, 0.0, 0, None, 0, None, 0,
                                None, None) == L.ITN_ERR_ARG
+
+
+def test_header_constants_match_python_binding():
+    """Every enum constant of the header (status codes, dtypes, schedules, precisions,
+    message initialisations, fault kinds) has the same value in the ctypes binding, under
+    its own name (ITN_OK, ITN_ERR_*) or without the ITN_ prefix (F32, PREC_*, FAULT_*...)."""
+    from itn_gb300 import _lib as L
+    txt = open(HEADER).read()
+    consts = {}
+    for body in re.findall(r"enum\s*\{([^}]*)\}", txt):
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        for name, val in re.findall(r"(ITN_\w+)\s*=\s*(\d+)", body):
+            consts[name] = int(val)
+    assert len(consts) >= 26 and "ITN_FAULT_NO_PERSISTENT_SWEEPS" in consts
+    for name, val in consts.items():
+        py = getattr(L, name, None)
+        if py is None:
+            py = getattr(L, name[len("ITN_"):], None)
+        assert py == val, (name, val, py)
