@@ -1358,8 +1358,6 @@ int make_par_plan(itn_ctx* c, const itn_bp_opts* o, ParPlan& p) {
   return ITN_OK;
 }
 
-// Record `nsweeps` outer iterations of the parallel schedule onto the stream, starting
-// from buffer `start`.
 // The CUDA-core sweeps of a two-layer network as one persistent cooperative launch: one item
 // class, every item on its own resident CTA (small networks: the 12x12 and 16x16 lattices), and
 // not switched off by itn_inject_fault(ITN_FAULT_NO_PERSISTENT_SWEEPS).
@@ -1372,6 +1370,8 @@ bool persistent_sweeps_fit(itn_ctx* c, const ParPlan& p, const itn_bp_opts* o) {
          (int64_t)generic_max_active(c->dtype, 2, cf.block, cf.smem) * c->sm_count >= a.n_items;
 }
 
+// Record `nsweeps` outer iterations of the parallel schedule onto the stream, starting
+// from buffer `start`.
 int record_parallel(itn_ctx* c, const ParPlan& p, int start, int nsweeps, const itn_bp_opts* o,
                     int* launches) {
   const bool use_tol = o->tol >= 0;
