@@ -1893,7 +1893,7 @@ int autotune_dual(itn_ctx* c, const void* m) {
     d.tan_in = c->d_mu.p;
     d.tan_out = c->d_cot.p;
     float ms = 1e30f;
-    for (int rep = 0; rep < 4; ++rep) {  // the first launch warms the caches
+    for (int rep = 0; rep < 7; ++rep) {  // the first launch warms the caches; best of six
       float t = 0.f;
       CK(cudaEventRecord(c->ev0, c->stream));
       CK(launch_dual(c->dtype, a, d, cfg, c->stream));
