@@ -433,6 +433,8 @@ def test_persistent_sweeps_equal_per_sweep_launches(dtype, L_, D):
     (a1, am1, a2, am2), (b1, bm1, b2, bm2) = out[0], out[1]
     print(f"{L_}x{L_} D={D}: persistent {a1.device_ms:.3f} ms / per-sweep {b1.device_ms:.3f} ms "
           f"({a1.iterations} sweeps to 1e-10)")
+    # the persistent form ran: one sweep launch (plus its barrier set-up) instead of one per sweep
+    assert a1.kernel_launches < b1.kernel_launches
     assert (a1.iterations, a1.at_iteration, a1.delta) == (b1.iterations, b1.at_iteration, b1.delta)
     assert 1 < a1.iterations < 60 and a1.at_iteration == a1.iterations
     assert a2.iterations == b2.iterations == 7
